@@ -1,0 +1,298 @@
+"""CPU oracle for the Anime4KCPP upscaling path -- TEST INFRASTRUCTURE ONLY.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` may use this package, and only as the checker or the timed CPU
+baseline.  The product library (``anime4kcpp_gb300``) never imports it.
+
+Two back ends:
+
+* ``liboracle.so`` -- this project's C restatement of the reference CPU path
+  (``acoracle.c``; FP32 in the reference's Generic operation order plus an FP64
+  twin).  Built by ``make -C oracle`` on any host.
+* ``_ref/libacref.so`` -- the reference's own CPU processor compiled from its
+  sources by ``make -C oracle ref``.  Exists only where the reference sources
+  were present at build time; never shipped as product.
+
+The pipeline function :func:`process` restates ``Processor::process``
+(core/src/processor/Processor.cpp:199-276) on top of the C primitives.
+"""
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+WEIGHTS_BLOB = os.path.join(ROOT, "anime4kcpp_gb300", "weights", "acnet_legacy.bin")
+
+U8, U16, F32 = 0x001, 0x002, 0x204
+_TYPE_OF = {np.dtype(np.uint8): U8, np.dtype(np.uint16): U16, np.dtype(np.float32): F32}
+_DTYPE_OF = {U8: np.uint8, U16: np.uint16, F32: np.float32}
+
+RESIZE_POINT, RESIZE_CATMULL_ROM, RESIZE_BILINEAR = 0, 1, 16
+ARNET_SEED_BASE = 0x41524E6574000000
+
+_lock = threading.Lock()
+_lib = None
+_ref = None
+
+
+def build(force=False):
+    """Compile liboracle.so with make (fast; a single C file)."""
+    so = os.path.join(HERE, "liboracle.so")
+    if force or not os.path.exists(so) or os.path.getmtime(so) < os.path.getmtime(os.path.join(HERE, "acoracle.c")):
+        subprocess.check_call(["make", "-s", "-C", HERE, "all"])
+    return so
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            so = build()
+            L = ctypes.CDLL(so)
+            vp, i, f, d, fp, dp = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p
+            L.orc_acnet_legacy_x2.argtypes = [vp, i, i, i, i, vp, i, fp, fp, i]
+            L.orc_acnet_legacy_x2_f64.argtypes = [vp, i, i, i, i, dp, fp, fp, i]
+            L.orc_arnet_x2.argtypes = [vp, i, i, i, i, vp, i, fp, fp, fp, i, i]
+            L.orc_arnet_x2_f64.argtypes = [vp, i, i, i, i, dp, fp, fp, fp, i, i]
+            L.orc_rgb2yuv.argtypes = [vp, i, i, i, i, i, vp, i, vp, i]
+            L.orc_yuv2rgb.argtypes = [vp, i, vp, i, i, i, i, i, vp, i]
+            L.orc_resize.argtypes = [vp, i, i, i, i, i, vp, i, i, i, i]
+            L.orc_resize_coeffs.argtypes = [i, i, i, vp, vp, i]
+            L.orc_arnet_synth.argtypes = [i, ctypes.c_uint64, fp, fp, fp]
+            for fn in ("orc_acnet_legacy_x2", "orc_acnet_legacy_x2_f64", "orc_arnet_x2", "orc_arnet_x2_f64",
+                       "orc_rgb2yuv", "orc_yuv2rgb", "orc_resize", "orc_resize_coeffs", "orc_arnet_synth"):
+                getattr(L, fn).restype = ctypes.c_int
+            _lib = L
+    return _lib
+
+
+def ref_available():
+    return os.path.exists(os.path.join(HERE, "_ref", "libacref.so"))
+
+
+def ref():
+    """The reference's own CPU processor (only where it was compiled)."""
+    global _ref
+    with _lock:
+        if _ref is None:
+            R = ctypes.CDLL(os.path.join(HERE, "_ref", "libacref.so"))
+            vp, i = ctypes.c_void_p, ctypes.c_int
+            R.acref_process.argtypes = [ctypes.c_char_p, i, vp, i, i, i, i, i, vp, i, i, i, ctypes.c_double]
+            R.acref_process.restype = i
+            R.acref_name.argtypes = [ctypes.c_char_p, i]
+            R.acref_name.restype = ctypes.c_char_p
+            R.acref_rgb2yuv.argtypes = [vp, i, i, i, i, i, vp, i, vp, i]
+            R.acref_yuv2rgb.argtypes = [vp, i, vp, i, i, i, i, i, vp, i]
+            _ref = R
+    return _ref
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _plane(a):
+    a = np.ascontiguousarray(a)
+    if a.dtype not in _TYPE_OF:
+        raise TypeError("unsupported dtype %s" % a.dtype)
+    return a
+
+
+# ------------------------------------------------------------------ models
+
+def parse_model(name):
+    """Model string -> (family, variant) following Processor.cpp:26-187 for the
+    ACNetLegacy and ARNet families.  Returns ("acnet_legacy", idx 0..4) with
+    0=GAN, 1..4=HDN0..3, or ("arnet", (blocks, kind))."""
+    s = (name or "").lower()
+    if "arnet" in s:
+        box = "box" in s
+        hdn = "hdn" in s
+        blocks = 8
+        for tag, b in (("b8", 8), ("b16", 16), ("b32", 32), ("b64", 64)):
+            if tag in s:
+                blocks = b
+                break
+        kind = (2 if box else 0) + (1 if hdn else 0)
+        return "arnet", (blocks, kind)
+    if "acnet" in s and "legacy" in s:
+        idx = 0
+        if "hdn" in s:
+            idx = 1
+            for ch in s:
+                if ch in "0123":
+                    idx = 1 + int(ch)
+                    break
+        return "acnet_legacy", idx
+    if "acnet" in s or "artcnn" in s or "fsrcnnx" in s:
+        raise ValueError("model family outside this backend's scope: %r" % name)
+    return "acnet_legacy", 0
+
+
+_weights_cache = {}
+
+
+def acnet_legacy_weights(variant):
+    """(kernels[4712], biases[72]) float32 for variant 0=GAN, 1..4=HDN0..3."""
+    if "acnet" not in _weights_cache:
+        raw = open(WEIGHTS_BLOB, "rb").read()
+        assert raw[:8] == b"ACGBW001"
+        n, nk, nb = np.frombuffer(raw[8:20], dtype="<u4")
+        arr = np.frombuffer(raw[20:], dtype="<f4").reshape(int(n), int(nk + nb))
+        _weights_cache["acnet"] = (arr, int(nk))
+    arr, nk = _weights_cache["acnet"]
+    return np.ascontiguousarray(arr[variant, :nk]), np.ascontiguousarray(arr[variant, nk:])
+
+
+def arnet_weights(blocks, kind):
+    key = ("arnet", blocks, kind)
+    if key not in _weights_cache:
+        nconv = 2 * blocks
+        k = np.zeros(72 + 576 * nconv + 64 + 288, np.float32)
+        b = np.zeros(8 + 8 * (nconv + 1) + 4, np.float32)
+        a = np.zeros(8 * (blocks + 1), np.float32)
+        rc = lib().orc_arnet_synth(blocks, ARNET_SEED_BASE + 16 * blocks + kind, _p(k), _p(b), _p(a))
+        assert rc == 0
+        _weights_cache[key] = (k, b, a)
+    return _weights_cache[key]
+
+
+# --------------------------------------------------------------- primitives
+
+def luma_x2(y, model, threads=0, f64=False):
+    """One x2 luma pass of ``model`` over a 2-D plane (u8/u16/f32)."""
+    y = _plane(y)
+    h, w = y.shape
+    t = _TYPE_OF[y.dtype]
+    threads = threads or os.cpu_count() or 1
+    fam, var = parse_model(model)
+    if f64:
+        out = np.empty((2 * h, 2 * w), np.float64)
+        if fam == "acnet_legacy":
+            k, b = acnet_legacy_weights(var)
+            rc = lib().orc_acnet_legacy_x2_f64(_p(y), w, h, y.strides[0], t, _p(out), _p(k), _p(b), threads)
+        else:
+            k, b, a = arnet_weights(*var)
+            rc = lib().orc_arnet_x2_f64(_p(y), w, h, y.strides[0], t, _p(out), _p(k), _p(b), _p(a), var[0], threads)
+    else:
+        out = np.empty((2 * h, 2 * w), y.dtype)
+        if fam == "acnet_legacy":
+            k, b = acnet_legacy_weights(var)
+            rc = lib().orc_acnet_legacy_x2(_p(y), w, h, y.strides[0], t, _p(out), out.strides[0], _p(k), _p(b), threads)
+        else:
+            k, b, a = arnet_weights(*var)
+            rc = lib().orc_arnet_x2(_p(y), w, h, y.strides[0], t, _p(out), out.strides[0], _p(k), _p(b), _p(a), var[0], threads)
+    if rc != 0:
+        raise RuntimeError("oracle luma pass failed: %d" % rc)
+    return out
+
+
+def rgb2yuv(img):
+    img = _plane(img)
+    h, w, c = img.shape
+    y = np.empty((h, w), img.dtype)
+    uv = np.empty((h, w, 3 if c == 4 else 2), img.dtype)
+    rc = lib().orc_rgb2yuv(_p(img), w, h, c, img.strides[0], _TYPE_OF[img.dtype], _p(y), y.strides[0], _p(uv), uv.strides[0])
+    assert rc == 0
+    return y, uv
+
+
+def yuv2rgb(y, uv):
+    y = _plane(y)
+    uv = _plane(uv)
+    h, w = y.shape
+    c = 4 if uv.shape[2] == 3 else 3
+    out = np.empty((h, w, c), y.dtype)
+    rc = lib().orc_yuv2rgb(_p(y), y.strides[0], _p(uv), uv.strides[0], w, h, c, _TYPE_OF[y.dtype], _p(out), out.strides[0])
+    assert rc == 0
+    return out
+
+
+def resize(img, dw, dh, mode=RESIZE_CATMULL_ROM):
+    img = _plane(img)
+    squeeze = img.ndim == 2
+    if squeeze:
+        img = img[:, :, None]
+    h, w, c = img.shape
+    out = np.empty((dh, dw, c), img.dtype)
+    rc = lib().orc_resize(_p(img), w, h, c, img.strides[0], _TYPE_OF[img.dtype], _p(out), dw, dh, out.strides[0], mode)
+    assert rc == 0
+    return out[:, :, 0] if squeeze else out
+
+
+def resize_coeffs(n_in, n_out, mode=RESIZE_CATMULL_ROM, maxtaps=64):
+    first = np.zeros(n_out, np.int32)
+    wts = np.zeros((n_out, maxtaps), np.float32)
+    lib().orc_resize_coeffs(n_in, n_out, mode, _p(first), _p(wts), maxtaps)
+    return first, wts
+
+
+def _ceil_log2(v):
+    # Util.hpp:80-89: exponent of v plus one when the mantissa is non-zero.
+    m, e = np.frexp(v)
+    return int(e - 1 + (1 if m != 0.5 else 0))
+
+
+# ----------------------------------------------------------------- pipeline
+
+def process(img, factor, model, threads=0):
+    """Restatement of Processor::process (Processor.cpp:199-276) with an empty
+    dst: luma passes, luma resize by the residual factor, chroma resize by the
+    full factor, colour merge.  ``img`` is (H, W) or (H, W, 3|4)."""
+    img = _plane(img)
+    power = _ceil_log2(factor) if factor > 2.0 else 1
+    fxy = factor / float(1 << power)
+    if img.ndim == 3 and img.shape[2] == 1:
+        img = img[:, :, 0]
+    if img.ndim == 2:
+        out = img
+        for _ in range(power):
+            out = luma_x2(out, model, threads)
+        if fxy != 1.0:
+            out = resize(out, int(out.shape[1] * fxy), int(out.shape[0] * fxy))
+        return out
+    y, uv = rgb2yuv(img)
+    out = y
+    for _ in range(power):
+        out = luma_x2(out, model, threads)
+    if fxy != 1.0:
+        out = resize(out, int(out.shape[1] * fxy), int(out.shape[0] * fxy))
+    h, w = img.shape[:2]
+    uv2 = resize(uv, int(w * factor), int(h * factor))
+    return yuv2rgb(out, uv2)
+
+
+def process_f64(img, model, threads=0):
+    """One x2 pass of the network in FP64 over a luma plane; returns the
+    unquantised, unsaturated (2H, 2W) float64 output."""
+    return luma_x2(img, model, threads, f64=True)
+
+
+# ----------------------------------------------------- the reference itself
+
+def ref_process(img, factor, model, arch=1):
+    """Run the reference's own CPU processor (arch 1 = Generic backend,
+    0 = its automatic ISA choice) with an empty dst."""
+    img = _plane(img)
+    squeeze = img.ndim == 2
+    src = img[:, :, None] if squeeze else img
+    h, w, c = src.shape
+    power = _ceil_log2(factor) if factor > 2.0 else 1
+    dw, dh = w, h
+    for _ in range(power):
+        dw, dh = dw * 2, dh * 2
+    fxy = factor / float(1 << power)
+    if fxy != 1.0:
+        dw, dh = int(dw * fxy), int(dh * fxy)
+    if c > 1:
+        dw, dh = int(w * factor), int(h * factor)
+    out = np.zeros((dh, dw, c), src.dtype)
+    rc = ref().acref_process(model.encode(), arch, _p(src), w, h, c, src.strides[0], _TYPE_OF[src.dtype],
+                             _p(out), dw, dh, out.strides[0], float(factor))
+    if rc != 0:
+        raise RuntimeError("reference process failed: %d" % rc)
+    return out[:, :, 0] if squeeze else out
