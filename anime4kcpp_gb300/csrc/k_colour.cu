@@ -1,0 +1,255 @@
+// Colour split / merge and separable resampling kernels.
+//
+// rgb2yuv / rgba2yuva restate core/src/ImageProcess.cpp:39-61 and :114-138;
+// yuv2rgb / yuva2rgba restate :192-215 and :276-308.  The resampler restates
+// the filter definitions of core/src/ImageResize.cpp:62-83 (Catmull-Rom),
+// :127-134 (bilinear) and point sampling with edge clamp; the reference runs
+// them through stb_image_resize2, which this backend does not use.
+//
+// All of these are memory-bound elementwise kernels: one thread per output
+// pixel, consecutive threads on consecutive pixels of a row (coalesced).
+// Arithmetic uses explicitly rounded intrinsics so it matches the
+// reference's scalar CPU code bit for bit.
+#include <atomic>
+
+#include "device_common.cuh"
+#include "kernels.hpp"
+
+namespace acgb {
+
+namespace {
+std::atomic<uint64_t> g_launches{0};
+}
+uint64_t launch_count() { return g_launches.load(); }
+void count_launch(int n) { g_launches.fetch_add(static_cast<uint64_t>(n)); }
+
+template <typename T, int C>
+__global__ void rgb2yuv_split_kernel(Plane rgb, Plane yp, Plane uvp)
+{
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y;
+    if (x >= rgb.w) return;
+    const T* in = row_ptr<T>(rgb.ptr, rgb.pitch, y) + x * C;
+    float r = to_float<T>(in[0]);
+    float g = to_float<T>(in[1]);
+    float b = to_float<T>(in[2]);
+    float a = 1.0f;
+    if constexpr (C == 4)
+    {
+        a = to_float<T>(in[3]);
+        r = __fmul_rn(r, a);
+        g = __fmul_rn(g, a);
+        b = __fmul_rn(b, a);
+    }
+    float yy = __fadd_rn(__fadd_rn(__fmul_rn(0.299f, r), __fmul_rn(0.587f, g)), __fmul_rn(0.114f, b));
+    float u = __fadd_rn(__fmul_rn(0.564f, __fsub_rn(b, yy)), 0.5f);
+    float v = __fadd_rn(__fmul_rn(0.713f, __fsub_rn(r, yy)), 0.5f);
+    row_ptr_w<T>(yp.ptr, yp.pitch, y)[x] = from_float<T>(yy);
+    T* uo = row_ptr_w<T>(uvp.ptr, uvp.pitch, y) + x * (C - 1);
+    uo[0] = from_float<T>(u);
+    uo[1] = from_float<T>(v);
+    if constexpr (C == 4) uo[2] = from_float<T>(a);
+}
+
+template <typename T, int C>
+__global__ void rgb2yuv_packed_kernel(Plane rgb, Plane yuv)
+{
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y;
+    if (x >= rgb.w) return;
+    const T* in = row_ptr<T>(rgb.ptr, rgb.pitch, y) + x * C;
+    float r = to_float<T>(in[0]);
+    float g = to_float<T>(in[1]);
+    float b = to_float<T>(in[2]);
+    float a = 1.0f;
+    if constexpr (C == 4)
+    {
+        a = to_float<T>(in[3]);
+        r = __fmul_rn(r, a);
+        g = __fmul_rn(g, a);
+        b = __fmul_rn(b, a);
+    }
+    float yy = __fadd_rn(__fadd_rn(__fmul_rn(0.299f, r), __fmul_rn(0.587f, g)), __fmul_rn(0.114f, b));
+    float u = __fadd_rn(__fmul_rn(0.564f, __fsub_rn(b, yy)), 0.5f);
+    float v = __fadd_rn(__fmul_rn(0.713f, __fsub_rn(r, yy)), 0.5f);
+    T* out = row_ptr_w<T>(yuv.ptr, yuv.pitch, y) + x * C;
+    out[0] = from_float<T>(yy);
+    out[1] = from_float<T>(u);
+    out[2] = from_float<T>(v);
+    if constexpr (C == 4) out[3] = from_float<T>(a);
+}
+
+// yuv2rgb math on normalised inputs; writes C channels.
+template <typename T, int C>
+__device__ __forceinline__ void yuv_to_rgb_store(float yy, float u, float v, float a, T* out)
+{
+    u = __fsub_rn(u, 0.5f);
+    v = __fsub_rn(v, 0.5f);
+    float r = __fadd_rn(yy, __fmul_rn(1.403f, v));
+    float g = __fsub_rn(__fsub_rn(yy, __fmul_rn(0.344f, u)), __fmul_rn(0.714f, v));
+    float b = __fadd_rn(yy, __fmul_rn(1.773f, u));
+    if constexpr (C == 4)
+    {
+        if (a > 1e-6f)
+        {
+            r = __fdiv_rn(r, a);
+            g = __fdiv_rn(g, a);
+            b = __fdiv_rn(b, a);
+        }
+        else r = g = b = 0.0f;
+    }
+    out[0] = from_float<T>(r);
+    out[1] = from_float<T>(g);
+    out[2] = from_float<T>(b);
+    if constexpr (C == 4) out[3] = from_float<T>(a);
+}
+
+template <typename T, int C>
+__global__ void yuv2rgb_packed_kernel(Plane yuv, Plane rgb)
+{
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y;
+    if (x >= yuv.w) return;
+    const T* in = row_ptr<T>(yuv.ptr, yuv.pitch, y) + x * C;
+    float yy = to_float<T>(in[0]);
+    float u = to_float<T>(in[1]);
+    float v = to_float<T>(in[2]);
+    float a = C == 4 ? to_float<T>(in[3]) : 1.0f;
+    yuv_to_rgb_store<T, C>(yy, u, v, a, row_ptr_w<T>(rgb.ptr, rgb.pitch, y) + x * C);
+}
+
+// Resampled value of channel `ch` of an interleaved plane at output (ox, oy):
+// horizontal sums per source row (ascending taps), then the vertical sum,
+// all in float with explicit rounding; zero weights skipped.
+template <typename T, int NC>
+__device__ __forceinline__ float resample(const Plane& src, const ResizeAxis& ax, const ResizeAxis& ay, int ox, int oy, int ch)
+{
+    const int fx = ax.first[ox];
+    const int fy = ay.first[oy];
+    const float* wxs = ax.w + static_cast<size_t>(ox) * ax.taps;
+    const float* wys = ay.w + static_cast<size_t>(oy) * ay.taps;
+    float s = 0.0f;
+    for (int j = 0; j < ay.taps; j++)
+    {
+        float wy = wys[j];
+        if (wy == 0.0f) continue;
+        int sy = clampi(fy + j, 0, src.h - 1);
+        const T* row = row_ptr<T>(src.ptr, src.pitch, sy);
+        float hsum = 0.0f;
+        for (int i = 0; i < ax.taps; i++)
+        {
+            float wx = wxs[i];
+            if (wx == 0.0f) continue;
+            int sx = clampi(fx + i, 0, src.w - 1);
+            hsum = __fadd_rn(hsum, __fmul_rn(wx, decode_float<T>(row[sx * NC + ch])));
+        }
+        s = __fadd_rn(s, __fmul_rn(wy, hsum));
+    }
+    return s;
+}
+
+template <typename T, int C>
+__global__ void merge_resize_kernel(Plane yp, Plane uvp, ResizeAxis ax, ResizeAxis ay, Plane rgb)
+{
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y;
+    if (x >= yp.w) return;
+    constexpr int UC = C - 1;
+    float yy = to_float<T>(row_ptr<T>(yp.ptr, yp.pitch, y)[x]);
+    // resample, quantise to the element type (the reference stores the
+    // resized UV as an image of the source type), then normalise again.
+    float u = to_float<T>(encode_resampled<T>(resample<T, UC>(uvp, ax, ay, x, y, 0)));
+    float v = to_float<T>(encode_resampled<T>(resample<T, UC>(uvp, ax, ay, x, y, 1)));
+    float a = 1.0f;
+    if constexpr (C == 4) a = to_float<T>(encode_resampled<T>(resample<T, UC>(uvp, ax, ay, x, y, 2)));
+    yuv_to_rgb_store<T, C>(yy, u, v, a, row_ptr_w<T>(rgb.ptr, rgb.pitch, y) + x * C);
+}
+
+template <typename T, int NC>
+__global__ void resize_kernel(Plane src, Plane dst, ResizeAxis ax, ResizeAxis ay)
+{
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y;
+    if (x >= dst.w) return;
+    T* out = row_ptr_w<T>(dst.ptr, dst.pitch, y) + x * NC;
+    for (int c = 0; c < NC; c++) out[c] = encode_resampled<T>(resample<T, NC>(src, ax, ay, x, y, c));
+}
+
+namespace {
+
+dim3 row_grid(int w, int h, int block) { return dim3((w + block - 1) / block, h); }
+
+}  // namespace
+
+#define ACGB_TYPE_SWITCH(type, ...)                     \
+    switch (type)                                       \
+    {                                                   \
+    case kU8: { using T = uint8_t; __VA_ARGS__ } break;  \
+    case kU16: { using T = uint16_t; __VA_ARGS__ } break; \
+    case kF32: { using T = float; __VA_ARGS__ } break;   \
+    default: return cudaErrorInvalidValue;              \
+    }
+
+cudaError_t launch_rgb2yuv_split(const Plane& rgb, const Plane& y, const Plane& uv, cudaStream_t stream)
+{
+    if (rgb.w <= 0 || rgb.h <= 0) return cudaSuccess;
+    dim3 grid = row_grid(rgb.w, rgb.h, 128);
+    ACGB_TYPE_SWITCH(rgb.type,
+        if (rgb.channels == 4) rgb2yuv_split_kernel<T, 4><<<grid, 128, 0, stream>>>(rgb, y, uv);
+        else rgb2yuv_split_kernel<T, 3><<<grid, 128, 0, stream>>>(rgb, y, uv);)
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rgb2yuv_packed(const Plane& rgb, const Plane& yuv, cudaStream_t stream)
+{
+    if (rgb.w <= 0 || rgb.h <= 0) return cudaSuccess;
+    dim3 grid = row_grid(rgb.w, rgb.h, 128);
+    ACGB_TYPE_SWITCH(rgb.type,
+        if (rgb.channels == 4) rgb2yuv_packed_kernel<T, 4><<<grid, 128, 0, stream>>>(rgb, yuv);
+        else rgb2yuv_packed_kernel<T, 3><<<grid, 128, 0, stream>>>(rgb, yuv);)
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_yuv2rgb_packed(const Plane& yuv, const Plane& rgb, cudaStream_t stream)
+{
+    if (yuv.w <= 0 || yuv.h <= 0) return cudaSuccess;
+    dim3 grid = row_grid(yuv.w, yuv.h, 128);
+    ACGB_TYPE_SWITCH(yuv.type,
+        if (yuv.channels == 4) yuv2rgb_packed_kernel<T, 4><<<grid, 128, 0, stream>>>(yuv, rgb);
+        else yuv2rgb_packed_kernel<T, 3><<<grid, 128, 0, stream>>>(yuv, rgb);)
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_merge_resize(const Plane& y, const Plane& uv, ResizeAxis ax, ResizeAxis ay, const Plane& rgb,
+                                cudaStream_t stream)
+{
+    if (y.w <= 0 || y.h <= 0) return cudaSuccess;
+    dim3 grid = row_grid(y.w, y.h, 128);
+    ACGB_TYPE_SWITCH(y.type,
+        if (rgb.channels == 4) merge_resize_kernel<T, 4><<<grid, 128, 0, stream>>>(y, uv, ax, ay, rgb);
+        else merge_resize_kernel<T, 3><<<grid, 128, 0, stream>>>(y, uv, ax, ay, rgb);)
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_resize(const Plane& src, const Plane& dst, ResizeAxis ax, ResizeAxis ay, cudaStream_t stream)
+{
+    if (dst.w <= 0 || dst.h <= 0) return cudaSuccess;
+    dim3 grid = row_grid(dst.w, dst.h, 128);
+    ACGB_TYPE_SWITCH(src.type,
+        switch (src.channels)
+        {
+        case 1: resize_kernel<T, 1><<<grid, 128, 0, stream>>>(src, dst, ax, ay); break;
+        case 2: resize_kernel<T, 2><<<grid, 128, 0, stream>>>(src, dst, ax, ay); break;
+        case 3: resize_kernel<T, 3><<<grid, 128, 0, stream>>>(src, dst, ax, ay); break;
+        case 4: resize_kernel<T, 4><<<grid, 128, 0, stream>>>(src, dst, ax, ay); break;
+        default: return cudaErrorInvalidValue;
+        })
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace acgb

@@ -1,0 +1,73 @@
+// Host-side launch interface of the CUDA kernels (no torch types, plain
+// pointers and sizes).  All planes live in device memory.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace acgb {
+
+// A device image plane: `channels` interleaved elements per pixel.
+struct Plane
+{
+    void* ptr = nullptr;
+    int w = 0, h = 0;
+    int pitch = 0;     // bytes between rows
+    int channels = 1;
+    int type = 0x001;  // ElemType
+};
+
+// ACNetLegacy parameters in the reference's NHWC layout
+// (core/include/AC/Core/Model/ACNet.hpp:34-60): 8*9 + 8*8*9*8 + 8*4 kernel
+// floats, 8 + 8*8 bias floats.
+constexpr int kAcnetKernels = 8 * 9 + 8 * 8 * 9 * 8 + 8 * 4;
+constexpr int kAcnetBiases = 8 + 8 * 8;
+struct AcnetLegacyWeights
+{
+    float k[kAcnetKernels];
+    float b[kAcnetBiases];
+};
+
+// Separable resampling table for one axis: for output index o, taps
+// first[o] .. first[o] + taps - 1 (clamped to the source) with weights
+// w[o * taps + t]; zero weights are skipped.
+struct ResizeAxis
+{
+    const int* first = nullptr;
+    const float* w = nullptr;
+    int taps = 0;
+};
+
+// Plain FP32 layer-fused ACNetLegacy x2 pass: in (1 ch) -> out (1 ch, 2w x 2h),
+// same element type.  Returns the launch error.
+cudaError_t launch_acnet_legacy_fp32(const AcnetLegacyWeights& wts, const Plane& in, const Plane& out, cudaStream_t stream);
+
+// Tensor-core (tcgen05) layer-fused ACNetLegacy x2 pass.  `packed` is the
+// device copy of pack_acnet_tc_weights(); bf16 selects BF16 operands
+// (FP16 otherwise).  Layer 0, the deconvolution and all element conversions
+// stay FP32.
+cudaError_t launch_acnet_legacy_tc(const AcnetLegacyWeights& wts, const void* packed, bool bf16, const Plane& in,
+                                   const Plane& out, cudaStream_t stream);
+void pack_acnet_tc_weights(const AcnetLegacyWeights& wts, bool bf16, std::vector<uint16_t>& packed);
+
+// RGB(A) -> Y + UV(A) (rgb2yuv / rgba2yuva of core/src/ImageProcess.cpp).
+cudaError_t launch_rgb2yuv_split(const Plane& rgb, const Plane& y, const Plane& uv, cudaStream_t stream);
+// Interleaved 3/4-channel RGB(A) -> interleaved YUV(A) in place or not.
+cudaError_t launch_rgb2yuv_packed(const Plane& rgb, const Plane& yuv, cudaStream_t stream);
+cudaError_t launch_yuv2rgb_packed(const Plane& yuv, const Plane& rgb, cudaStream_t stream);
+
+// Y (full size) + UV(A) at any size, resampled on the fly to Y's size with
+// the given tables, then yuv2rgb / yuva2rgba into rgb.
+cudaError_t launch_merge_resize(const Plane& y, const Plane& uv, ResizeAxis ax, ResizeAxis ay, const Plane& rgb,
+                                cudaStream_t stream);
+
+// General separable resize of an interleaved plane (any channel count).
+cudaError_t launch_resize(const Plane& src, const Plane& dst, ResizeAxis ax, ResizeAxis ay, cudaStream_t stream);
+
+// Number of kernel launches issued by this library in the process so far.
+uint64_t launch_count();
+void count_launch(int n = 1);
+
+}  // namespace acgb

@@ -1,0 +1,139 @@
+// Model string parsing and parameter tables.
+#include "models.hpp"
+
+#include <algorithm>
+#include <cctype>
+#include <cstring>
+#include <map>
+#include <mutex>
+
+namespace acgb {
+
+// Generated at build time from weights/acnet_legacy.bin (see build.py):
+// 5 variants (GAN, HDN0..3) x (4712 kernel + 72 bias) float32 bit patterns.
+extern const uint32_t kAcnetLegacyBlob[];
+extern const int kAcnetLegacyVariants;
+extern const int kAcnetLegacyKernels;
+extern const int kAcnetLegacyBiases;
+
+bool parse_model(const char* model, ModelSpec& spec, std::string& error)
+{
+    std::string s = model ? model : "";
+    for (char& ch : s) ch = static_cast<char>(std::tolower(static_cast<unsigned char>(ch)));
+    spec = ModelSpec{};
+    spec.name = model ? model : "";
+    auto has = [&](const char* t) { return s.find(t) != std::string::npos; };
+    if (has("fsrcnnx") || has("artcnn"))
+    {
+        error = "model family not provided by the GB300 backend: " + spec.name;
+        return false;
+    }
+    if (has("arnet"))
+    {
+        spec.family = Family::ARNet;
+        spec.blocks = 8;
+        // Processor.cpp:82-124 checks b8 before b16/b32/b64.
+        if (has("b8")) spec.blocks = 8;
+        else if (has("b16")) spec.blocks = 16;
+        else if (has("b32")) spec.blocks = 32;
+        else if (has("b64")) spec.blocks = 64;
+        spec.kind = (has("box") ? 2 : 0) + (has("hdn") ? 1 : 0);
+        return true;
+    }
+    if (has("acnet"))
+    {
+        if (has("legacy"))
+        {
+            spec.family = Family::ACNetLegacy;
+            spec.variant = 0;
+            if (has("hdn"))
+            {
+                // Processor.cpp:130-141: first digit 0..3 found picks HDN0..3.
+                spec.variant = 1;
+                for (char ch : s)
+                    if (ch >= '0' && ch <= '3')
+                    {
+                        spec.variant = 1 + (ch - '0');
+                        break;
+                    }
+            }
+            return true;
+        }
+        error = "model family not provided by the GB300 backend (ACNet<8>): " + spec.name;
+        return false;
+    }
+    // Processor.cpp:186: anything else is ACNetLegacy GAN.
+    spec.family = Family::ACNetLegacy;
+    spec.variant = 0;
+    return true;
+}
+
+namespace {
+
+uint64_t splitmix64(uint64_t& s)
+{
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// 24-bit uniform in [-1, 1): exact in float.
+float uniform_pm1(uint64_t& s)
+{
+    uint64_t r = splitmix64(s) >> 40;
+    return static_cast<float>(r) * (1.0f / 8388608.0f) - 1.0f;
+}
+
+}  // namespace
+
+void arnet_synthetic_params(int blocks, uint64_t seed, ModelParams& out)
+{
+    const int nconv = 2 * blocks;
+    const int kl = 72 + 576 * nconv + 64 + 288;
+    const int bl = 8 + 8 * (nconv + 1) + 4;
+    const int al = 8 * (blocks + 1);
+    out.kernels.resize(kl);
+    out.biases.resize(bl);
+    out.alphas.resize(al);
+    uint64_t s = seed;
+    for (int i = 0; i < kl; i++)
+    {
+        float scale;
+        if (i < 72) scale = 0.5f;                            // head 1 -> 8
+        else if (i < 72 + 576 * nconv) scale = 0.12f;         // body 3x3 8 -> 8
+        else if (i < 72 + 576 * nconv + 64) scale = 0.2f;    // tail 1x1 8 -> 8
+        else scale = 0.02f;                                   // upscale 3x3 8 -> 4
+        out.kernels[i] = uniform_pm1(s) * scale;
+    }
+    for (int i = 0; i < bl; i++) out.biases[i] = uniform_pm1(s) * 0.01f;
+    for (int i = 0; i < al; i++) out.alphas[i] = (uniform_pm1(s) + 1.0f) * 0.125f;
+}
+
+const ModelParams& model_params(const ModelSpec& spec)
+{
+    static std::mutex m;
+    static std::map<std::pair<int, int>, ModelParams> cache;
+    std::lock_guard<std::mutex> lock(m);
+    std::pair<int, int> key = spec.family == Family::ACNetLegacy ? std::make_pair(0, spec.variant)
+                                                                  : std::make_pair(spec.blocks, spec.kind);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    ModelParams p;
+    if (spec.family == Family::ACNetLegacy)
+    {
+        const int per = kAcnetLegacyKernels + kAcnetLegacyBiases;
+        const uint32_t* base = kAcnetLegacyBlob + static_cast<size_t>(spec.variant) * per;
+        p.kernels.resize(kAcnetLegacyKernels);
+        p.biases.resize(kAcnetLegacyBiases);
+        std::memcpy(p.kernels.data(), base, sizeof(float) * kAcnetLegacyKernels);
+        std::memcpy(p.biases.data(), base + kAcnetLegacyKernels, sizeof(float) * kAcnetLegacyBiases);
+    }
+    else
+    {
+        arnet_synthetic_params(spec.blocks, kArnetSeedBase + 16ull * spec.blocks + spec.kind, p);
+    }
+    return cache.emplace(key, std::move(p)).first->second;
+}
+
+}  // namespace acgb

@@ -1,0 +1,44 @@
+// Model selection and parameters for the GB300 backend.
+//
+// Families on the hot path: ACNetLegacy (trained parameters of the
+// reference, variants GAN and HDN0..3) and ARNet<8> (B8/16/32/64 x
+// {normal, HDN, Box, Box-HDN}; seeded synthetic parameters because the
+// reference's trained ARNet parameters are not distributed with its source).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace acgb {
+
+enum class Family { ACNetLegacy, ARNet };
+
+struct ModelSpec
+{
+    Family family = Family::ACNetLegacy;
+    int variant = 0;  // ACNetLegacy: 0 GAN, 1..4 HDN0..3
+    int blocks = 0;   // ARNet: 8, 16, 32, 64
+    int kind = 0;     // ARNet: 0 normal, 1 HDN, 2 Box, 3 Box-HDN
+    std::string name;
+};
+
+// Parses a model string like core/src/processor/Processor.cpp:26-187 does
+// for the ACNetLegacy and ARNet families.  Returns false (with a message)
+// for the families this backend does not run (ACNet<8>, ArtCNN, FSRCNNX).
+bool parse_model(const char* model, ModelSpec& spec, std::string& error);
+
+struct ModelParams
+{
+    std::vector<float> kernels, biases, alphas;
+};
+
+// Parameters in the reference's NHWC blob layout (ACNet.hpp:34-60,
+// ARNet.hpp:26-70).
+const ModelParams& model_params(const ModelSpec& spec);
+
+// Seed of the synthetic ARNet parameters of a variant.
+constexpr uint64_t kArnetSeedBase = 0x41524E6574000000ull;
+void arnet_synthetic_params(int blocks, uint64_t seed, ModelParams& out);
+
+}  // namespace acgb

@@ -1,0 +1,638 @@
+// GB300 processor: the whole Processor::process path on one GPU.
+//
+// Pipeline of one call (core/src/processor/Processor.cpp:199-276):
+//   power = factor > 2 ? ceilLog2(factor) : 1, fxy = factor / 2^power
+//   RGB(A): split into Y and UV(A) (quantised to the source type)
+//   `power` luma passes of the CNN, each x2
+//   luma resize by fxy when fxy != 1 (Catmull-Rom)
+//   RGB(A): chroma resampled by `factor` on the fly and merged back
+// Host images are copied to device buffers once per call; intermediates stay
+// in HBM.  Per calling thread the processor keeps a CUDA stream, grow-only
+// device workspaces, cached resampling tables and the error state (the
+// reference keeps per-thread scratch and error state the same way,
+// core/src/processor/cuda/CUDAProcessor.cpp:284,374-377).
+#include "processor_impl.hpp"
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstring>
+#include <sstream>
+
+namespace acgb {
+
+// ---------------------------------------------------------------- helpers
+
+int ceil_log2(double v)
+{
+    // core/internal/AC/Core/Internal/Util.hpp:80-89.
+    uint64_t bits;
+    std::memcpy(&bits, &v, sizeof(bits));
+    return static_cast<int>(static_cast<int64_t>((bits >> 52) & 0x7ff) - 1023 + ((bits << 12) != 0 ? 1 : 0));
+}
+
+void output_shape(int w, int h, int c, double factor, int& ow, int& oh)
+{
+    int power = factor > 2.0 ? ceil_log2(factor) : 1;
+    double fxy = factor / static_cast<double>(1 << power);
+    int lw = w << power, lh = h << power;
+    if (fxy != 1.0)
+    {
+        lw = static_cast<int>(lw * fxy);
+        lh = static_cast<int>(lh * fxy);
+    }
+    ow = lw;
+    oh = lh;
+    (void)c;
+}
+
+namespace {
+
+// Resampling coefficients: the same arithmetic as the project's CPU
+// restatement of the reference filters (ImageResize.cpp:62-83, 127-134).
+float filter_eval(int mode, float x)
+{
+    float ax = std::fabs(x);
+    if (mode == 16) return ax < 1.0f ? 1.0f - ax : 0.0f;
+    if (mode == 0) return ax <= 0.5f ? 1.0f : 0.0f;
+    if (ax < 1.0f) return 1.0f + ax * (0.0f + ax * (-2.5f + ax * 1.5f));
+    if (ax < 2.0f) return 2.0f + ax * (-4.0f + ax * (2.5f + ax * -0.5f));
+    return 0.0f;
+}
+float filter_support(int mode) { return mode == 16 ? 1.0f : (mode == 0 ? 0.5f : 2.0f); }
+
+}  // namespace
+
+void make_axis_table(int n_in, int n_out, int mode, std::vector<int>& first, std::vector<float>& weights, int& taps)
+{
+    constexpr int MT = 64;
+    double scale = static_cast<double>(n_out) / static_cast<double>(n_in);
+    float sup = filter_support(mode);
+    float fscale = scale < 1.0 ? static_cast<float>(scale) : 1.0f;
+    float radius = sup / fscale;
+    std::vector<float> full(static_cast<size_t>(n_out) * MT, 0.0f);
+    first.assign(n_out, 0);
+    int maxUsed = 1;
+    for (int o = 0; o < n_out; o++)
+    {
+        float center = static_cast<float>((static_cast<double>(o) + 0.5) / scale - 0.5);
+        int lo = static_cast<int>(std::ceil(center - radius));
+        int hi = static_cast<int>(std::floor(center + radius));
+        if (mode == 0)
+        {
+            lo = static_cast<int>(std::floor(center + 0.5f));
+            hi = lo;
+        }
+        if (hi - lo + 1 > MT) hi = lo + MT - 1;
+        int cnt = hi - lo + 1;
+        float wv[MT];
+        float sum = 0.0f;
+        for (int t = 0; t < cnt; t++)
+        {
+            float d = (static_cast<float>(lo + t) - center) * fscale;
+            wv[t] = mode == 0 ? 1.0f : filter_eval(mode, d);
+            sum += wv[t];
+        }
+        first[o] = lo;
+        for (int t = 0; t < cnt; t++)
+        {
+            float v = sum != 0.0f ? wv[t] / sum : 0.0f;
+            full[static_cast<size_t>(o) * MT + t] = v;
+            if (v != 0.0f) maxUsed = std::max(maxUsed, t + 1);
+        }
+    }
+    taps = maxUsed;
+    weights.assign(static_cast<size_t>(n_out) * taps, 0.0f);
+    for (int o = 0; o < n_out; o++)
+        for (int t = 0; t < taps; t++) weights[static_cast<size_t>(o) * taps + t] = full[static_cast<size_t>(o) * MT + t];
+}
+
+// ----------------------------------------------------------- DeviceBuffer
+
+cudaError_t DeviceBuffer::ensure(size_t bytes)
+{
+    if (bytes <= cap) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    size_t want = (bytes + (2u << 20) - 1) & ~static_cast<size_t>((2u << 20) - 1);
+    cudaError_t err = cudaMalloc(&ptr, want);
+    if (err != cudaSuccess)
+    {
+        ptr = nullptr;
+        return err;
+    }
+    cap = want;
+    return cudaSuccess;
+}
+
+void DeviceBuffer::release()
+{
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+}
+
+// ------------------------------------------------------------ Processor
+
+Image Processor::process(const Image& src, double factor)
+{
+    Image dst{};
+    process(src, dst, factor);
+    return dst;
+}
+
+void Processor::process(const Image& src, Image& dst, double factor) { processHost(src, dst, factor); }
+
+namespace {
+
+class UnavailableProcessor final : public Processor
+{
+public:
+    UnavailableProcessor(int type, std::string why) : type_(type), why_(std::move(why)) {}
+    bool ok() noexcept override { return false; }
+    const char* error() noexcept override { return why_.c_str(); }
+    const char* name() const noexcept override { return "unavailable"; }
+    int type() const noexcept override { return type_; }
+    const char* typeName() const noexcept override
+    {
+        return type_ == CPU ? "CPU" : (type_ == OpenCL ? "OpenCL" : "CUDA");
+    }
+
+protected:
+    void processHost(const Image&, Image&, double) override {}
+
+private:
+    int type_;
+    std::string why_;
+};
+
+int find_processor_type(const char* type)
+{
+    // Processor.cpp:12-25: "auto" -> -1, "opencl", "cuda", anything else CPU.
+    if (!type) return Processor::CPU;
+    std::string s = type;
+    for (char& ch : s) ch = static_cast<char>(std::tolower(static_cast<unsigned char>(ch)));
+    if (s == "auto") return -1;
+    if (s == "opencl") return Processor::OpenCL;
+    if (s == "cuda") return Processor::CUDA;
+    return Processor::CPU;
+}
+
+}  // namespace
+
+std::shared_ptr<Processor> Processor::create(const char* type, int device, const char* model)
+{
+    int t = find_processor_type(type);
+    if (t == CPU)
+        return std::make_shared<UnavailableProcessor>(CPU, "the GB300 backend provides no CPU processor; use type \"cuda\"");
+    if (t == OpenCL)
+        return std::make_shared<UnavailableProcessor>(OpenCL, "the GB300 backend provides no OpenCL processor; use type \"cuda\"");
+    ModelSpec spec;
+    std::string err;
+    if (!parse_model(model, spec, err)) return std::make_shared<UnavailableProcessor>(CUDA, err);
+    return std::make_shared<GB300Processor>(t == -1 ? -1 : device, spec);
+}
+
+const char* Processor::info(int type)
+{
+    if (type != CUDA) return "not provided by the GB300 backend\n";
+    static std::string text = []() {
+        std::ostringstream os;
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess) n = 0;
+        os << "GB300 CUDA backend (sm_103a):\n";
+        if (n == 0) os << "  no CUDA device\n";
+        for (int i = 0; i < n; i++)
+        {
+            cudaDeviceProp p{};
+            if (cudaGetDeviceProperties(&p, i) != cudaSuccess) continue;
+            os << "  [" << i << "] " << p.name << ", compute capability " << p.major << "." << p.minor << ", "
+               << p.multiProcessorCount << " SMs, " << (p.totalGlobalMem >> 20) << " MiB\n";
+        }
+        return os.str();
+    }();
+    return text.c_str();
+}
+
+const char* Processor::listInfo() { return info(CUDA); }
+
+// --------------------------------------------------------- GB300Processor
+
+GB300Processor::GB300Processor(int device, const ModelSpec& spec) : spec_(spec)
+{
+    precision_ = default_precision();
+    int n = 0;
+    cudaError_t err = cudaGetDeviceCount(&n);
+    if (err != cudaSuccess || n == 0)
+    {
+        initError_ = std::string("no CUDA device: ") + cudaGetErrorString(err == cudaSuccess ? cudaErrorNoDevice : err);
+        return;
+    }
+    if (device >= 0 && device < n) device_ = device;
+    else
+    {
+        // Like the reference (CUDAProcessor.cpp:233-251), pick the device with
+        // the largest SM-count x clock score.
+        long best = -1;
+        for (int i = 0; i < n; i++)
+        {
+            int clk = 0, sms = 0;
+            cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, i);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, i);
+            if (static_cast<long>(clk) * sms > best)
+            {
+                best = static_cast<long>(clk) * sms;
+                device_ = i;
+            }
+        }
+    }
+    cudaDeviceProp prop{};
+    err = cudaGetDeviceProperties(&prop, device_);
+    if (err != cudaSuccess)
+    {
+        initError_ = cudaGetErrorString(err);
+        return;
+    }
+    if (!(prop.major == 10 && prop.minor == 3))
+    {
+        initError_ = std::string("device ") + prop.name + " is not sm_103 (GB300); this build only carries sm_103a code";
+        return;
+    }
+    name_ = prop.name;
+    smCount_ = prop.multiProcessorCount;
+    const ModelParams& mp = model_params(spec_);
+    if (spec_.family == Family::ACNetLegacy)
+    {
+        acnet_ = std::make_unique<AcnetLegacyWeights>();
+        std::memcpy(acnet_->k, mp.kernels.data(), sizeof(acnet_->k));
+        std::memcpy(acnet_->b, mp.biases.data(), sizeof(acnet_->b));
+    }
+}
+
+GB300Processor::~GB300Processor()
+{
+    std::lock_guard<std::mutex> lock(mutex_);
+    if (device_ >= 0) cudaSetDevice(device_);
+    for (auto& kv : states_)
+    {
+        ThreadState& ts = *kv.second;
+        if (ts.stream) cudaStreamSynchronize(ts.stream);
+        ts.src.release();
+        ts.y.release();
+        ts.uv.release();
+        ts.la.release();
+        ts.lb.release();
+        ts.out.release();
+        for (auto& t : ts.tables) t.second.dev.release();
+        for (auto& e : ts.events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+        for (auto& e : ts.pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+        if (ts.stream) cudaStreamDestroy(ts.stream);
+    }
+    states_.clear();
+    for (auto& d : deviceWeights_) d.release();
+}
+
+Precision GB300Processor::default_precision()
+{
+    const char* env = std::getenv("AC_GB300_PRECISION");
+    if (env)
+    {
+        std::string s = env;
+        for (char& ch : s) ch = static_cast<char>(std::tolower(static_cast<unsigned char>(ch)));
+        if (s == "fp32") return Precision::FP32;
+        if (s == "fp16") return Precision::FP16;
+        if (s == "bf16") return Precision::BF16;
+    }
+    return Precision::FP32;
+}
+
+GB300Processor::ThreadState& GB300Processor::state()
+{
+    std::lock_guard<std::mutex> lock(mutex_);
+    auto& slot = states_[std::this_thread::get_id()];
+    if (!slot) slot = std::make_unique<ThreadState>();
+    return *slot;
+}
+
+bool GB300Processor::ok() noexcept
+{
+    if (!initError_.empty()) return false;
+    return state().ok;
+}
+
+const char* GB300Processor::error() noexcept
+{
+    if (!initError_.empty()) return initError_.c_str();
+    return state().err.c_str();
+}
+
+const char* GB300Processor::name() const noexcept { return name_.empty() ? "unavailable" : name_.c_str(); }
+
+bool GB300Processor::fail(ThreadState& ts, const std::string& what, cudaError_t err)
+{
+    ts.ok = false;
+    ts.err = what;
+    if (err != cudaSuccess)
+    {
+        ts.err += ": ";
+        ts.err += cudaGetErrorString(err);
+        cudaGetLastError();  // clear a non-sticky error for the next call
+    }
+    return false;
+}
+
+bool GB300Processor::begin(ThreadState& ts)
+{
+    ts.ok = true;
+    ts.err = "NO ERROR";
+    if (!initError_.empty()) return fail(ts, initError_);
+    cudaError_t err = cudaSetDevice(device_);
+    if (err != cudaSuccess) return fail(ts, "cudaSetDevice", err);
+    if (!ts.stream)
+    {
+        err = cudaStreamCreateWithFlags(&ts.stream, cudaStreamNonBlocking);
+        if (err != cudaSuccess) return fail(ts, "cudaStreamCreate", err);
+    }
+    return true;
+}
+
+const ResizeAxis* GB300Processor::axis(ThreadState& ts, int n_in, int n_out, int mode, cudaStream_t stream, cudaError_t& err)
+{
+    auto key = std::make_tuple(n_in, n_out, mode);
+    auto it = ts.tables.find(key);
+    if (it != ts.tables.end()) return &it->second.axis;
+    AxisTable t;
+    make_axis_table(n_in, n_out, mode, t.first, t.w, t.taps);
+    size_t fb = sizeof(int) * t.first.size();
+    size_t wb = sizeof(float) * t.w.size();
+    size_t off = (fb + 255) & ~static_cast<size_t>(255);
+    err = t.dev.ensure(off + wb);
+    if (err != cudaSuccess) return nullptr;
+    err = cudaMemcpyAsync(t.dev.ptr, t.first.data(), fb, cudaMemcpyHostToDevice, stream);
+    if (err != cudaSuccess) return nullptr;
+    err = cudaMemcpyAsync(static_cast<char*>(t.dev.ptr) + off, t.w.data(), wb, cudaMemcpyHostToDevice, stream);
+    if (err != cudaSuccess) return nullptr;
+    // The host vectors must outlive the asynchronous copies: they live in the cache.
+    t.axis.first = static_cast<const int*>(t.dev.ptr);
+    t.axis.w = reinterpret_cast<const float*>(static_cast<char*>(t.dev.ptr) + off);
+    t.axis.taps = t.taps;
+    auto res = ts.tables.emplace(key, std::move(t));
+    return &res.first->second.axis;
+}
+
+cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Plane& out, cudaStream_t stream)
+{
+    std::pair<cudaEvent_t, cudaEvent_t> ev{nullptr, nullptr};
+    if (profiling_)
+    {
+        if (ts.pool.empty())
+        {
+            cudaEventCreate(&ev.first);
+            cudaEventCreate(&ev.second);
+        }
+        else
+        {
+            ev = ts.pool.back();
+            ts.pool.pop_back();
+        }
+        cudaEventRecord(ev.first, stream);
+    }
+    cudaError_t err = cudaErrorNotSupported;
+    if (spec_.family == Family::ACNetLegacy)
+    {
+        if (precision_ == Precision::FP32) err = launch_acnet_legacy_fp32(*acnet_, in, out, stream);
+        else
+        {
+            const void* w = tcWeights(precision_, stream);
+            err = w ? launch_acnet_legacy_tc(*acnet_, w, precision_ == Precision::BF16, in, out, stream) : cudaErrorMemoryAllocation;
+        }
+    }
+    if (profiling_)
+    {
+        cudaEventRecord(ev.second, stream);
+        ts.events.push_back(ev);
+        ts.eventPixels.push_back(static_cast<double>(out.w) * out.h);
+    }
+    return err;
+}
+
+void GB300Processor::setProfiling(bool on) { profiling_ = on; }
+
+int GB300Processor::collectProfile(double& ms, int& launches, double& outPixels)
+{
+    ThreadState& ts = state();
+    ms = 0.0;
+    outPixels = 0.0;
+    launches = static_cast<int>(ts.events.size());
+    for (size_t i = 0; i < ts.events.size(); i++)
+    {
+        auto& e = ts.events[i];
+        if (cudaEventSynchronize(e.second) != cudaSuccess) return -1;
+        float t = 0.0f;
+        if (cudaEventElapsedTime(&t, e.first, e.second) != cudaSuccess) return -1;
+        ms += t;
+        outPixels += ts.eventPixels[i];
+        ts.pool.push_back(e);
+    }
+    ts.events.clear();
+    ts.eventPixels.clear();
+    return 0;
+}
+
+const void* GB300Processor::tcWeights(Precision p, cudaStream_t stream)
+{
+    int idx = p == Precision::BF16 ? 1 : 0;
+    std::lock_guard<std::mutex> lock(mutex_);
+    if (!deviceWeights_[idx].ptr)
+    {
+        std::vector<uint16_t> packed;
+        pack_acnet_tc_weights(*acnet_, p == Precision::BF16, packed);
+        if (deviceWeights_[idx].ensure(packed.size() * sizeof(uint16_t)) != cudaSuccess) return nullptr;
+        cudaMemcpy(deviceWeights_[idx].ptr, packed.data(), packed.size() * sizeof(uint16_t), cudaMemcpyHostToDevice);
+    }
+    (void)stream;
+    return deviceWeights_[idx].ptr;
+}
+
+static inline int align_pitch(int bytes) { return (bytes + 255) & ~255; }
+
+static inline Plane plane_of(const DeviceImage& d)
+{
+    Plane p;
+    p.ptr = d.ptr;
+    p.w = d.w;
+    p.h = d.h;
+    p.pitch = d.stride;
+    p.channels = d.c;
+    p.type = d.type;
+    return p;
+}
+
+bool GB300Processor::validate(ThreadState& ts, int w, int h, int c, int type, double factor)
+{
+    if (w <= 0 || h <= 0) return fail(ts, "empty source image");
+    if (c != 1 && c != 3 && c != 4) return fail(ts, "unsupported channel count (1, 3 or 4)");
+    if (type != Image::UInt8 && type != Image::UInt16 && type != Image::Float32)
+        return fail(ts, "unsupported element type (u8, u16 or f32)");
+    if (!(factor > 0.0) || !std::isfinite(factor) || factor > 64.0) return fail(ts, "factor must be in (0, 64]");
+    int power = factor > 2.0 ? ceil_log2(factor) : 1;
+    double lw = static_cast<double>(w) * (1 << power), lh = static_cast<double>(h) * (1 << power);
+    if (lw * lh * c * (type & 0xff) > 2147483647.0) return fail(ts, "output image too large");
+    if (spec_.family != Family::ACNetLegacy) return fail(ts, "model not available in this build: " + spec_.name);
+    return true;
+}
+
+// Runs the pipeline between device images.  `dst` has the final shape.
+bool GB300Processor::run(ThreadState& ts, const DeviceImage& src, const DeviceImage& dst, double factor, cudaStream_t stream)
+{
+    const int c = src.c, type = src.type, es = type & 0xff;
+    const int power = factor > 2.0 ? ceil_log2(factor) : 1;
+    const double fxy = factor / static_cast<double>(1 << power);
+    const int lw = src.w << power, lh = src.h << power;
+    const bool lumaResize = (dst.w != lw) || (dst.h != lh);
+    cudaError_t err;
+
+    Plane cur;
+    Plane uv;
+    if (c == 1) cur = plane_of(src);
+    else
+    {
+        int yp = align_pitch(src.w * es), up = align_pitch(src.w * (c - 1) * es);
+        if ((err = ts.y.ensure(static_cast<size_t>(yp) * src.h)) != cudaSuccess) return fail(ts, "device allocation", err);
+        if ((err = ts.uv.ensure(static_cast<size_t>(up) * src.h)) != cudaSuccess) return fail(ts, "device allocation", err);
+        Plane rgb = plane_of(src);
+        cur = Plane{ts.y.ptr, src.w, src.h, yp, 1, type};
+        uv = Plane{ts.uv.ptr, src.w, src.h, up, c - 1, type};
+        if ((err = launch_rgb2yuv_split(rgb, cur, uv, stream)) != cudaSuccess) return fail(ts, "rgb2yuv", err);
+    }
+    const int lp = align_pitch(lw * es);
+    DeviceBuffer* pp[2] = {&ts.la, &ts.lb};
+    int which = 0;
+    for (int k = 0; k < power; k++)
+    {
+        Plane next;
+        const bool last = k == power - 1;
+        if (last && !lumaResize && c == 1) next = plane_of(dst);
+        else
+        {
+            if ((err = pp[which]->ensure(static_cast<size_t>(lp) * lh)) != cudaSuccess) return fail(ts, "device allocation", err);
+            next = Plane{pp[which]->ptr, cur.w * 2, cur.h * 2, align_pitch(cur.w * 2 * es), 1, type};
+            which ^= 1;
+        }
+        if ((err = luma_pass(ts, cur, next, stream)) != cudaSuccess) return fail(ts, "luma pass", err);
+        cur = next;
+    }
+    if (lumaResize)
+    {
+        Plane r;
+        if (c == 1) r = plane_of(dst);
+        else
+        {
+            if ((err = pp[which]->ensure(static_cast<size_t>(lp) * lh)) != cudaSuccess) return fail(ts, "device allocation", err);
+            r = Plane{pp[which]->ptr, dst.w, dst.h, align_pitch(dst.w * es), 1, type};
+        }
+        const ResizeAxis* ax = axis(ts, cur.w, r.w, 1, stream, err);
+        if (!ax) return fail(ts, "resize table", err);
+        const ResizeAxis* ay = axis(ts, cur.h, r.h, 1, stream, err);
+        if (!ay) return fail(ts, "resize table", err);
+        if ((err = launch_resize(cur, r, *ax, *ay, stream)) != cudaSuccess) return fail(ts, "luma resize", err);
+        cur = r;
+    }
+    if (c > 1)
+    {
+        const ResizeAxis* ax = axis(ts, src.w, dst.w, 1, stream, err);
+        if (!ax) return fail(ts, "resize table", err);
+        const ResizeAxis* ay = axis(ts, src.h, dst.h, 1, stream, err);
+        if (!ay) return fail(ts, "resize table", err);
+        if ((err = launch_merge_resize(cur, uv, *ax, *ay, plane_of(dst), stream)) != cudaSuccess)
+            return fail(ts, "yuv2rgb", err);
+    }
+    (void)fxy;
+    return true;
+}
+
+void GB300Processor::processHost(const Image& src, Image& dst, double factor)
+{
+    ThreadState& ts = state();
+    if (!begin(ts)) return;
+    if (src.empty())
+    {
+        fail(ts, "empty source image");
+        return;
+    }
+    if (!validate(ts, src.width(), src.height(), src.channels(), src.type(), factor)) return;
+    int ow, oh;
+    output_shape(src.width(), src.height(), src.channels(), factor, ow, oh);
+    if (!dst.empty())
+    {
+        // Processor.cpp:215-229: a preallocated gray dst whose size differs
+        // from the power-of-two result is reached by a final resize.
+        if (src.channels() == 1 && factor / static_cast<double>(1 << (factor > 2.0 ? ceil_log2(factor) : 1)) != 1.0)
+        {
+            ow = dst.width();
+            oh = dst.height();
+        }
+        if (dst.width() != ow || dst.height() != oh || dst.channels() != src.channels() || dst.type() != src.type())
+        {
+            fail(ts, "preallocated dst has the wrong shape or type");
+            return;
+        }
+    }
+    else
+    {
+        try
+        {
+            dst.create(ow, oh, src.channels(), src.type());
+        }
+        catch (...)
+        {
+            fail(ts, "host allocation failed");
+            return;
+        }
+    }
+    cudaStream_t stream = ts.stream;
+    cudaError_t err;
+    const int es = src.elementSize();
+    DeviceImage dsrc{nullptr, src.width(), src.height(), src.channels(), align_pitch(src.width() * src.pixelSize()), src.type()};
+    DeviceImage ddst{nullptr, ow, oh, src.channels(), align_pitch(ow * src.channels() * es), src.type()};
+    if ((err = ts.src.ensure(static_cast<size_t>(dsrc.stride) * dsrc.h)) != cudaSuccess) { fail(ts, "device allocation", err); return; }
+    if ((err = ts.out.ensure(static_cast<size_t>(ddst.stride) * ddst.h)) != cudaSuccess) { fail(ts, "device allocation", err); return; }
+    dsrc.ptr = ts.src.ptr;
+    ddst.ptr = ts.out.ptr;
+    err = cudaMemcpy2DAsync(dsrc.ptr, dsrc.stride, src.ptr(), src.stride(), static_cast<size_t>(src.width()) * src.pixelSize(),
+                            src.height(), cudaMemcpyHostToDevice, stream);
+    if (err != cudaSuccess) { fail(ts, "host to device copy", err); return; }
+    if (!run(ts, dsrc, ddst, factor, stream)) return;
+    err = cudaMemcpy2DAsync(dst.ptr(), dst.stride(), ddst.ptr, ddst.stride, static_cast<size_t>(ow) * dst.pixelSize(), oh,
+                            cudaMemcpyDeviceToHost, stream);
+    if (err != cudaSuccess) { fail(ts, "device to host copy", err); return; }
+    err = cudaStreamSynchronize(stream);
+    if (err != cudaSuccess) fail(ts, "kernel execution", err);
+}
+
+int GB300Processor::processDevice(const DeviceImage& src, const DeviceImage& dst, double factor, cudaStream_t stream, bool sync)
+{
+    ThreadState& ts = state();
+    if (!begin(ts)) return -1;
+    if (!src.ptr || !dst.ptr) return fail(ts, "null device pointer"), -1;
+    if (!validate(ts, src.w, src.h, src.c, src.type, factor)) return -1;
+    int ow, oh;
+    output_shape(src.w, src.h, src.c, factor, ow, oh);
+    if (src.c == 1 && factor / static_cast<double>(1 << (factor > 2.0 ? ceil_log2(factor) : 1)) != 1.0)
+    {
+        ow = dst.w;
+        oh = dst.h;
+    }
+    if (dst.w != ow || dst.h != oh || dst.c != src.c || dst.type != src.type) return fail(ts, "dst has the wrong shape or type"), -1;
+    cudaStream_t s = stream ? stream : ts.stream;
+    if (!run(ts, src, dst, factor, s)) return -1;
+    if (sync)
+    {
+        cudaError_t err = cudaStreamSynchronize(s);
+        if (err != cudaSuccess) return fail(ts, "kernel execution", err), -1;
+    }
+    return 0;
+}
+
+}  // namespace acgb

@@ -1,0 +1,102 @@
+// Internal definition of the GPU processor (shared by processor.cpp and the
+// C ABI translation unit).
+#pragma once
+
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <tuple>
+#include <unordered_map>
+#include <vector>
+
+#include "processor.hpp"
+
+namespace acgb {
+
+int ceil_log2(double v);
+void make_axis_table(int n_in, int n_out, int mode, std::vector<int>& first, std::vector<float>& weights, int& taps);
+
+// Grow-only device allocation.
+struct DeviceBuffer
+{
+    void* ptr = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes);
+    void release();
+};
+
+class GB300Processor final : public Processor
+{
+public:
+    GB300Processor(int device, const ModelSpec& spec);
+    ~GB300Processor() override;
+
+    bool ok() noexcept override;
+    const char* error() noexcept override;
+    const char* name() const noexcept override;
+
+    // Device-pointer entry: src/dst already in HBM; work is queued on
+    // `stream` (the calling thread's own stream when null).  Returns 0 or -1
+    // (details through ok()/error()).
+    int processDevice(const DeviceImage& src, const DeviceImage& dst, double factor, cudaStream_t stream, bool sync);
+
+    // Kernel timing of the luma passes with CUDA events recorded on the
+    // launching stream around each launch (for roofline figures).
+    void setProfiling(bool on);
+    int collectProfile(double& ms, int& launches, double& outPixels);
+
+    void setPrecision(Precision p) { precision_ = p; }
+    Precision precision() const { return precision_; }
+    int device() const { return device_; }
+    const ModelSpec& spec() const { return spec_; }
+
+protected:
+    void processHost(const Image& src, Image& dst, double factor) override;
+
+private:
+    struct AxisTable
+    {
+        std::vector<int> first;
+        std::vector<float> w;
+        int taps = 0;
+        DeviceBuffer dev;
+        ResizeAxis axis;
+    };
+    struct ThreadState
+    {
+        cudaStream_t stream = nullptr;
+        DeviceBuffer src, y, uv, la, lb, out;
+        std::map<std::tuple<int, int, int>, AxisTable> tables;
+        bool ok = true;
+        std::string err = "NO ERROR";
+        std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;  // recorded pairs
+        std::vector<double> eventPixels;                           // output pixels per pair
+        std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pool;     // free pairs
+    };
+
+    static Precision default_precision();
+    ThreadState& state();
+    bool begin(ThreadState& ts);
+    bool fail(ThreadState& ts, const std::string& what, cudaError_t err = cudaSuccess);
+    bool validate(ThreadState& ts, int w, int h, int c, int type, double factor);
+    bool run(ThreadState& ts, const DeviceImage& src, const DeviceImage& dst, double factor, cudaStream_t stream);
+    const ResizeAxis* axis(ThreadState& ts, int n_in, int n_out, int mode, cudaStream_t stream, cudaError_t& err);
+    cudaError_t luma_pass(ThreadState& ts, const Plane& in, const Plane& out, cudaStream_t stream);
+    const void* tcWeights(Precision p, cudaStream_t stream);
+
+    int device_ = -1;
+    int smCount_ = 0;
+    ModelSpec spec_;
+    std::string name_;
+    std::string initError_;
+    Precision precision_ = Precision::FP32;
+    bool profiling_ = false;
+    std::unique_ptr<AcnetLegacyWeights> acnet_;
+    DeviceBuffer deviceWeights_[2];
+    std::mutex mutex_;
+    std::unordered_map<std::thread::id, std::unique_ptr<ThreadState>> states_;
+};
+
+}  // namespace acgb

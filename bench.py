@@ -1,0 +1,401 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 upscaling backend (one JSON line on rank 0).
+
+Workload (the headline metric's configuration): 1920x1080 RGB u8 frames
+upscaled x2 to 3840x2160 by ACNetLegacy HDN0 through the full path (RGB->YUV
+split, luma CNN, Catmull-Rom chroma resize, YUV->RGB merge); 8 distinct
+frames per step, two alternating batches of 8 so each step's 50 MB of input
+and 200 MB of output exceed the 129 MB L2.  Inputs are seeded synthetic
+Voronoi-edge images (no public dataset is attached to this workload).
+
+  value  output Mpx/s with inputs resident in HBM (device-pointer entry point,
+         CUDA events on the launching stream)
+  e2e    the same metric through the C ABI with pinned host buffers, H2D and
+         D2H copies inside the timed region (several host threads share one
+         processor, as the reference CLI does)
+
+--impl reference times the reference CPU path instead (the reference CPU
+processor built from its sources where available, else the project's C
+restatement of it) on the host cores, one frame per step.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mpx/s out, 1080p→2160p ACNet: FP16-TC fused vs plain FP32; serve p50/p99 ms"
+MODEL = "acnet-legacy-hdn0"
+H, W, FACTOR = 1080, 1920, 2.0
+OH, OW = 2160, 3840
+FLOP_PER_OUT_PX = 2356.0  # ACNetLegacy x2: 9424 FLOP per input pixel
+WORKLOAD = "1920x1080 RGB u8 -> 3840x2160 x2, ACNetLegacy HDN0, full split/CNN/chroma/merge path"
+DATA = "synthetic: seeded 64-cell Voronoi-edge RGB u8 frames (blur 0.7, noise 2 LSB)"
+
+
+def env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def make_frames(n, seed=0):
+    from anime4kcpp_gb300 import synthetic
+    base = [synthetic.rgb_u8(H, W, cells=64, seed=seed + i) for i in range(min(n, 4))]
+    frames = []
+    for i in range(n):
+        b = base[i % len(base)]
+        frames.append(np.ascontiguousarray(np.roll(b, shift=(37 * (i // len(base)), 53 * (i // len(base))), axis=(0, 1))))
+    return frames
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_baseline(seconds=12.0):
+    """The reference CPU path on this host's cores over a bounded sample of the
+    workload: whole 1080p frames until ~`seconds` of work."""
+    import oracle
+    frame = make_frames(1, seed=100)[0]
+    cores = os.cpu_count() or 1
+    use_ref = False
+    if oracle.ref_available():
+        try:
+            oracle.ref()
+            use_ref = True
+        except OSError:
+            use_ref = False
+
+    def one():
+        if use_ref:
+            return oracle.ref_process(frame, FACTOR, MODEL, arch=0)
+        return oracle.process(frame, FACTOR, MODEL, threads=cores)
+
+    one()  # warm-up
+    n, t0 = 0, time.perf_counter()
+    while True:
+        one()
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or n >= 20:
+            break
+    return {"value": OW * OH * n / el / 1e6, "unit": "Mpx/s", "cores": cores,
+            "kind": "reference" if use_ref else "port",
+            "sample": "%d full 1920x1080 RGB u8 frames x2 (%.1f s)" % (n, el)}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return None
+    import oracle
+    frame = make_frames(1, seed=100)[0]
+    cores = os.cpu_count() or 1
+    use_ref = False
+    if oracle.ref_available():
+        try:
+            oracle.ref()
+            use_ref = True
+        except OSError:
+            use_ref = False
+    fn = (lambda: oracle.ref_process(frame, FACTOR, MODEL, arch=0)) if use_ref else \
+         (lambda: oracle.process(frame, FACTOR, MODEL, threads=cores))
+    for _ in range(args.warmup):
+        fn()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        fn()
+    el = time.perf_counter() - t0
+    value = OW * OH * args.steps / el / 1e6
+    kind = "reference" if use_ref else "port"
+    return {
+        "metric": METRIC, "value": value, "unit": "Mpx/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": DATA, "impl": "reference",
+        "config": {"workload": WORKLOAD, "frames_per_step": 1, "note": "bounded sample: one frame per step on host cores"},
+        "cpu_baseline": {"value": value, "unit": "Mpx/s", "cores": cores, "kind": kind,
+                         "sample": "%d steps of one 1920x1080 RGB u8 frame x2" % args.steps},
+        "e2e": {"value": value, "unit": "Mpx/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def time_device(ac, torch, proc, srcs, dsts, frames, steps, warmup, profile=False, clocks=None):
+    stream = torch.cuda.current_stream()
+    handle = stream.cuda_stream
+    nb = len(srcs) // frames
+
+    def step(i):
+        b = i % nb
+        for j in range(frames):
+            proc.process_device(srcs[b * frames + j], dsts[b * frames + j], FACTOR, stream=handle, sync=False)
+
+    for i in range(warmup):
+        step(i)
+    torch.cuda.synchronize()
+    if profile:
+        proc.profile(True)
+        proc.collect_profile()
+    launches0 = ac.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx = clocks if clocks is not None else _Null()
+    with ctx:
+        e0.record(stream)
+        for i in range(steps):
+            step(i)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = ac.launch_count() - launches0
+    prof = None
+    if profile:
+        prof = proc.collect_profile()
+        proc.profile(False)
+    if not proc.ok():
+        raise RuntimeError(proc.error())
+    return ms, launches, prof
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
+def time_e2e(ac, torch, proc, frames_host, outs_host, frames, steps, warmup, threads):
+    """Host API: every call copies its frame in, runs, copies the result out."""
+    per = frames // threads
+
+    def step_worker(t, i, errs):
+        for j in range(per):
+            k = (i % 2) * frames + t * per + j
+            proc.process(frames_host[k], FACTOR, dst=outs_host[k])
+            if not proc.ok():
+                errs.append(proc.error())
+
+    def step(i):
+        errs = []
+        ts = [threading.Thread(target=step_worker, args=(t, i, errs)) for t in range(threads)]
+        [t.start() for t in ts]
+        [t.join() for t in ts]
+        if errs:
+            raise RuntimeError(errs[0])
+
+    for i in range(warmup):
+        step(i)
+    t0 = time.perf_counter()
+    for i in range(steps):
+        step(i)
+    return time.perf_counter() - t0
+
+
+def run_gb300(args, rank, world, local_rank):
+    import torch
+
+    import anime4kcpp_gb300 as ac
+    from anime4kcpp_gb300 import build
+    build.build()
+    torch.cuda.set_device(local_rank)
+    frames = args.frames
+    host = make_frames(2 * frames, seed=10 * rank)
+    srcs = [torch.from_numpy(f).cuda() for f in host]
+    dsts = [torch.empty((OH, OW, 3), dtype=torch.uint8, device="cuda") for _ in host]
+
+    forms = {}
+    headline = None
+    for form in args.forms:
+        proc = ac.Processor("cuda", local_rank, MODEL, precision=form)
+        if not proc.ok():
+            raise RuntimeError(proc.error())
+        try:
+            time_device(ac, torch, proc, srcs[:frames], dsts[:frames], frames, 1, 1)
+        except RuntimeError as e:
+            forms[form] = {"unavailable": str(e)}
+            continue
+        is_head = headline is None
+        sampler = ClockSampler(local_rank) if is_head else None
+        steps = args.steps if is_head else max(3, args.steps // 2)
+        ms, launches, prof = time_device(ac, torch, proc, srcs, dsts, frames, steps, args.warmup, profile=True,
+                                         clocks=sampler)
+        out_px = OW * OH * frames * steps
+        rec = {"value": out_px / (ms / 1e3) / 1e6, "ms_per_step": ms / steps, "launches": launches,
+               "kernel_ms_per_launch": prof[0] / max(prof[1], 1), "kernel_launches": prof[1],
+               "kernel_out_px": prof[2], "steps": steps}
+        forms[form] = rec
+        if is_head:
+            headline = (form, proc, rec, sampler)
+
+    if headline is None:
+        raise RuntimeError("no arithmetic form ran: %s" % forms)
+    form, proc, rec, sampler = headline
+
+    # max over ranks of the headline time
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([rec["ms_per_step"]], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        rec["ms_per_step"] = float(t.item())
+        rec["value"] = OW * OH * frames * world / (rec["ms_per_step"] / 1e3) / 1e6
+
+    # end to end through the C ABI with pinned host buffers
+    pin_src = [torch.from_numpy(f).pin_memory() for f in host]
+    pin_dst = [torch.empty((OH, OW, 3), dtype=torch.uint8).pin_memory() for _ in host]
+    e2e_steps = max(2, args.steps // 2)
+    el = time_e2e(ac, torch, proc, [p.numpy() for p in pin_src], [p.numpy() for p in pin_dst], frames, e2e_steps,
+                  max(1, args.warmup // 2), args.e2e_threads)
+    e2e_value = OW * OH * frames * e2e_steps / el / 1e6
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([el], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_value = OW * OH * frames * e2e_steps * world / float(t.item()) / 1e6
+
+    peaks = measured_peaks()
+    kernel_s = rec["kernel_ms_per_launch"] / 1e3
+    flops_per_launch = FLOP_PER_OUT_PX * rec["kernel_out_px"] / max(rec["kernel_launches"], 1)
+    achieved = flops_per_launch / kernel_s / 1e12
+    props = torch.cuda.get_device_properties(local_rank)
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = 2.0 * 128 * props.multi_processor_count * sm_max * 1e6 / 1e12
+    traffic = None
+    tr_path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tr_path):
+        traffic = json.load(open(tr_path)).get(form)
+    if form == "fp32":
+        roofline = {"bound": "fp32-core", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                    "frac": achieved / fp32_peak, "traffic": traffic,
+                    "peak_source": "computed 2 x 128 FP32 lanes x %d SMs x %.0f MHz (not in MEASURED_PEAKS)" % (props.multi_processor_count, sm_max)}
+    else:
+        peak = float(peaks.get("bf16_tflops_sustained", 1700.0))
+        roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                    "traffic": traffic, "peak_source": "of measured (MEASURED_PEAKS.json bf16_tflops_sustained)"
+                    if "bf16_tflops_sustained" in peaks else "of fallback"}
+
+    out = {
+        "metric": METRIC, "value": rec["value"], "unit": "Mpx/s", "n_gpus": world, "steps": rec["steps"],
+        "warmup": args.warmup, "ms_per_step": rec["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if form == "fp32" else ("f16" if form == "fp16" else "bf16"),
+        "data": DATA,
+        "config": {"workload": WORKLOAD, "frames_per_step": frames, "form": form,
+                   "l2": "inputs larger than L2: 2 alternating batches of 8 distinct frames (50 MB in, 200 MB out per step)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": e2e_value, "unit": "Mpx/s", "h2d_bytes_per_step": H * W * 3 * frames,
+                "d2h_bytes_per_step": OH * OW * 3 * frames, "host_threads": args.e2e_threads},
+        "gpu_launches": rec["launches"],
+        "roofline": roofline,
+        "forms": {k: ({kk: round(vv, 4) if isinstance(vv, float) else vv for kk, vv in v.items()}) for k, v in forms.items()},
+    }
+    if "fp32" in forms and "value" in forms["fp32"]:
+        for tc in ("fp16", "bf16"):
+            if tc in forms and "value" in forms[tc]:
+                out["%s_over_fp32" % tc] = forms[tc]["value"] / forms["fp32"]["value"]
+    clocks = sampler.summary() if sampler else None
+    out["clocks"] = clocks
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--frames", type=int, default=8)
+    ap.add_argument("--forms", default="fp16,fp32,bf16")
+    ap.add_argument("--e2e-threads", type=int, default=4)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.forms = [f for f in args.forms.split(",") if f]
+    args.warmup = max(args.warmup, 3)
+
+    rank, world, local_rank = env_int("RANK", 0), env_int("WORLD_SIZE", 1), env_int("LOCAL_RANK", 0)
+    if args.impl == "reference":
+        res = run_reference(args, rank)
+        if res is not None:
+            print(json.dumps(res), flush=True)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+        dist.barrier()
+    res = run_gb300(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

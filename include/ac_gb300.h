@@ -1,0 +1,70 @@
+/*
+ * Extensions of the GB300 backend beyond the reference C ABI.
+ *
+ * None of these has a counterpart in the reference binding; they expose what
+ * a GPU-resident caller needs (device pointers, streams, arithmetic form) and
+ * what the tests and benchmarks need (model parameters, launch counts).
+ */
+#ifndef AC_GB300_EXT_H
+#define AC_GB300_EXT_H
+
+#include <stdint.h>
+
+#include "ac_processor.h"
+
+/* Arithmetic form of the 8->8 convolutions of the luma network. */
+enum ACGB300Precision
+{
+    AC_GB300_FP32 = 0, /* plain FP32 on CUDA cores (the parity form) */
+    AC_GB300_FP16 = 1, /* tcgen05 tensor cores, FP16 operands, FP32 accumulation */
+    AC_GB300_BF16 = 2  /* tcgen05 tensor cores, BF16 operands, FP32 accumulation */
+};
+
+/* A pitched image in device memory (same field meaning as ACImage). */
+typedef struct ACGB300DeviceImage
+{
+    void* ptr;
+    int width;
+    int height;
+    int channels;
+    int stride;
+    int element_type;
+} ACGB300DeviceImage;
+
+/* Selects the arithmetic form of a created processor.  The initial form is
+ * AC_GB300_FP32, or the one named by the environment variable
+ * AC_GB300_PRECISION ("fp32", "fp16", "bf16") at creation. */
+AC_C_API int ac_gb300_set_precision(ACProcessor* processor, int precision);
+AC_C_API int ac_gb300_get_precision(const ACProcessor* processor);
+
+/* Output size that ac_processor_process gives for an empty dst. */
+AC_C_API int ac_gb300_output_shape(int width, int height, int channels, double factor, int* out_width, int* out_height);
+
+/* Processor::process between device-resident images: src and dst are in HBM
+ * (dst preallocated with the output shape), all work is queued on `stream`
+ * (a cudaStream_t; NULL = the calling thread's stream of this processor).
+ * With sync != 0 the call waits for completion.  Returns AC_SUCCESS or
+ * AC_ERROR(AC_EPROCESSOR) / AC_ERROR(AC_EINVAL); details via
+ * ac_processor_error(). */
+AC_C_API int ac_gb300_process_device(ACProcessor* processor, const ACGB300DeviceImage* src, const ACGB300DeviceImage* dst,
+                                     double factor, void* stream, int sync);
+
+/* Kernel timing of the luma network passes: when enabled, the processor
+ * records a CUDA event pair on the launching stream around every luma-pass
+ * launch of the calling thread; ac_gb300_profile_collect waits for them and
+ * returns the summed milliseconds, the launch count and the summed output
+ * pixels of those launches, then clears the record. */
+AC_C_API int ac_gb300_profile_enable(ACProcessor* processor, int enable);
+AC_C_API int ac_gb300_profile_collect(ACProcessor* processor, double* ms, int* launches, double* out_pixels);
+
+/* Number of kernels this library has launched in the process so far. */
+AC_C_API uint64_t ac_gb300_launch_count(void);
+
+/* Copies the parameters of `model` (reference NHWC blob layout) into the
+ * given arrays when non-NULL and stores the element counts in counts[3]
+ * (kernels, biases, alphas).  Returns AC_ERROR(AC_EINVAL) for an unknown
+ * model or arrays that are too small. */
+AC_C_API int ac_gb300_model_params(const char* model, float* kernels, int kernels_len, float* biases, int biases_len,
+                                   float* alphas, int alphas_len, int* counts);
+
+#endif

@@ -61,10 +61,11 @@ def lib():
             L.orc_rgb2yuv.argtypes = [vp, i, i, i, i, i, vp, i, vp, i]
             L.orc_yuv2rgb.argtypes = [vp, i, vp, i, i, i, i, i, vp, i]
             L.orc_resize.argtypes = [vp, i, i, i, i, i, vp, i, i, i, i]
+            L.orc_resize_mt.argtypes = [vp, i, i, i, i, i, vp, i, i, i, i, i]
             L.orc_resize_coeffs.argtypes = [i, i, i, vp, vp, i]
             L.orc_arnet_synth.argtypes = [i, ctypes.c_uint64, fp, fp, fp]
             for fn in ("orc_acnet_legacy_x2", "orc_acnet_legacy_x2_f64", "orc_arnet_x2", "orc_arnet_x2_f64",
-                       "orc_rgb2yuv", "orc_yuv2rgb", "orc_resize", "orc_resize_coeffs", "orc_arnet_synth"):
+                       "orc_rgb2yuv", "orc_yuv2rgb", "orc_resize", "orc_resize_mt", "orc_resize_coeffs", "orc_arnet_synth"):
                 getattr(L, fn).restype = ctypes.c_int
             _lib = L
     return _lib
@@ -212,14 +213,15 @@ def yuv2rgb(y, uv):
     return out
 
 
-def resize(img, dw, dh, mode=RESIZE_CATMULL_ROM):
+def resize(img, dw, dh, mode=RESIZE_CATMULL_ROM, threads=0):
     img = _plane(img)
+    threads = threads or os.cpu_count() or 1
     squeeze = img.ndim == 2
     if squeeze:
         img = img[:, :, None]
     h, w, c = img.shape
     out = np.empty((dh, dw, c), img.dtype)
-    rc = lib().orc_resize(_p(img), w, h, c, img.strides[0], _TYPE_OF[img.dtype], _p(out), dw, dh, out.strides[0], mode)
+    rc = lib().orc_resize_mt(_p(img), w, h, c, img.strides[0], _TYPE_OF[img.dtype], _p(out), dw, dh, out.strides[0], mode, threads)
     assert rc == 0
     return out[:, :, 0] if squeeze else out
 

@@ -707,7 +707,8 @@ int orc_yuv2rgb(const void* y, int ystride, const void* uv, int uvstride, int w,
  * (ImageResize.cpp:269).  Sample placement: the centre of output pixel o maps
  * to source coordinate (o + 0.5) / scale - 0.5.  For downscaling the filter is
  * widened by 1/scale.  Weights are normalised to sum to 1.  Decode multiplies
- * by the reciprocal of the type's maximum; encode is fromFloat.  Horizontal
+ * by the reciprocal of the type's maximum; integer outputs are encoded with
+ * fromFloat, float outputs are stored unsaturated.  Horizontal
  * pass first (float intermediate), then vertical; taps are summed in
  * ascending source order.  mode: 1 = Catmull-Rom, 16 = bilinear, 0 = point. */
 
@@ -769,8 +770,63 @@ static inline float decode(const void* base, size_t idx, int type)
     }
 }
 
-int orc_resize(const void* src, int w, int h, int c, int sstride, int type,
-               void* dst, int dw, int dh, int dstride, int mode)
+typedef struct {
+    const void* src; int w, h, c, sstride, type;
+    void* dst; int dw, dh, dstride;
+    const int* fx; const int* fy; const float* wx; const float* wy; float* tmp; int mt; int stride;
+} rs_ctx;
+
+static void rs_h_rows(void* p, int y0, int y1)
+{
+    rs_ctx* k = (rs_ctx*)p;
+    for (int i = y0; i < y1; i++)
+    {
+        const void* row = rowp(k->src, k->sstride, i);
+        for (int o = 0; o < k->dw; o++)
+            for (int ch = 0; ch < k->c; ch++)
+            {
+                float s = 0.0f;
+                for (int t = 0; t < k->mt; t++)
+                {
+                    float wt = k->wx[(size_t)o * k->stride + t];
+                    if (wt == 0.0f) continue;
+                    int xi = k->fx[o] + t;
+                    xi = xi < 0 ? 0 : (xi > k->w - 1 ? k->w - 1 : xi);
+                    float m = wt * decode(row, (size_t)xi * k->c + ch, k->type);
+                    s = s + m;
+                }
+                k->tmp[((size_t)i * k->dw + o) * k->c + ch] = s;
+            }
+    }
+}
+
+static void rs_v_rows(void* p, int o0, int o1)
+{
+    rs_ctx* k = (rs_ctx*)p;
+    for (int o = o0; o < o1; o++)
+    {
+        void* row = rowpw(k->dst, k->dstride, o);
+        for (int x = 0; x < k->dw; x++)
+            for (int ch = 0; ch < k->c; ch++)
+            {
+                float s = 0.0f;
+                for (int t = 0; t < k->mt; t++)
+                {
+                    float wt = k->wy[(size_t)o * k->stride + t];
+                    if (wt == 0.0f) continue;
+                    int yi = k->fy[o] + t;
+                    yi = yi < 0 ? 0 : (yi > k->h - 1 ? k->h - 1 : yi);
+                    float m = wt * k->tmp[((size_t)yi * k->dw + x) * k->c + ch];
+                    s = s + m;
+                }
+                if (k->type == ORC_F32) ((float*)row)[(size_t)x * k->c + ch] = s; /* float output is not saturated */
+                else from_float(row, (size_t)x * k->c + ch, k->type, s);
+            }
+    }
+}
+
+int orc_resize_mt(const void* src, int w, int h, int c, int sstride, int type,
+                  void* dst, int dw, int dh, int dstride, int mode, int threads)
 {
     if (!src || !dst || w <= 0 || h <= 0 || dw <= 0 || dh <= 0 || c <= 0) return -22;
     const int MT = 64;
@@ -782,48 +838,21 @@ int orc_resize(const void* src, int w, int h, int c, int sstride, int type,
     if (!fx || !fy || !wx || !wy || !tmp) { free(fx); free(fy); free(wx); free(wy); free(tmp); return -12; }
     orc_resize_coeffs(w, dw, mode, fx, wx, MT);
     orc_resize_coeffs(h, dh, mode, fy, wy, MT);
-    /* horizontal */
-    for (int i = 0; i < h; i++)
-    {
-        const void* row = rowp(src, sstride, i);
-        for (int o = 0; o < dw; o++)
-            for (int ch = 0; ch < c; ch++)
-            {
-                float s = 0.0f;
-                for (int t = 0; t < MT; t++)
-                {
-                    float wt = wx[(size_t)o * MT + t];
-                    if (wt == 0.0f) continue;
-                    int xi = fx[o] + t;
-                    xi = xi < 0 ? 0 : (xi > w - 1 ? w - 1 : xi);
-                    float m = wt * decode(row, (size_t)xi * c + ch, type);
-                    s = s + m;
-                }
-                tmp[((size_t)i * dw + o) * c + ch] = s;
-            }
-    }
-    /* vertical */
-    for (int o = 0; o < dh; o++)
-    {
-        void* row = rowpw(dst, dstride, o);
-        for (int x = 0; x < dw; x++)
-            for (int ch = 0; ch < c; ch++)
-            {
-                float s = 0.0f;
-                for (int t = 0; t < MT; t++)
-                {
-                    float wt = wy[(size_t)o * MT + t];
-                    if (wt == 0.0f) continue;
-                    int yi = fy[o] + t;
-                    yi = yi < 0 ? 0 : (yi > h - 1 ? h - 1 : yi);
-                    float m = wt * tmp[((size_t)yi * dw + x) * c + ch];
-                    s = s + m;
-                }
-                from_float(row, (size_t)x * c + ch, type, s);
-            }
-    }
+    /* trim the tap count to the widest non-zero span */
+    int mt = 1;
+    for (int o = 0; o < dw; o++) for (int t = 0; t < MT; t++) if (wx[(size_t)o * MT + t] != 0.0f && t + 1 > mt) mt = t + 1;
+    for (int o = 0; o < dh; o++) for (int t = 0; t < MT; t++) if (wy[(size_t)o * MT + t] != 0.0f && t + 1 > mt) mt = t + 1;
+    rs_ctx k = { src, w, h, c, sstride, type, dst, dw, dh, dstride, fx, fy, wx, wy, tmp, mt, MT };
+    parallel_rows(rs_h_rows, &k, h, threads);   /* horizontal pass, float intermediate */
+    parallel_rows(rs_v_rows, &k, dh, threads);  /* vertical pass */
     free(fx); free(fy); free(wx); free(wy); free(tmp);
     return 0;
+}
+
+int orc_resize(const void* src, int w, int h, int c, int sstride, int type,
+               void* dst, int dw, int dh, int dstride, int mode)
+{
+    return orc_resize_mt(src, w, h, c, sstride, type, dst, dw, dh, dstride, mode, 1);
 }
 
 /* --------------------------------------------- synthetic ARNet parameters */

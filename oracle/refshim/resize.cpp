@@ -2,10 +2,12 @@
 // (core/src/ImageResize.cpp:136-273; stb is not vendored).  Size and aliasing
 // rules follow ImageResize.cpp:138-170 and :275-293; the sampling is this
 // project's restatement (orc_resize in oracle/acoracle.c).
+#include <thread>
+
 #include "AC/Core/Image.hpp"
 
-extern "C" int orc_resize(const void* src, int w, int h, int c, int sstride, int type,
-                          void* dst, int dw, int dh, int dstride, int mode);
+extern "C" int orc_resize_mt(const void* src, int w, int h, int c, int sstride, int type,
+                             void* dst, int dw, int dh, int dstride, int mode, int threads);
 
 namespace
 {
@@ -28,8 +30,8 @@ namespace
                 dst.create(dst.width(), dst.height(), src.channels(), src.type());
         }
         int m = (mode == ac::core::RESIZE_POINT) ? 0 : ((mode == ac::core::RESIZE_BILINEAR) ? 16 : 1);
-        orc_resize(src.ptr(), src.width(), src.height(), src.channels(), src.stride(), src.type(),
-                   dst.ptr(), dst.width(), dst.height(), dst.stride(), m);
+        orc_resize_mt(src.ptr(), src.width(), src.height(), src.channels(), src.stride(), src.type(),
+                      dst.ptr(), dst.width(), dst.height(), dst.stride(), m, static_cast<int>(std::thread::hardware_concurrency()));
     }
 }
 
