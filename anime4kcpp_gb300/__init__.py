@@ -58,6 +58,7 @@ EXPORTS = (
     "ac_processor_type_name", "ac_processor_info", "ac_processor_list_info",
     "ac_gb300_set_precision", "ac_gb300_get_precision", "ac_gb300_output_shape", "ac_gb300_process_device",
     "ac_gb300_launch_count", "ac_gb300_model_params", "ac_gb300_profile_enable", "ac_gb300_profile_collect",
+    "ac_gb300_tc_selftest",
 )
 
 _lock = threading.Lock()
@@ -96,6 +97,7 @@ def native():
             "ac_gb300_model_params": (I, [ctypes.c_char_p, V, I, V, I, V, I, P(I)]),
             "ac_gb300_profile_enable": (I, [pproc, I]),
             "ac_gb300_profile_collect": (I, [pproc, P(D), P(I), P(D)]),
+            "ac_gb300_tc_selftest": (I, [V, I, V, I, I, I, V]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -270,6 +272,16 @@ def resize(src, dsize=None, fx=0.0, fy=0.0, mode=RESIZE_BILINEAR):
     if out_ptr != dst.ctypes.data:
         raise RuntimeError("resize did not write into the destination buffer")
     return dst
+
+
+def tc_selftest(x, b, shift, bf16=False):
+    """Tensor-core self-test: x uint16 [px, 8], b uint16 [16, k]; returns (status, d[128, 16])."""
+    x = np.ascontiguousarray(x, np.uint16)
+    b = np.ascontiguousarray(b, np.uint16)
+    d = np.zeros((128, 16), np.float32)
+    rc = native().ac_gb300_tc_selftest(x.ctypes.data, x.shape[0], b.ctypes.data, b.shape[1], int(shift), 1 if bf16 else 0,
+                                       d.ctypes.data)
+    return rc, d
 
 
 def launch_count():

@@ -51,6 +51,8 @@ cudaError_t launch_acnet_legacy_fp32(const AcnetLegacyWeights& wts, const Plane&
 cudaError_t launch_acnet_legacy_tc(const AcnetLegacyWeights& wts, const void* packed, bool bf16, const Plane& in,
                                    const Plane& out, cudaStream_t stream);
 void pack_acnet_tc_weights(const AcnetLegacyWeights& wts, bool bf16, std::vector<uint16_t>& packed);
+// Reads and clears the tensor-core wait-timeout flag (1 = some wait gave up).
+int tc_status_reset();
 
 // RGB(A) -> Y + UV(A) (rgb2yuv / rgba2yuva of core/src/ImageProcess.cpp).
 cudaError_t launch_rgb2yuv_split(const Plane& rgb, const Plane& y, const Plane& uv, cudaStream_t stream);

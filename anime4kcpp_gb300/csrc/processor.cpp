@@ -608,7 +608,12 @@ void GB300Processor::processHost(const Image& src, Image& dst, double factor)
                             cudaMemcpyDeviceToHost, stream);
     if (err != cudaSuccess) { fail(ts, "device to host copy", err); return; }
     err = cudaStreamSynchronize(stream);
-    if (err != cudaSuccess) fail(ts, "kernel execution", err);
+    if (err != cudaSuccess)
+    {
+        fail(ts, "kernel execution", err);
+        return;
+    }
+    if (precision_ != Precision::FP32 && tc_status_reset() != 0) fail(ts, "tensor-core wait timed out");
 }
 
 int GB300Processor::processDevice(const DeviceImage& src, const DeviceImage& dst, double factor, cudaStream_t stream, bool sync)
@@ -631,6 +636,7 @@ int GB300Processor::processDevice(const DeviceImage& src, const DeviceImage& dst
     {
         cudaError_t err = cudaStreamSynchronize(s);
         if (err != cudaSuccess) return fail(ts, "kernel execution", err), -1;
+        if (precision_ != Precision::FP32 && tc_status_reset() != 0) return fail(ts, "tensor-core wait timed out"), -1;
     }
     return 0;
 }

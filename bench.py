@@ -184,7 +184,8 @@ def run_reference(args, rank):
 
 
 def time_device(ac, torch, proc, srcs, dsts, frames, steps, warmup, profile=False, clocks=None):
-    stream = torch.cuda.current_stream()
+    # A dedicated stream: the kernels and the timing events share it.
+    stream = torch.cuda.Stream()
     handle = stream.cuda_stream
     nb = len(srcs) // frames
 
@@ -208,6 +209,8 @@ def time_device(ac, torch, proc, srcs, dsts, frames, steps, warmup, profile=Fals
             step(i)
         e1.record(stream)
         torch.cuda.synchronize()
+        if clocks is not None:
+            time.sleep(0.05)
     ms = e0.elapsed_time(e1)
     launches = ac.launch_count() - launches0
     prof = None

@@ -57,6 +57,14 @@ AC_C_API int ac_gb300_process_device(ACProcessor* processor, const ACGB300Device
 AC_C_API int ac_gb300_profile_enable(ACProcessor* processor, int enable);
 AC_C_API int ac_gb300_profile_collect(ACProcessor* processor, double* ms, int* launches, double* out_pixels);
 
+/* Diagnostic: one tensor-core tile D[128][16] = A * B^T computed with the
+ * same tcgen05 descriptors, tensor-memory layout and completion protocol the
+ * kernels use.  A(m, k) = x[(m + (k / 8) * shift) * 8 + k % 8] (x holds px
+ * pixels of 8 16-bit values), b is [16][k] with k a multiple of 16 (<= 64),
+ * FP16 or (bf16 != 0) BF16 bit patterns; d receives [128][16] floats.
+ * Returns 0, 1 if the tensor core did not complete within 2 s, -1 on error. */
+AC_C_API int ac_gb300_tc_selftest(const uint16_t* x, int px, const uint16_t* b, int k, int shift, int bf16, float* d);
+
 /* Number of kernels this library has launched in the process so far. */
 AC_C_API uint64_t ac_gb300_launch_count(void);
 

@@ -1,0 +1,119 @@
+"""Tensor-core (tcgen05) form: building-block self-test and network accuracy
+(GPU required).
+
+The FP16/BF16 forms round the 8-channel activations and the 8->8 weights to
+16 bits; they are held to the precision targets of the headline workload:
+PSNR >= 50 dB against the FP64 oracle on u8 outputs and agreement with the
+reference CPU processor within +-1 LSB on >= 99 % of u8 pixels (FP16), never
+more than a few LSB anywhere.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import anime4kcpp_gb300 as ac
+import oracle
+from anime4kcpp_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = np.load(os.path.join(HERE, "golden", "golden.npz"))
+META = json.load(open(os.path.join(HERE, "golden", "golden.json")))["cases"]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from anime4kcpp_gb300 import build
+    build.build()
+    oracle.build()
+
+
+def to_bits(a, bf16):
+    a = np.asarray(a, np.float32)
+    if bf16:
+        u = a.view(np.uint32)
+        return ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+    return a.astype(np.float16).view(np.uint16)
+
+
+def from_bits(b, bf16):
+    if bf16:
+        return (b.astype(np.uint32) << 16).view(np.float32)
+    return b.view(np.float16).astype(np.float32)
+
+
+@pytest.mark.parametrize("bf16", [False, True])
+@pytest.mark.parametrize("shift,k", [(128, 32), (1, 16), (37, 32), (64, 64)])
+def test_tcgen05_tile_selftest(shift, k, bf16):
+    rng = np.random.default_rng(shift * 7 + k)
+    px = 128 + (k // 8 - 1) * shift + 8
+    x = to_bits(rng.uniform(-1, 1, size=(px, 8)), bf16)
+    b = to_bits(rng.uniform(-1, 1, size=(16, k)), bf16)
+    rc, d = ac.tc_selftest(x, b, shift, bf16)
+    assert rc == 0
+    xf, bf = from_bits(x, bf16).astype(np.float64), from_bits(b, bf16).astype(np.float64)
+    a = np.zeros((128, k))
+    for kk in range(k):
+        a[:, kk] = xf[np.arange(128) + (kk // 8) * shift, kk % 8]
+    want = a @ bf.T
+    assert np.abs(d - want).max() <= 1e-4 * max(1.0, np.abs(want).max())
+
+
+def psnr(got_u8, ref_f64):
+    err = got_u8.astype(np.float64) / 255.0 - np.clip(ref_f64, 0.0, 1.0)
+    mse = np.mean(err * err)
+    return 99.0 if mse == 0 else 10 * np.log10(1.0 / mse)
+
+
+@pytest.mark.parametrize("form", ["fp16", "bf16"])
+@pytest.mark.parametrize("shape", [(67, 95), (46, 46), (47, 93), (1, 30), (30, 1), (140, 200)])
+def test_tc_luma_vs_fp64_oracle(form, shape):
+    h, w = shape
+    x = synthetic.luma(h, w, np.uint8, seed=h * 131 + w)
+    ref64 = oracle.process_f64(x, "acnet-legacy-hdn1")
+    ref32 = oracle.process(x, 2.0, "acnet-legacy-hdn1")
+    p = ac.Processor("cuda", 0, "acnet-legacy-hdn1", precision=form)
+    got = p.process(x, 2.0)
+    assert p.ok(), p.error()
+    d = np.abs(got.astype(int) - ref32.astype(int))
+    if form == "fp16":
+        assert psnr(got, ref64) >= 50.0
+        assert (d <= 1).mean() >= 0.99
+        assert d.max() <= 4
+    else:
+        assert psnr(got, ref64) >= 40.0
+        assert d.max() <= 16
+
+
+@pytest.mark.parametrize("form", ["fp16", "bf16"])
+def test_tc_rgb_full_hd(form):
+    x = synthetic.rgb_u8(1080, 1920, cells=64, seed=2024)
+    ref32 = oracle.process(x, 2.0, "acnet-legacy-hdn0")
+    p = ac.Processor("cuda", 0, "acnet-legacy-hdn0", precision=form)
+    got = p.process(x, 2.0)
+    assert p.ok(), p.error()
+    d = np.abs(got.astype(int) - ref32.astype(int))
+    if form == "fp16":
+        assert (d <= 1).mean() >= 0.99
+        assert d.max() <= 6
+    else:
+        assert (d <= 2).mean() >= 0.95
+
+
+@pytest.mark.parametrize("case", [c for c in META if "arnet" not in c["model"]], ids=lambda c: c["name"])
+def test_tc_golden_fp16(case):
+    x = GOLD[case["name"] + "/in"]
+    want = GOLD[case["name"] + "/generic"]
+    p = ac.Processor("cuda", 0, case["model"], precision="fp16")
+    got = p.process(x, case["factor"])
+    assert p.ok(), p.error()
+    d = np.abs(got.astype(np.float64) - want.astype(np.float64))
+    if x.dtype == np.float32:
+        assert d.max() <= 5e-3
+    elif x.dtype == np.uint16:
+        assert d.max() <= 6 * 257
+    else:
+        assert d.max() <= 6
