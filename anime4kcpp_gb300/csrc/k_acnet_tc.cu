@@ -73,13 +73,6 @@ struct Params
     int* status;
 };
 
-__device__ __forceinline__ uint64_t gtimer()
-{
-    uint64_t t;
-    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-    return t;
-}
-
 // Pixel shift of tap t (row-major 3x3) in the flattened window.
 __device__ __forceinline__ int tap_shift(int t) { return (t / 3 - 1) * WIN + (t % 3 - 1); }
 
@@ -196,13 +189,10 @@ __global__ void __launch_bounds__(THREADS, 1) acnet_tc_kernel(const __grid_const
             }
             tc::mma_commit(mbar);
         }
-        // bounded wait for this layer's MMAs
-        bool done = false;
-        const uint64_t t0 = gtimer();
-        while (!(done = tc::mbar_try_wait(mbar, phase)))
-            if (gtimer() - t0 > 2000000000ull) break;
+        // bounded wait for this layer's MMAs, made CTA-uniform (tcgen05.ld is warp-collective)
+        const bool done = __syncthreads_and(tc::mbar_wait_ns(mbar, phase, 2000000000ull) ? 1 : 0) != 0;
         phase ^= 1;
-        if (!done) *abort_flag = 1;
+        if (!done && tid == 0) *abort_flag = 1;
         tc::fence_after_sync();
         if (done)
         {
@@ -336,16 +326,13 @@ void pack_acnet_tc_weights(const AcnetLegacyWeights& w, bool bf16, std::vector<u
     }
 }
 
-namespace {
-int* status_buffer()
+// Device word that a tensor-core kernel sets when a bounded wait gave up.
+int* tc_status_buffer()
 {
     static int* p = nullptr;
     if (!p && cudaMalloc(&p, sizeof(int)) == cudaSuccess) cudaMemset(p, 0, sizeof(int));
     return p;
 }
-}  // namespace
-
-int tc_status_reset();
 
 cudaError_t launch_acnet_legacy_tc(const AcnetLegacyWeights& wts, const void* packed, bool bf16, const Plane& in,
                                    const Plane& out, cudaStream_t stream)
@@ -360,7 +347,7 @@ cudaError_t launch_acnet_legacy_tc(const AcnetLegacyWeights& wts, const void* pa
     for (int i = 0; i < 32; i++) p.k2[i] = wts.k[72 + 576 * 8 + i];
     p.in = in;
     p.out = out;
-    p.status = status_buffer();
+    p.status = tc_status_buffer();
     if (!p.status) return cudaErrorMemoryAllocation;
     dim3 grid((in.w + TILE - 1) / TILE, (in.h + TILE - 1) / TILE);
     cudaError_t err;
@@ -378,7 +365,7 @@ cudaError_t launch_acnet_legacy_tc(const AcnetLegacyWeights& wts, const void* pa
 // Reads and clears the tensor-core timeout flag (1 if any MMA wait gave up).
 int tc_status_reset()
 {
-    int* p = status_buffer();
+    int* p = tc_status_buffer();
     if (!p) return -1;
     int v = 0;
     cudaMemcpy(&v, p, sizeof(int), cudaMemcpyDeviceToHost);

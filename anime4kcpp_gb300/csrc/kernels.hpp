@@ -54,6 +54,13 @@ void pack_acnet_tc_weights(const AcnetLegacyWeights& wts, bool bf16, std::vector
 // Reads and clears the tensor-core wait-timeout flag (1 = some wait gave up).
 int tc_status_reset();
 
+// Pair-interleaved tensor-core form (TMA input tile; needs a 16-byte aligned
+// input plane and pitch, see acnet_tc2_supported).
+bool acnet_tc2_supported(const Plane& in);
+cudaError_t launch_acnet_legacy_tc2(const AcnetLegacyWeights& wts, const void* packed2, bool bf16, const Plane& in,
+                                    const Plane& out, cudaStream_t stream);
+void pack_acnet_tc2_weights(const AcnetLegacyWeights& wts, bool bf16, std::vector<uint16_t>& packed);
+
 // RGB(A) -> Y + UV(A) (rgb2yuv / rgba2yuva of core/src/ImageProcess.cpp).
 cudaError_t launch_rgb2yuv_split(const Plane& rgb, const Plane& y, const Plane& uv, cudaStream_t stream);
 // Interleaved 3/4-channel RGB(A) -> interleaved YUV(A) in place or not.

@@ -222,6 +222,7 @@ const char* Processor::listInfo() { return info(CUDA); }
 GB300Processor::GB300Processor(int device, const ModelSpec& spec) : spec_(spec)
 {
     precision_ = default_precision();
+    if (const char* k = std::getenv("AC_GB300_TC_KERNEL")) tcKernel_ = std::atoi(k) == 1 ? 1 : 2;
     int n = 0;
     cudaError_t err = cudaGetDeviceCount(&n);
     if (err != cudaSuccess || n == 0)
@@ -404,8 +405,14 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
         if (precision_ == Precision::FP32) err = launch_acnet_legacy_fp32(*acnet_, in, out, stream);
         else
         {
-            const void* w = tcWeights(precision_, stream);
-            err = w ? launch_acnet_legacy_tc(*acnet_, w, precision_ == Precision::BF16, in, out, stream) : cudaErrorMemoryAllocation;
+            const bool bf16 = precision_ == Precision::BF16;
+            // The pair-interleaved TMA form needs a 16-byte aligned plane;
+            // other planes take the one-pixel-per-row form.
+            const bool v2 = tcKernel_ != 1 && acnet_tc2_supported(in);
+            const void* w = tcWeights(precision_, v2);
+            if (!w) err = cudaErrorMemoryAllocation;
+            else if (v2) err = launch_acnet_legacy_tc2(*acnet_, w, bf16, in, out, stream);
+            else err = launch_acnet_legacy_tc(*acnet_, w, bf16, in, out, stream);
         }
     }
     if (profiling_)
@@ -440,18 +447,24 @@ int GB300Processor::collectProfile(double& ms, int& launches, double& outPixels)
     return 0;
 }
 
-const void* GB300Processor::tcWeights(Precision p, cudaStream_t stream)
+const void* GB300Processor::tcWeights(Precision p, bool pairForm)
 {
-    int idx = p == Precision::BF16 ? 1 : 0;
+    const bool bf16 = p == Precision::BF16;
+    const int idx = (pairForm ? 2 : 0) + (bf16 ? 1 : 0);
     std::lock_guard<std::mutex> lock(mutex_);
     if (!deviceWeights_[idx].ptr)
     {
         std::vector<uint16_t> packed;
-        pack_acnet_tc_weights(*acnet_, p == Precision::BF16, packed);
+        if (pairForm) pack_acnet_tc2_weights(*acnet_, bf16, packed);
+        else pack_acnet_tc_weights(*acnet_, bf16, packed);
         if (deviceWeights_[idx].ensure(packed.size() * sizeof(uint16_t)) != cudaSuccess) return nullptr;
-        cudaMemcpy(deviceWeights_[idx].ptr, packed.data(), packed.size() * sizeof(uint16_t), cudaMemcpyHostToDevice);
+        if (cudaMemcpy(deviceWeights_[idx].ptr, packed.data(), packed.size() * sizeof(uint16_t), cudaMemcpyHostToDevice) !=
+            cudaSuccess)
+        {
+            deviceWeights_[idx].release();
+            return nullptr;
+        }
     }
-    (void)stream;
     return deviceWeights_[idx].ptr;
 }
 

@@ -84,7 +84,7 @@ private:
     bool run(ThreadState& ts, const DeviceImage& src, const DeviceImage& dst, double factor, cudaStream_t stream);
     const ResizeAxis* axis(ThreadState& ts, int n_in, int n_out, int mode, cudaStream_t stream, cudaError_t& err);
     cudaError_t luma_pass(ThreadState& ts, const Plane& in, const Plane& out, cudaStream_t stream);
-    const void* tcWeights(Precision p, cudaStream_t stream);
+    const void* tcWeights(Precision p, bool pairForm);
 
     int device_ = -1;
     int smCount_ = 0;
@@ -94,7 +94,8 @@ private:
     Precision precision_ = Precision::FP32;
     bool profiling_ = false;
     std::unique_ptr<AcnetLegacyWeights> acnet_;
-    DeviceBuffer deviceWeights_[2];
+    DeviceBuffer deviceWeights_[4];  // TC weights: {one-pixel, pair} x {FP16, BF16}
+    int tcKernel_ = 2;               // 1 forces the one-pixel-per-row TC kernel (AC_GB300_TC_KERNEL=1)
     std::mutex mutex_;
     std::unordered_map<std::thread::id, std::unique_ptr<ThreadState>> states_;
 };

@@ -128,6 +128,56 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mbar, uint32_t phase
     return false;
 }
 
+__device__ __forceinline__ uint64_t global_timer_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+// Wait on an mbarrier phase for at most `ns` nanoseconds.
+__device__ __forceinline__ bool mbar_wait_ns(uint64_t* mbar, uint32_t phase, uint64_t ns)
+{
+    if (mbar_try_wait(mbar, phase)) return true;
+    const uint64_t t0 = global_timer_ns();
+    while (!mbar_try_wait(mbar, phase))
+        if (global_timer_ns() - t0 > ns) return false;
+    return true;
+}
+
+// ---- TMA / bulk copies ----
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes) : "memory");
+}
+// 2-D tiled tensor load into shared memory; completion counted in bytes on mbar.
+// The innermost coordinate x times the element size must be a multiple of 16.
+__device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, int x, int y, uint64_t* mbar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(smem_u32(mbar))
+        : "memory");
+}
+// 2-D tiled tensor store from shared memory (bulk group); x, y >= 0.
+__device__ __forceinline__ void tma_store_2d(const void* tmap, int x, int y, const void* src)
+{
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                     reinterpret_cast<uint64_t>(tmap)),
+                 "r"(x), "r"(y), "r"(smem_u32(src))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// Plain bulk copy global -> shared (16-byte aligned addresses, size multiple of 16).
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* mbar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+                 "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(mbar))
+                 : "memory");
+}
+
 // ---- packing ----
 __device__ __forceinline__ uint32_t pack_relu_f16x2(float lo, float hi)
 {

@@ -1,0 +1,21 @@
+// Host helpers for TMA tensor maps.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace acgb {
+
+// True when a plane can be described by a tensor map: 16-byte aligned base
+// and pitch, and the driver offers the encoder.
+bool tma_plane_ok(const void* base, int pitch);
+
+// 2-D tiled tensor map over a pitched plane of dim_x elements per row
+// (elements of elem_bytes = 1, 2 or 4 bytes) and dim_y rows; box of
+// box_x x box_y elements (box_x * elem_bytes a multiple of 16), no swizzle,
+// out-of-bounds elements read as zero.
+bool encode_tmap_2d(CUtensorMap* map, const void* base, int elem_bytes, int dim_x, int dim_y, int pitch, int box_x, int box_y);
+
+}  // namespace acgb

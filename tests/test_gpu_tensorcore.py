@@ -68,9 +68,12 @@ def psnr(got_u8, ref_f64):
     return 99.0 if mse == 0 else 10 * np.log10(1.0 / mse)
 
 
+@pytest.mark.parametrize("kernel", ["1", "2"])
 @pytest.mark.parametrize("form", ["fp16", "bf16"])
-@pytest.mark.parametrize("shape", [(67, 95), (46, 46), (47, 93), (1, 30), (30, 1), (140, 200)])
-def test_tc_luma_vs_fp64_oracle(form, shape):
+@pytest.mark.parametrize("shape", [(67, 95), (46, 46), (47, 93), (1, 30), (30, 1), (140, 200), (45, 49), (89, 97)])
+def test_tc_luma_vs_fp64_oracle(form, shape, kernel, monkeypatch):
+    """kernel "1": one pixel per GEMM row; "2": pixel pairs with TMA staging."""
+    monkeypatch.setenv("AC_GB300_TC_KERNEL", kernel)
     h, w = shape
     x = synthetic.luma(h, w, np.uint8, seed=h * 131 + w)
     ref64 = oracle.process_f64(x, "acnet-legacy-hdn1")
@@ -88,8 +91,10 @@ def test_tc_luma_vs_fp64_oracle(form, shape):
         assert d.max() <= 16
 
 
+@pytest.mark.parametrize("kernel", ["1", "2"])
 @pytest.mark.parametrize("form", ["fp16", "bf16"])
-def test_tc_rgb_full_hd(form):
+def test_tc_rgb_full_hd(form, kernel, monkeypatch):
+    monkeypatch.setenv("AC_GB300_TC_KERNEL", kernel)
     x = synthetic.rgb_u8(1080, 1920, cells=64, seed=2024)
     ref32 = oracle.process(x, 2.0, "acnet-legacy-hdn0")
     p = ac.Processor("cuda", 0, "acnet-legacy-hdn0", precision=form)
@@ -103,8 +108,10 @@ def test_tc_rgb_full_hd(form):
         assert (d <= 2).mean() >= 0.95
 
 
+@pytest.mark.parametrize("kernel", ["1", "2"])
 @pytest.mark.parametrize("case", [c for c in META if "arnet" not in c["model"]], ids=lambda c: c["name"])
-def test_tc_golden_fp16(case):
+def test_tc_golden_fp16(case, kernel, monkeypatch):
+    monkeypatch.setenv("AC_GB300_TC_KERNEL", kernel)
     x = GOLD[case["name"] + "/in"]
     want = GOLD[case["name"] + "/generic"]
     p = ac.Processor("cuda", 0, case["model"], precision="fp16")
