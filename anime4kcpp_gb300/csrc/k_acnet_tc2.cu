@@ -174,11 +174,14 @@ acnet_tc2_kernel(const __grid_constant__ CUtensorMap in_map, const __grid_consta
     {
         const int y = 1 + i / (WW - 2), x = 1 + i % (WW - 2);
         const int cy = clampi(y, iy0, iy1), cx = clampi(x, ix0, ix1);
+        // the TMA tile holds zeros outside the image: clamp every tap
+        const int ty[3] = {max(cy - 1, iy0), cy, min(cy + 1, iy1)};
+        const int tx[3] = {xoff + max(cx - 1, ix0), xoff + cx, xoff + min(cx + 1, ix1)};
         float r[9];
 #pragma unroll
         for (int t = 0; t < 9; t++)
         {
-            const T v = raw[(cy + t / 3 - 1) * InBox<T>::w + xoff + cx + t % 3 - 1];
+            const T v = raw[ty[t / 3] * InBox<T>::w + tx[t % 3]];
             if constexpr (sizeof(T) == 1) r[t] = lut[v];
             else r[t] = to_float<T>(v);
         }
@@ -261,11 +264,22 @@ acnet_tc2_kernel(const __grid_constant__ CUtensorMap in_map, const __grid_consta
                         *slot(smem, p) = val;
                         // clamp-to-edge for the next layer: the out-of-image
                         // neighbours it reads get this edge value
-                        const int ex = (x == ix0 && x > 0) ? -1 : ((x == ix1 && x < WW - 1) ? 1 : 0);
-                        const int ey = (y == iy0 && y > 0) ? -1 : ((y == iy1 && y < WH - 1) ? 1 : 0);
-                        if (ex) *slot(smem, p + ex) = val;
-                        if (ey) *slot(smem, p + ey * WW) = val;
-                        if (ex && ey) *slot(smem, p + ey * WW + ex) = val;
+                        const bool xl = x == ix0 && x > 0, xr = x == ix1 && x < WW - 1;
+                        const bool yt = y == iy0 && y > 0, yb = y == iy1 && y < WH - 1;
+                        if (xl) *slot(smem, p - 1) = val;
+                        if (xr) *slot(smem, p + 1) = val;
+                        if (yt)
+                        {
+                            *slot(smem, p - WW) = val;
+                            if (xl) *slot(smem, p - WW - 1) = val;
+                            if (xr) *slot(smem, p - WW + 1) = val;
+                        }
+                        if (yb)
+                        {
+                            *slot(smem, p + WW) = val;
+                            if (xl) *slot(smem, p + WW - 1) = val;
+                            if (xr) *slot(smem, p + WW + 1) = val;
+                        }
                     }
                     else
                     {
