@@ -165,6 +165,94 @@ __global__ void merge_resize_kernel(Plane yp, Plane uvp, ResizeAxis ax, ResizeAx
     yuv_to_rgb_store<T, C>(yy, u, v, a, row_ptr_w<T>(rgb.ptr, rgb.pitch, y) + x * C);
 }
 
+// Integer-factor merge: the chroma plane (W x H) is resampled by exactly F on
+// both axes.  Output o = F*i + k samples source taps i + off[k] .. + 3 with
+// weights w[k][0..3] (phase k only), so one thread per source pixel computes
+// its F x F output block: horizontal sums for the rows it needs once, then the
+// vertical sums -- the same operations, in the same order, as the separable
+// table-driven path (horizontal pass per source row, ascending taps, then the
+// vertical pass), so the results are identical.
+template <int F>
+struct PhaseTable
+{
+    float w[F][4];
+};
+
+// First source tap of output phase k relative to the source index i:
+// ceil((k + 0.5) / F - 2.5) for the support-2 Catmull-Rom filter.
+template <int F>
+__host__ __device__ constexpr int phase_off(int k)
+{
+    return F == 2 ? (k == 0 ? -2 : -1) : (k < F / 2 ? -2 : -1);
+}
+
+template <typename T, int C, int F>
+__global__ void merge_int_kernel(Plane yp, Plane uvp, PhaseTable<F> tab, Plane rgb)
+{
+    const int sx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int sy = blockIdx.y;
+    if (sx >= uvp.w) return;
+    constexpr int UC = C - 1;
+    constexpr int RLO = -2, NR = 5;  // source rows sy-2 .. sy+2 cover every phase
+    float h[NR][F][UC];
+#pragma unroll
+    for (int rr = 0; rr < NR; rr++)
+    {
+        const T* row = row_ptr<T>(uvp.ptr, uvp.pitch, clampi(sy + RLO + rr, 0, uvp.h - 1));
+        T v[5][UC];
+#pragma unroll
+        for (int dx = 0; dx < 5; dx++)
+        {
+            const int xs = clampi(sx - 2 + dx, 0, uvp.w - 1);
+#pragma unroll
+            for (int c = 0; c < UC; c++) v[dx][c] = row[xs * UC + c];
+        }
+#pragma unroll
+        for (int k = 0; k < F; k++)
+#pragma unroll
+            for (int c = 0; c < UC; c++)
+            {
+                float s = 0.0f;
+#pragma unroll
+                for (int t = 0; t < 4; t++)
+                {
+                    const float wt = tab.w[k][t];
+                    if (wt == 0.0f) continue;
+                    s = __fadd_rn(s, __fmul_rn(wt, decode_float<T>(v[phase_off<F>(k) + t + 2][c])));
+                }
+                h[rr][k][c] = s;
+            }
+    }
+#pragma unroll
+    for (int j = 0; j < F; j++)
+    {
+        const int oy = F * sy + j;
+        const T* yrow = row_ptr<T>(yp.ptr, yp.pitch, oy);
+        T* orow = row_ptr_w<T>(rgb.ptr, rgb.pitch, oy);
+#pragma unroll
+        for (int k = 0; k < F; k++)
+        {
+            float uvv[UC];
+#pragma unroll
+            for (int c = 0; c < UC; c++)
+            {
+                float s = 0.0f;
+#pragma unroll
+                for (int t = 0; t < 4; t++)
+                {
+                    const float wt = tab.w[j][t];
+                    if (wt == 0.0f) continue;
+                    s = __fadd_rn(s, __fmul_rn(wt, h[phase_off<F>(j) + t - RLO][k][c]));
+                }
+                uvv[c] = to_float<T>(encode_resampled<T>(s));
+            }
+            const int ox = F * sx + k;
+            const float yy = to_float<T>(yrow[ox]);
+            yuv_to_rgb_store<T, C>(yy, uvv[0], uvv[1], C == 4 ? uvv[2] : 1.0f, orow + ox * C);
+        }
+    }
+}
+
 template <typename T, int NC>
 __global__ void resize_kernel(Plane src, Plane dst, ResizeAxis ax, ResizeAxis ay)
 {
@@ -233,6 +321,31 @@ cudaError_t launch_merge_resize(const Plane& y, const Plane& uv, ResizeAxis ax, 
         else merge_resize_kernel<T, 3><<<grid, 128, 0, stream>>>(y, uv, ax, ay, rgb);)
     count_launch();
     return cudaGetLastError();
+}
+
+template <int F>
+static cudaError_t launch_merge_int_f(const Plane& y, const Plane& uv, const float* wx, const Plane& rgb, cudaStream_t stream)
+{
+    PhaseTable<F> tab;
+    for (int k = 0; k < F; k++)
+        for (int t = 0; t < 4; t++) tab.w[k][t] = wx[k * 4 + t];
+    dim3 grid = row_grid(uv.w, uv.h, 128);
+    ACGB_TYPE_SWITCH(y.type,
+        if (rgb.channels == 4) merge_int_kernel<T, 4, F><<<grid, 128, 0, stream>>>(y, uv, tab, rgb);
+        else merge_int_kernel<T, 3, F><<<grid, 128, 0, stream>>>(y, uv, tab, rgb);)
+    count_launch();
+    return cudaGetLastError();
+}
+
+int merge_int_phase_offset(int factor, int k) { return factor == 2 ? phase_off<2>(k) : phase_off<4>(k); }
+
+cudaError_t launch_merge_int(const Plane& y, const Plane& uv, int factor, const float* phase_weights, const Plane& rgb,
+                             cudaStream_t stream)
+{
+    if (uv.w <= 0 || uv.h <= 0) return cudaSuccess;
+    if (factor == 2) return launch_merge_int_f<2>(y, uv, phase_weights, rgb, stream);
+    if (factor == 4) return launch_merge_int_f<4>(y, uv, phase_weights, rgb, stream);
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_resize(const Plane& src, const Plane& dst, ResizeAxis ax, ResizeAxis ay, cudaStream_t stream)

@@ -72,6 +72,13 @@ cudaError_t launch_yuv2rgb_packed(const Plane& yuv, const Plane& rgb, cudaStream
 cudaError_t launch_merge_resize(const Plane& y, const Plane& uv, ResizeAxis ax, ResizeAxis ay, const Plane& rgb,
                                 cudaStream_t stream);
 
+// Merge for chroma resampled by exactly `factor` (2 or 4) on both axes:
+// phase_weights[k*4 + t] is the Catmull-Rom weight of tap t of output phase k,
+// whose first tap is source index + merge_int_phase_offset(factor, k).
+cudaError_t launch_merge_int(const Plane& y, const Plane& uv, int factor, const float* phase_weights, const Plane& rgb,
+                             cudaStream_t stream);
+int merge_int_phase_offset(int factor, int k);
+
 // General separable resize of an interleaved plane (any channel count).
 cudaError_t launch_resize(const Plane& src, const Plane& dst, ResizeAxis ax, ResizeAxis ay, cudaStream_t stream);
 

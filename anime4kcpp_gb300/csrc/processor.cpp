@@ -107,6 +107,32 @@ void make_axis_table(int n_in, int n_out, int mode, std::vector<int>& first, std
         for (int t = 0; t < taps; t++) weights[static_cast<size_t>(o) * taps + t] = full[static_cast<size_t>(o) * MT + t];
 }
 
+// Catmull-Rom weights of an exact integer upscale, per output phase: output
+// o = F*i + k uses source taps i + merge_int_phase_offset(F, k) + 0..3.  The
+// weights do not depend on i (centres are exact binary fractions), which is
+// verified here on a table of 64 outputs; returns false if the table has any
+// other structure.
+bool phase_weights(int F, float* w)
+{
+    std::vector<int> first;
+    std::vector<float> wt;
+    int taps = 0;
+    make_axis_table(16, 16 * F, 1, first, wt, taps);
+    if (taps > 4) return false;
+    for (int o = 0; o < 16 * F; o++)
+    {
+        const int k = o % F;
+        if (first[o] - o / F != merge_int_phase_offset(F, k)) return false;
+        for (int t = 0; t < 4; t++)
+        {
+            const float v = t < taps ? wt[static_cast<size_t>(o) * taps + t] : 0.0f;
+            if (o < F) w[k * 4 + t] = v;
+            else if (v != w[k * 4 + t]) return false;
+        }
+    }
+    return true;
+}
+
 // ----------------------------------------------------------- DeviceBuffer
 
 cudaError_t DeviceBuffer::ensure(size_t bytes)
@@ -554,6 +580,13 @@ bool GB300Processor::run(ThreadState& ts, const DeviceImage& src, const DeviceIm
     }
     if (c > 1)
     {
+        const int F = (dst.w == 2 * src.w && dst.h == 2 * src.h) ? 2 : ((dst.w == 4 * src.w && dst.h == 4 * src.h) ? 4 : 0);
+        float pw[16];
+        if (F && phase_weights(F, pw))
+        {
+            if ((err = launch_merge_int(cur, uv, F, pw, plane_of(dst), stream)) != cudaSuccess) return fail(ts, "yuv2rgb", err);
+            return true;
+        }
         const ResizeAxis* ax = axis(ts, src.w, dst.w, 1, stream, err);
         if (!ax) return fail(ts, "resize table", err);
         const ResizeAxis* ay = axis(ts, src.h, dst.h, 1, stream, err);

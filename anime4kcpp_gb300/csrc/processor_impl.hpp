@@ -17,6 +17,7 @@ namespace acgb {
 
 int ceil_log2(double v);
 void make_axis_table(int n_in, int n_out, int mode, std::vector<int>& first, std::vector<float>& weights, int& taps);
+bool phase_weights(int F, float* w);
 
 // Grow-only device allocation.
 struct DeviceBuffer
