@@ -23,8 +23,14 @@
 // Weights are passed by value as a __grid_constant__ kernel parameter (19 KB,
 // constant bank 0); every layer is unrolled with compile-time weight offsets
 // so each FFMA takes its weight straight from the constant bank.
+//
+// RGB(A) inputs take the fused path: the staging step converts the RGB(A)
+// window to quantised Y (rgb2yuv) and keeps the UV(A) of the tile plus 2
+// pixels in shared memory; the last layer resamples it x2 (Catmull-Rom) and
+// merges it with the new luma (yuv2rgb), writing RGB(A) output directly.
 #include <cuda_runtime.h>
 
+#include "colour.cuh"
 #include "device_common.cuh"
 #include "kernels.hpp"
 
@@ -42,7 +48,20 @@ struct Smem
     float4 fb[2][BH][BW];
     float inp[WH][WW];
 };
-constexpr size_t kSmemBytes = sizeof(Smem);
+constexpr int UVW = TW + 4;          // chroma region: the tile plus 2 pixels each side
+constexpr int UVX0 = HALO - 2;       // its origin in window coordinates
+template <typename T, int C>
+constexpr size_t smem_bytes()
+{
+    return sizeof(Smem) + (C == 1 ? 0 : ((UVW * UVW * (C - 1) * sizeof(T) + 15) / 16 * 16));
+}
+
+// Fused-colour arguments of the kernel (small; the weights go separately).
+struct ColourArgs
+{
+    Plane in, out;
+    Phase2 ph;
+};
 
 // Layer 0: 1 -> 8 from the staged input window (edge-replicated at staging,
 // which equals clamped reads).
@@ -126,9 +145,10 @@ __device__ __forceinline__ void layer8(const AcnetLegacyWeights& W, const float4
 }
 
 // Layer 8 + deconv 2x2 stride 2 (8 -> 1, no bias) straight to global memory.
-template <typename T>
+template <typename T, int C>
 __device__ __forceinline__ void layer_last(const AcnetLegacyWeights& W, const float4 (*src)[BH][BW], const Plane& out,
-                                           int gx0, int gy0, int ix0, int ix1, int iy0, int iy1)
+                                           const T* uvs, const Phase2& ph, int gx0, int gy0, int ix0, int ix1, int iy0,
+                                           int iy1)
 {
     constexpr int L = 8;
     constexpr int K2 = 72 + 576 * 8;
@@ -144,10 +164,9 @@ __device__ __forceinline__ void layer_last(const AcnetLegacyWeights& W, const fl
         float s[8];
         conv8<L>(W, src, wx, wy, lox, hix, loy, hiy, s);
         const int ox = 2 * (gx0 + wx), oy = 2 * (gy0 + wy);
+        T o[2][2];
 #pragma unroll
         for (int dy = 0; dy < 2; dy++)
-        {
-            T o[2];
 #pragma unroll
             for (int dx = 0; dx < 2; dx++)
             {
@@ -155,21 +174,30 @@ __device__ __forceinline__ void layer_last(const AcnetLegacyWeights& W, const fl
                 float d = s[0] * W.k[ko];
 #pragma unroll
                 for (int c = 1; c < 8; c++) d = fmaf(s[c], W.k[ko + c], d);
-                o[dx] = from_float<T>(d);
+                o[dy][dx] = from_float<T>(d);
             }
-            T* row = row_ptr_w<T>(out.ptr, out.pitch, oy + dy) + ox;
-            row[0] = o[0];
-            row[1] = o[1];
+        T* row0 = row_ptr_w<T>(out.ptr, out.pitch, oy) + ox * C;
+        T* row1 = row_ptr_w<T>(out.ptr, out.pitch, oy + 1) + ox * C;
+        if constexpr (C == 1)
+        {
+            row0[0] = o[0][0];
+            row0[1] = o[0][1];
+            row1[0] = o[1][0];
+            row1[1] = o[1][1];
         }
+        else merge_block2<T, C>(uvs, UVW, wx - UVX0, wy - UVX0, ph, o, row0, row1);
     }
 }
 
-template <typename T>
+template <typename T, int C>
 __global__ void __launch_bounds__(THREADS, 1)
-acnet_legacy_fp32_kernel(const __grid_constant__ AcnetLegacyWeights W, const Plane in, const Plane out)
+acnet_legacy_fp32_kernel(const __grid_constant__ AcnetLegacyWeights W, const __grid_constant__ ColourArgs A)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem& S = *reinterpret_cast<Smem*>(smem_raw);
+    T* uvs = reinterpret_cast<T*>(smem_raw + sizeof(Smem));
+    const Plane& in = A.in;
+    const Plane& out = A.out;
 
     const int gx0 = blockIdx.x * TW - HALO, gy0 = blockIdx.y * TH - HALO;
     // Window range that lies inside the image (inclusive, window coordinates).
@@ -182,7 +210,24 @@ acnet_legacy_fp32_kernel(const __grid_constant__ AcnetLegacyWeights W, const Pla
     {
         const int wy = i / WW, wx = i % WW;
         const int gx = clampi(gx0 + wx, 0, in.w - 1), gy = clampi(gy0 + wy, 0, in.h - 1);
-        S.inp[wy][wx] = to_float<T>(row_ptr<T>(in.ptr, in.pitch, gy)[gx]);
+        if constexpr (C == 1) S.inp[wy][wx] = to_float<T>(row_ptr<T>(in.ptr, in.pitch, gy)[gx]);
+        else
+        {
+            // fused split: quantised Y (rgb2yuv) and, near the tile, UV(A)
+            const T* px = row_ptr<T>(in.ptr, in.pitch, gy) + gx * C;
+            T v[C];
+#pragma unroll
+            for (int c = 0; c < C; c++) v[c] = px[c];
+            T yq, uvq[C - 1];
+            rgb_to_yuv_q<T, C>(v, yq, uvq);
+            S.inp[wy][wx] = to_float<T>(yq);
+            const int ux = wx - UVX0, uy = wy - UVX0;
+            if (ux >= 0 && ux < UVW && uy >= 0 && uy < UVW)
+            {
+#pragma unroll
+                for (int c = 0; c < C - 1; c++) uvs[(uy * UVW + ux) * (C - 1) + c] = uvq[c];
+            }
+        }
     }
     __syncthreads();
     layer0(W, S, S.fa, ix0, ix1, iy0, iy1);
@@ -201,38 +246,61 @@ acnet_legacy_fp32_kernel(const __grid_constant__ AcnetLegacyWeights W, const Pla
     __syncthreads();
     layer8<7>(W, S.fa, S.fb, ix0, ix1, iy0, iy1);
     __syncthreads();
-    layer_last<T>(W, S.fb, out, gx0, gy0, ix0, ix1, iy0, iy1);
+    layer_last<T, C>(W, S.fb, out, uvs, A.ph, gx0, gy0, ix0, ix1, iy0, iy1);
 }
 
 }  // namespace fp32
 
-cudaError_t launch_acnet_legacy_fp32(const AcnetLegacyWeights& wts, const Plane& in, const Plane& out, cudaStream_t stream)
+namespace fp32 {
+template <typename T, int C>
+cudaError_t launch_typed(const AcnetLegacyWeights& wts, const ColourArgs& a, dim3 grid, cudaStream_t stream)
+{
+    constexpr size_t bytes = smem_bytes<T, C>();
+    static bool configured = false;
+    if (!configured)
+    {
+        cudaError_t err = cudaFuncSetAttribute(acnet_legacy_fp32_kernel<T, C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               static_cast<int>(bytes));
+        if (err != cudaSuccess) return err;
+        configured = true;
+    }
+    acnet_legacy_fp32_kernel<T, C><<<grid, THREADS, bytes, stream>>>(wts, a);
+    return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_channels(const AcnetLegacyWeights& wts, const ColourArgs& a, dim3 grid, cudaStream_t stream)
+{
+    switch (a.in.channels)
+    {
+    case 1: return launch_typed<T, 1>(wts, a, grid, stream);
+    case 3: return launch_typed<T, 3>(wts, a, grid, stream);
+    case 4: return launch_typed<T, 4>(wts, a, grid, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+}  // namespace fp32
+
+cudaError_t launch_acnet_legacy_fp32(const AcnetLegacyWeights& wts, const Plane& in, const Plane& out, const Phase2* phase2,
+                                     cudaStream_t stream)
 {
     using namespace fp32;
     if (in.w <= 0 || in.h <= 0) return cudaSuccess;
+    if (in.channels > 1 && !phase2) return cudaErrorInvalidValue;
+    ColourArgs a;
+    a.in = in;
+    a.out = out;
+    if (phase2) a.ph = *phase2;
     dim3 grid((in.w + TW - 1) / TW, (in.h + TH - 1) / TH);
-    cudaError_t err = cudaSuccess;
+    cudaError_t err;
     switch (in.type)
     {
-    case kU8:
-        err = cudaFuncSetAttribute(acnet_legacy_fp32_kernel<uint8_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
-        if (err != cudaSuccess) return err;
-        acnet_legacy_fp32_kernel<uint8_t><<<grid, THREADS, kSmemBytes, stream>>>(wts, in, out);
-        break;
-    case kU16:
-        err = cudaFuncSetAttribute(acnet_legacy_fp32_kernel<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
-        if (err != cudaSuccess) return err;
-        acnet_legacy_fp32_kernel<uint16_t><<<grid, THREADS, kSmemBytes, stream>>>(wts, in, out);
-        break;
-    case kF32:
-        err = cudaFuncSetAttribute(acnet_legacy_fp32_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
-        if (err != cudaSuccess) return err;
-        acnet_legacy_fp32_kernel<float><<<grid, THREADS, kSmemBytes, stream>>>(wts, in, out);
-        break;
+    case kU8: err = launch_channels<uint8_t>(wts, a, grid, stream); break;
+    case kU16: err = launch_channels<uint16_t>(wts, a, grid, stream); break;
+    case kF32: err = launch_channels<float>(wts, a, grid, stream); break;
     default: return cudaErrorInvalidValue;
     }
-    count_launch();
-    return cudaGetLastError();
+    if (err == cudaSuccess) count_launch();
+    return err;
 }
 
 }  // namespace acgb

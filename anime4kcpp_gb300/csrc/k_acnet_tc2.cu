@@ -31,11 +31,21 @@
 // neighbour the next layer reads (clamp-to-edge of the intermediate map).
 // The last layer keeps FP32, applies the 2x2 transposed convolution and
 // stores the outputs.
+//
+// RGB(A) inputs (C = 3 or 4) take the fused path: the prologue loads the
+// RGB(A) window with coalesced loads and derives the quantised Y window and
+// the UV(A) region (tile + 2 pixels) exactly as rgb2yuv does; the last
+// layer's epilogue resamples UV(A) x2 with Catmull-Rom and merges it with the
+// new luma (yuv2rgb), writing RGB(A) output directly.  No intermediate plane
+// touches HBM.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <cstring>
+
+#include "colour.cuh"
 #include "device_common.cuh"
 #include "kernels.hpp"
 #include "tc_ptx.cuh"
@@ -77,13 +87,18 @@ constexpr int B_OFF = ONES_OFF + ONES_BYTES;
 constexpr int IN_OFF = B_OFF + B_BYTES;
 static_assert(IN_OFF % 128 == 0, "TMA destination must be 128-byte aligned");
 
-template <typename T>
+constexpr int UVW = TW + 4, UVH = TH + 4;  // chroma region: the tile plus 2 pixels each side
+constexpr int UVX0 = HALO - 2, UVY0 = HALO - 2;  // its origin in window coordinates
+
+template <typename T, int C>
 struct Layout
 {
     static constexpr int in_bytes = (InBox<T>::bytes + 127) / 128 * 128;
     static constexpr int lut_off = IN_OFF + in_bytes;
     static constexpr int lut_bytes = sizeof(T) == 1 ? 1024 : 0;
-    static constexpr int misc_off = lut_off + lut_bytes;
+    static constexpr int uv_off = lut_off + lut_bytes;
+    static constexpr int uv_bytes = C == 1 ? 0 : (UVW * UVH * (C - 1) * static_cast<int>(sizeof(T)) + 15) / 16 * 16;
+    static constexpr int misc_off = uv_off + uv_bytes;
     static constexpr int smem = misc_off + 64;
 };
 
@@ -94,7 +109,9 @@ struct Params
     float b0[8];
     float k2[32];
     int w, h;         // input size
-    Plane out;
+    Plane in;         // RGB(A) input for C = 3, 4
+    Plane out;        // luma (C = 1) or RGB(A) output
+    Phase2 ph;        // x2 Catmull-Rom weights for the fused chroma
     int* status;
 };
 
@@ -118,13 +135,14 @@ __device__ __forceinline__ uint4* slot(unsigned char* smem, int p)
     return reinterpret_cast<uint4*>(smem + ((p & 1) ? O_OFF : E_OFF)) + PADP + (p >> 1);
 }
 
-template <typename T, bool BF16>
-__global__ void __launch_bounds__(THREADS, 1)
+template <typename T, int C, bool BF16>
+__global__ void __launch_bounds__(THREADS, 2)
 acnet_tc2_kernel(const __grid_constant__ CUtensorMap in_map, const __grid_constant__ Params P)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
-    using L = Layout<T>;
-    const T* raw = reinterpret_cast<const T*>(smem + IN_OFF);
+    using L = Layout<T, C>;
+    T* raw = reinterpret_cast<T*>(smem + IN_OFF);
+    T* uvs = reinterpret_cast<T*>(smem + L::uv_off);
     float* lut = reinterpret_cast<float*>(smem + L::lut_off);
     uint64_t* mbar_in = reinterpret_cast<uint64_t*>(smem + L::misc_off);
     uint64_t* mbar_mma = reinterpret_cast<uint64_t*>(smem + L::misc_off + 8);
@@ -137,7 +155,7 @@ acnet_tc2_kernel(const __grid_constant__ CUtensorMap in_map, const __grid_consta
     const int iy0 = max(0, -gy0), iy1 = min(WH - 1, P.h - 1 - gy0);
     // TMA origin: x rounded down to a 16-byte boundary (may be negative; zero fill)
     const int xal = gx0 >= 0 ? (gx0 / InBox<T>::align) * InBox<T>::align : -(((-gx0) + InBox<T>::align - 1) / InBox<T>::align) * InBox<T>::align;
-    const int xoff = gx0 - xal;
+    const int xoff = C == 1 ? gx0 - xal : 0;
 
     if (tid == 0)
     {
@@ -149,9 +167,36 @@ acnet_tc2_kernel(const __grid_constant__ CUtensorMap in_map, const __grid_consta
     __syncthreads();
     if (tid == 0)
     {
-        tc::mbar_arrive_expect_tx(mbar_in, static_cast<uint32_t>(InBox<T>::bytes + B_BYTES));
-        tc::tma_load_2d(smem + IN_OFF, &in_map, xal, gy0, mbar_in);
+        if constexpr (C == 1)
+        {
+            tc::mbar_arrive_expect_tx(mbar_in, static_cast<uint32_t>(InBox<T>::bytes + B_BYTES));
+            tc::tma_load_2d(smem + IN_OFF, &in_map, xal, gy0, mbar_in);
+        }
+        else tc::mbar_arrive_expect_tx(mbar_in, static_cast<uint32_t>(B_BYTES));
         tc::bulk_load(smem + B_OFF, P.bw, B_BYTES, mbar_in);
+    }
+    if constexpr (C > 1)
+    {
+        // fused split: quantised Y for the whole window, UV(A) for the chroma
+        // region; out-of-image positions take the clamped (edge) pixel
+        for (int i = tid; i < WW * WH; i += THREADS)
+        {
+            const int wy = i / WW, wx = i - (i / WW) * WW;
+            const int gx = clampi(gx0 + wx, 0, P.w - 1), gy = clampi(gy0 + wy, 0, P.h - 1);
+            T px[C];
+            const T* src = row_ptr<T>(P.in.ptr, P.in.pitch, gy) + gx * C;
+#pragma unroll
+            for (int c = 0; c < C; c++) px[c] = src[c];
+            T yq, uvq[C - 1];
+            rgb_to_yuv_q<T, C>(px, yq, uvq);
+            raw[wy * InBox<T>::w + wx] = yq;
+            const int ux = wx - UVX0, uy = wy - UVY0;
+            if (ux >= 0 && ux < UVW && uy >= 0 && uy < UVH)
+            {
+#pragma unroll
+                for (int c = 0; c < C - 1; c++) uvs[(uy * UVW + ux) * (C - 1) + c] = uvq[c];
+            }
+        }
     }
     if (tid < 129)
     {
@@ -287,10 +332,9 @@ acnet_tc2_kernel(const __grid_constant__ CUtensorMap in_map, const __grid_consta
 #pragma unroll
                         for (int c = 0; c < 8; c++) s[c] = fmaxf(v[8 * k + c], 0.0f);
                         const int ox = 2 * (gx0 + x), oy = 2 * (gy0 + y);
+                        T o[2][2];
 #pragma unroll
                         for (int dy = 0; dy < 2; dy++)
-                        {
-                            T o[2];
 #pragma unroll
                             for (int dx = 0; dx < 2; dx++)
                             {
@@ -298,12 +342,19 @@ acnet_tc2_kernel(const __grid_constant__ CUtensorMap in_map, const __grid_consta
                                 float d = s[0] * P.k2[ko];
 #pragma unroll
                                 for (int c = 1; c < 8; c++) d = fmaf(s[c], P.k2[ko + c], d);
-                                o[dx] = from_float<T>(d);
+                                o[dy][dx] = from_float<T>(d);
                             }
-                            T* row = row_ptr_w<T>(P.out.ptr, P.out.pitch, oy + dy) + ox;
-                            row[0] = o[0];
-                            row[1] = o[1];
+                        T* row0 = row_ptr_w<T>(P.out.ptr, P.out.pitch, oy) + ox * C;
+                        T* row1 = row_ptr_w<T>(P.out.ptr, P.out.pitch, oy + 1) + ox * C;
+                        if constexpr (C == 1)
+                        {
+                            row0[0] = o[0][0];
+                            row0[1] = o[0][1];
+                            row1[0] = o[1][0];
+                            row1[1] = o[1][1];
                         }
+                        else
+                            merge_block2<T, C>(uvs, UVW, x - UVX0, y - UVY0, P.ph, o, row0, row1);
                     }
                 }
             }
@@ -319,19 +370,31 @@ acnet_tc2_kernel(const __grid_constant__ CUtensorMap in_map, const __grid_consta
     if (warp == 0) tc::tmem_dealloc(tmem, TMEM_COLS);
 }
 
-template <typename T, bool BF16>
+template <typename T, int C, bool BF16>
 cudaError_t launch_typed(const CUtensorMap& map, const Params& p, dim3 grid, cudaStream_t stream)
 {
     static bool configured = false;
     if (!configured)
     {
-        cudaError_t err = cudaFuncSetAttribute(acnet_tc2_kernel<T, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               Layout<T>::smem);
+        cudaError_t err = cudaFuncSetAttribute(acnet_tc2_kernel<T, C, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               Layout<T, C>::smem);
         if (err != cudaSuccess) return err;
         configured = true;
     }
-    acnet_tc2_kernel<T, BF16><<<grid, THREADS, Layout<T>::smem, stream>>>(map, p);
+    acnet_tc2_kernel<T, C, BF16><<<grid, THREADS, Layout<T, C>::smem, stream>>>(map, p);
     return cudaGetLastError();
+}
+
+template <typename T, bool BF16>
+cudaError_t launch_channels(int c, const CUtensorMap& map, const Params& p, dim3 grid, cudaStream_t stream)
+{
+    switch (c)
+    {
+    case 1: return launch_typed<T, 1, BF16>(map, p, grid, stream);
+    case 3: return launch_typed<T, 3, BF16>(map, p, grid, stream);
+    case 4: return launch_typed<T, 4, BF16>(map, p, grid, stream);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 uint16_t to_bits(float v, bool bf16)
@@ -411,10 +474,10 @@ void pack_acnet_tc2_weights(const AcnetLegacyWeights& w, bool bf16, std::vector<
 
 int* tc_status_buffer();
 
-bool acnet_tc2_supported(const Plane& in) { return tma_plane_ok(in.ptr, in.pitch); }
+bool acnet_tc2_supported(const Plane& in) { return in.channels > 1 || tma_plane_ok(in.ptr, in.pitch); }
 
 cudaError_t launch_acnet_legacy_tc2(const AcnetLegacyWeights& wts, const void* packed2, bool bf16, const Plane& in,
-                                    const Plane& out, cudaStream_t stream)
+                                    const Plane& out, const Phase2* phase2, cudaStream_t stream)
 {
     using namespace tcv2;
     if (in.w <= 0 || in.h <= 0) return cudaSuccess;
@@ -422,8 +485,13 @@ cudaError_t launch_acnet_legacy_tc2(const AcnetLegacyWeights& wts, const void* p
     const int es = in.type & 0xff;
     const int boxw = es == 1 ? InBox<uint8_t>::w : (es == 2 ? InBox<uint16_t>::w : InBox<float>::w);
     CUtensorMap map;
-    if (!encode_tmap_2d(&map, in.ptr, es, in.w, in.h, in.pitch, boxw, WH)) return cudaErrorInvalidValue;
+    std::memset(&map, 0, sizeof(map));
+    if (in.channels == 1 && !encode_tmap_2d(&map, in.ptr, es, in.w, in.h, in.pitch, boxw, WH)) return cudaErrorInvalidValue;
+    if (in.channels > 1 && !phase2)
+        return cudaErrorInvalidValue;
     Params p;
+    if (phase2) p.ph = *phase2;
+    p.in = in;
     p.bw = static_cast<const uint4*>(packed2);
     for (int i = 0; i < 72; i++) p.k0[i] = wts.k[i];
     for (int i = 0; i < 8; i++) p.b0[i] = wts.b[i];
@@ -435,11 +503,12 @@ cudaError_t launch_acnet_legacy_tc2(const AcnetLegacyWeights& wts, const void* p
     if (!p.status) return cudaErrorMemoryAllocation;
     dim3 grid((in.w + TW - 1) / TW, (in.h + TH - 1) / TH);
     cudaError_t err;
+    const int c = in.channels;
     switch (in.type)
     {
-    case kU8: err = bf16 ? launch_typed<uint8_t, true>(map, p, grid, stream) : launch_typed<uint8_t, false>(map, p, grid, stream); break;
-    case kU16: err = bf16 ? launch_typed<uint16_t, true>(map, p, grid, stream) : launch_typed<uint16_t, false>(map, p, grid, stream); break;
-    case kF32: err = bf16 ? launch_typed<float, true>(map, p, grid, stream) : launch_typed<float, false>(map, p, grid, stream); break;
+    case kU8: err = bf16 ? launch_channels<uint8_t, true>(c, map, p, grid, stream) : launch_channels<uint8_t, false>(c, map, p, grid, stream); break;
+    case kU16: err = bf16 ? launch_channels<uint16_t, true>(c, map, p, grid, stream) : launch_channels<uint16_t, false>(c, map, p, grid, stream); break;
+    case kF32: err = bf16 ? launch_channels<float, true>(c, map, p, grid, stream) : launch_channels<float, false>(c, map, p, grid, stream); break;
     default: return cudaErrorInvalidValue;
     }
     if (err == cudaSuccess) count_launch();

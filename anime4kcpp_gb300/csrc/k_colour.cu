@@ -12,6 +12,7 @@
 // reference's scalar CPU code bit for bit.
 #include <atomic>
 
+#include "colour.cuh"
 #include "device_common.cuh"
 #include "kernels.hpp"
 
@@ -76,31 +77,6 @@ __global__ void rgb2yuv_packed_kernel(Plane rgb, Plane yuv)
     out[0] = from_float<T>(yy);
     out[1] = from_float<T>(u);
     out[2] = from_float<T>(v);
-    if constexpr (C == 4) out[3] = from_float<T>(a);
-}
-
-// yuv2rgb math on normalised inputs; writes C channels.
-template <typename T, int C>
-__device__ __forceinline__ void yuv_to_rgb_store(float yy, float u, float v, float a, T* out)
-{
-    u = __fsub_rn(u, 0.5f);
-    v = __fsub_rn(v, 0.5f);
-    float r = __fadd_rn(yy, __fmul_rn(1.403f, v));
-    float g = __fsub_rn(__fsub_rn(yy, __fmul_rn(0.344f, u)), __fmul_rn(0.714f, v));
-    float b = __fadd_rn(yy, __fmul_rn(1.773f, u));
-    if constexpr (C == 4)
-    {
-        if (a > 1e-6f)
-        {
-            r = __fdiv_rn(r, a);
-            g = __fdiv_rn(g, a);
-            b = __fdiv_rn(b, a);
-        }
-        else r = g = b = 0.0f;
-    }
-    out[0] = from_float<T>(r);
-    out[1] = from_float<T>(g);
-    out[2] = from_float<T>(b);
     if constexpr (C == 4) out[3] = from_float<T>(a);
 }
 

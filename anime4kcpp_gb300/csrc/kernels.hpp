@@ -40,9 +40,18 @@ struct ResizeAxis
     int taps = 0;
 };
 
+// Catmull-Rom weights of an exact x2 upscale by output phase (even, odd):
+// even outputs take source taps i-2 .. i+1, odd outputs i-1 .. i+2.
+struct Phase2
+{
+    float w[2][4];
+};
+
 // Plain FP32 layer-fused ACNetLegacy x2 pass: in (1 ch) -> out (1 ch, 2w x 2h),
-// same element type.  Returns the launch error.
-cudaError_t launch_acnet_legacy_fp32(const AcnetLegacyWeights& wts, const Plane& in, const Plane& out, cudaStream_t stream);
+// same element type; or, for a 3/4-channel RGB(A) input, the fused
+// split/CNN/chroma/merge pass writing RGB(A) (phase2 required).
+cudaError_t launch_acnet_legacy_fp32(const AcnetLegacyWeights& wts, const Plane& in, const Plane& out, const Phase2* phase2,
+                                     cudaStream_t stream);
 
 // Tensor-core (tcgen05) layer-fused ACNetLegacy x2 pass.  `packed` is the
 // device copy of pack_acnet_tc_weights(); bf16 selects BF16 operands
@@ -54,11 +63,13 @@ void pack_acnet_tc_weights(const AcnetLegacyWeights& wts, bool bf16, std::vector
 // Reads and clears the tensor-core wait-timeout flag (1 = some wait gave up).
 int tc_status_reset();
 
-// Pair-interleaved tensor-core form (TMA input tile; needs a 16-byte aligned
-// input plane and pitch, see acnet_tc2_supported).
+// Pair-interleaved tensor-core form.  A 1-channel input is staged by TMA and
+// needs a 16-byte aligned plane and pitch (acnet_tc2_supported); a 3/4-channel
+// RGB(A) input runs the fused split/merge path (phase2 required) and writes
+// RGB(A) output.
 bool acnet_tc2_supported(const Plane& in);
 cudaError_t launch_acnet_legacy_tc2(const AcnetLegacyWeights& wts, const void* packed2, bool bf16, const Plane& in,
-                                    const Plane& out, cudaStream_t stream);
+                                    const Plane& out, const Phase2* phase2, cudaStream_t stream);
 void pack_acnet_tc2_weights(const AcnetLegacyWeights& wts, bool bf16, std::vector<uint16_t>& packed);
 
 // RGB(A) -> Y + UV(A) (rgb2yuv / rgba2yuva of core/src/ImageProcess.cpp).

@@ -249,6 +249,7 @@ GB300Processor::GB300Processor(int device, const ModelSpec& spec) : spec_(spec)
 {
     precision_ = default_precision();
     if (const char* k = std::getenv("AC_GB300_TC_KERNEL")) tcKernel_ = std::atoi(k) == 1 ? 1 : 2;
+    if (const char* f = std::getenv("AC_GB300_FUSED")) fused_ = std::atoi(f) != 0;
     int n = 0;
     cudaError_t err = cudaGetDeviceCount(&n);
     if (err != cudaSuccess || n == 0)
@@ -408,7 +409,7 @@ const ResizeAxis* GB300Processor::axis(ThreadState& ts, int n_in, int n_out, int
     return &res.first->second.axis;
 }
 
-cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Plane& out, cudaStream_t stream)
+cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Plane& out, const Phase2* ph, cudaStream_t stream)
 {
     std::pair<cudaEvent_t, cudaEvent_t> ev{nullptr, nullptr};
     if (profiling_)
@@ -428,17 +429,19 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
     cudaError_t err = cudaErrorNotSupported;
     if (spec_.family == Family::ACNetLegacy)
     {
-        if (precision_ == Precision::FP32) err = launch_acnet_legacy_fp32(*acnet_, in, out, stream);
+        if (precision_ == Precision::FP32) err = launch_acnet_legacy_fp32(*acnet_, in, out, ph, stream);
         else
         {
             const bool bf16 = precision_ == Precision::BF16;
-            // The pair-interleaved TMA form needs a 16-byte aligned plane;
-            // other planes take the one-pixel-per-row form.
-            const bool v2 = tcKernel_ != 1 && acnet_tc2_supported(in);
+            // The pair-interleaved form stages 1-channel input by TMA (16-byte
+            // aligned plane) and runs the fused RGB(A) path; other 1-channel
+            // planes take the one-pixel-per-row form.
+            const bool v2 = (tcKernel_ != 1 || in.channels > 1) && acnet_tc2_supported(in);
             const void* w = tcWeights(precision_, v2);
             if (!w) err = cudaErrorMemoryAllocation;
-            else if (v2) err = launch_acnet_legacy_tc2(*acnet_, w, bf16, in, out, stream);
-            else err = launch_acnet_legacy_tc(*acnet_, w, bf16, in, out, stream);
+            else if (v2) err = launch_acnet_legacy_tc2(*acnet_, w, bf16, in, out, ph, stream);
+            else if (in.channels == 1) err = launch_acnet_legacy_tc(*acnet_, w, bf16, in, out, stream);
+            else err = cudaErrorInvalidValue;
         }
     }
     if (profiling_)
@@ -532,6 +535,25 @@ bool GB300Processor::run(ThreadState& ts, const DeviceImage& src, const DeviceIm
     const bool lumaResize = (dst.w != lw) || (dst.h != lh);
     cudaError_t err;
 
+    // Fused path: RGB(A) x2 in one kernel (split, CNN, chroma resample and
+    // merge), when the chroma resample is the exact x2 Catmull-Rom.
+    if (c > 1 && power == 1 && fxy == 1.0 && dst.w == 2 * src.w && dst.h == 2 * src.h && fused_)
+    {
+        Phase2 ph;
+        if (phase_weights(2, &ph.w[0][0]))
+        {
+            bool nonzero = true;
+            for (int k = 0; k < 2; k++)
+                for (int t = 0; t < 4; t++) nonzero = nonzero && ph.w[k][t] != 0.0f;
+            if (nonzero)
+            {
+                if ((err = luma_pass(ts, plane_of(src), plane_of(dst), &ph, stream)) != cudaSuccess)
+                    return fail(ts, "fused upscale", err);
+                return true;
+            }
+        }
+    }
+
     Plane cur;
     Plane uv;
     if (c == 1) cur = plane_of(src);
@@ -559,7 +581,7 @@ bool GB300Processor::run(ThreadState& ts, const DeviceImage& src, const DeviceIm
             next = Plane{pp[which]->ptr, cur.w * 2, cur.h * 2, align_pitch(cur.w * 2 * es), 1, type};
             which ^= 1;
         }
-        if ((err = luma_pass(ts, cur, next, stream)) != cudaSuccess) return fail(ts, "luma pass", err);
+        if ((err = luma_pass(ts, cur, next, nullptr, stream)) != cudaSuccess) return fail(ts, "luma pass", err);
         cur = next;
     }
     if (lumaResize)

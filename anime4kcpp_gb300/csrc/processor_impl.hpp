@@ -84,7 +84,7 @@ private:
     bool validate(ThreadState& ts, int w, int h, int c, int type, double factor);
     bool run(ThreadState& ts, const DeviceImage& src, const DeviceImage& dst, double factor, cudaStream_t stream);
     const ResizeAxis* axis(ThreadState& ts, int n_in, int n_out, int mode, cudaStream_t stream, cudaError_t& err);
-    cudaError_t luma_pass(ThreadState& ts, const Plane& in, const Plane& out, cudaStream_t stream);
+    cudaError_t luma_pass(ThreadState& ts, const Plane& in, const Plane& out, const Phase2* ph, cudaStream_t stream);
     const void* tcWeights(Precision p, bool pairForm);
 
     int device_ = -1;
@@ -96,6 +96,7 @@ private:
     bool profiling_ = false;
     std::unique_ptr<AcnetLegacyWeights> acnet_;
     DeviceBuffer deviceWeights_[4];  // TC weights: {one-pixel, pair} x {FP16, BF16}
+    bool fused_ = true;              // RGB(A) x2 in one fused kernel (AC_GB300_FUSED=0 disables)
     int tcKernel_ = 2;               // 1 forces the one-pixel-per-row TC kernel (AC_GB300_TC_KERNEL=1)
     std::mutex mutex_;
     std::unordered_map<std::thread::id, std::unique_ptr<ThreadState>> states_;

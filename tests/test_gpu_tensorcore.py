@@ -124,3 +124,23 @@ def test_tc_golden_fp16(case, kernel, monkeypatch):
         assert d.max() <= 6 * 257
     else:
         assert d.max() <= 6
+
+
+@pytest.mark.parametrize("form", ["fp32", "fp16", "bf16"])
+@pytest.mark.parametrize("c", [3, 4])
+@pytest.mark.parametrize("dtype", ["uint8", "uint16", "float32"])
+def test_fused_colour_path_matches_unfused(form, c, dtype, monkeypatch):
+    """RGB(A) x2 runs split + CNN + chroma resample + merge in one kernel; the
+    result must equal the separate split / CNN / merge kernels bit for bit."""
+    x = synthetic.rgb_u8(61, 83, seed=5, alpha=(c == 4))
+    if dtype == "uint16":
+        x = (x.astype(np.uint16) * 257).astype(np.uint16)
+    elif dtype == "float32":
+        x = (x.astype(np.float32) / 255.0).astype(np.float32)
+    outs = []
+    for fused in ("1", "0"):
+        monkeypatch.setenv("AC_GB300_FUSED", fused)
+        p = ac.Processor("cuda", 0, "acnet-legacy-hdn2", precision=form)
+        outs.append(p.process(x, 2.0))
+        assert p.ok(), p.error()
+    assert np.array_equal(outs[0], outs[1])
