@@ -165,4 +165,7 @@ def test_gpu_image_ops_vs_oracle():
 def test_launch_counter_advances():
     before = ac.launch_count()
     run("acnet-legacy-hdn0", synthetic.rgb_u8(32, 32, seed=0), 2.0)
-    assert ac.launch_count() - before == 3  # split, CNN pass, merge
+    assert ac.launch_count() - before == 1  # RGB x2: one fused kernel
+    before = ac.launch_count()
+    run("acnet-legacy-hdn0", synthetic.rgb_u8(32, 32, seed=0), 4.0)
+    assert ac.launch_count() - before == 4  # split, two CNN passes, x4 merge
