@@ -62,6 +62,85 @@ __device__ __forceinline__ void yuv_to_rgb_store(float yy, float u, float v, flo
     if constexpr (C == 4) out[3] = from_float<T>(a);
 }
 
+// toFloat through a table of the 256 u8 values (built with IEEE division, so
+// identical to to_float<uint8_t>); other types convert directly.
+template <typename T>
+__device__ __forceinline__ float to_float_lut(T v, const float* lut)
+{
+    if constexpr (sizeof(T) == 1) return lut[v];
+    else return to_float<T>(v);
+}
+
+template <typename T, int C>
+__device__ __forceinline__ void rgb_to_yuv_q_lut(const T* in, T& yq, T* uvq, const float* lut)
+{
+    float r = to_float_lut<T>(in[0], lut);
+    float g = to_float_lut<T>(in[1], lut);
+    float b = to_float_lut<T>(in[2], lut);
+    float a = 1.0f;
+    if constexpr (C == 4)
+    {
+        a = to_float_lut<T>(in[3], lut);
+        r = __fmul_rn(r, a);
+        g = __fmul_rn(g, a);
+        b = __fmul_rn(b, a);
+    }
+    const float yy = __fadd_rn(__fadd_rn(__fmul_rn(0.299f, r), __fmul_rn(0.587f, g)), __fmul_rn(0.114f, b));
+    const float u = __fadd_rn(__fmul_rn(0.564f, __fsub_rn(b, yy)), 0.5f);
+    const float v = __fadd_rn(__fmul_rn(0.713f, __fsub_rn(r, yy)), 0.5f);
+    yq = from_float<T>(yy);
+    uvq[0] = from_float<T>(u);
+    uvq[1] = from_float<T>(v);
+    if constexpr (C == 4) uvq[2] = from_float<T>(a);
+}
+
+// Horizontal pass of the x2 chroma resample for one region row: for output
+// column ox = 2*i + k (i = tile-local source column), the weighted sum of
+// region columns i + k .. i + k + 3 (the region starts two pixels left of the
+// tile), ascending.  H receives UC floats per output column.
+template <typename T, int UC>
+__device__ __forceinline__ void chroma_hpass(const T* uv_row, int i, int k, const Phase2& ph, float* h_out)
+{
+#pragma unroll
+    for (int c = 0; c < UC; c++)
+    {
+        float s = 0.0f;
+#pragma unroll
+        for (int t = 0; t < 4; t++) s = __fadd_rn(s, __fmul_rn(ph.w[k][t], decode_float<T>(uv_row[(i + k + t) * UC + c])));
+        h_out[c] = s;
+    }
+}
+
+// Vertical pass + merge for the 2x2 outputs of tile-local source pixel
+// (i, j): H holds the horizontal sums, rows = region rows (region row 0 is two
+// rows above the tile), hpitch output columns per row, UC floats each.
+template <typename T, int C>
+__device__ __forceinline__ void merge_block2_h(const float* H, int hpitch, int i, int j, const Phase2& ph, const T (&yq)[2][2],
+                                               T* out0, T* out1, const float* lut)
+{
+    constexpr int UC = C - 1;
+#pragma unroll
+    for (int dy = 0; dy < 2; dy++)
+    {
+        T* out = dy ? out1 : out0;
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+        {
+            float q[UC];
+#pragma unroll
+            for (int c = 0; c < UC; c++)
+            {
+                float s = 0.0f;
+#pragma unroll
+                for (int t = 0; t < 4; t++)
+                    s = __fadd_rn(s, __fmul_rn(ph.w[dy][t], H[((j + dy + t) * hpitch + 2 * i + k) * UC + c]));
+                q[c] = to_float_lut<T>(encode_resampled<T>(s), lut);
+            }
+            yuv_to_rgb_store<T, C>(to_float_lut<T>(yq[dy][k], lut), q[0], q[1], C == 4 ? q[2] : 1.0f, out + k * C);
+        }
+    }
+}
+
 // The 2x2 output block of source pixel (cx, cy): luma yq[dy][dx] (already
 // quantised) merged with the chroma of a UV(A) region `uv` (UC channels of
 // type T per pixel, `pitch` pixels per row; (cx, cy) in region coordinates

@@ -51,10 +51,16 @@ struct Smem
 constexpr int UVW = TW + 4;          // chroma region: the tile plus 2 pixels each side
 constexpr int UVX0 = HALO - 2;       // its origin in window coordinates
 template <typename T, int C>
-constexpr size_t smem_bytes()
+__host__ __device__ constexpr size_t uv_bytes()
 {
-    return sizeof(Smem) + (C == 1 ? 0 : ((UVW * UVW * (C - 1) * sizeof(T) + 15) / 16 * 16));
+    return C == 1 ? 0 : ((UVW * UVW * (C - 1) * sizeof(T) + 15) / 16 * 16);
 }
+template <typename T, int C>
+__host__ __device__ constexpr size_t smem_bytes()
+{
+    return sizeof(Smem) + uv_bytes<T, C>() + 1024;  // + u8 conversion table
+}
+static_assert(UVW * 2 * TW * 3 * 4 <= sizeof(float4) * 2 * BH * BW, "horizontal chroma sums must fit a feature buffer");
 
 // Fused-colour arguments of the kernel (small; the weights go separately).
 struct ColourArgs
@@ -147,8 +153,8 @@ __device__ __forceinline__ void layer8(const AcnetLegacyWeights& W, const float4
 // Layer 8 + deconv 2x2 stride 2 (8 -> 1, no bias) straight to global memory.
 template <typename T, int C>
 __device__ __forceinline__ void layer_last(const AcnetLegacyWeights& W, const float4 (*src)[BH][BW], const Plane& out,
-                                           const T* uvs, const Phase2& ph, int gx0, int gy0, int ix0, int ix1, int iy0,
-                                           int iy1)
+                                           const float* H, const float* lut, const Phase2& ph, int gx0, int gy0, int ix0,
+                                           int ix1, int iy0, int iy1)
 {
     constexpr int L = 8;
     constexpr int K2 = 72 + 576 * 8;
@@ -185,7 +191,7 @@ __device__ __forceinline__ void layer_last(const AcnetLegacyWeights& W, const fl
             row1[0] = o[1][0];
             row1[1] = o[1][1];
         }
-        else merge_block2<T, C>(uvs, UVW, wx - UVX0, wy - UVX0, ph, o, row0, row1);
+        else merge_block2_h<T, C>(H, 2 * TW, wx - HALO, wy - HALO, ph, o, row0, row1, lut);
     }
 }
 
@@ -196,8 +202,14 @@ acnet_legacy_fp32_kernel(const __grid_constant__ AcnetLegacyWeights W, const __g
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem& S = *reinterpret_cast<Smem*>(smem_raw);
     T* uvs = reinterpret_cast<T*>(smem_raw + sizeof(Smem));
+    float* lut = reinterpret_cast<float*>(smem_raw + sizeof(Smem) + uv_bytes<T, C>());
     const Plane& in = A.in;
     const Plane& out = A.out;
+    if constexpr (sizeof(T) == 1)
+    {
+        if (threadIdx.x < 256) lut[threadIdx.x] = __fdiv_rn(static_cast<float>(threadIdx.x), 255.0f);
+        __syncthreads();
+    }
 
     const int gx0 = blockIdx.x * TW - HALO, gy0 = blockIdx.y * TH - HALO;
     // Window range that lies inside the image (inclusive, window coordinates).
@@ -219,8 +231,8 @@ acnet_legacy_fp32_kernel(const __grid_constant__ AcnetLegacyWeights W, const __g
 #pragma unroll
             for (int c = 0; c < C; c++) v[c] = px[c];
             T yq, uvq[C - 1];
-            rgb_to_yuv_q<T, C>(v, yq, uvq);
-            S.inp[wy][wx] = to_float<T>(yq);
+            rgb_to_yuv_q_lut<T, C>(v, yq, uvq, lut);
+            S.inp[wy][wx] = to_float_lut<T>(yq, lut);
             const int ux = wx - UVX0, uy = wy - UVX0;
             if (ux >= 0 && ux < UVW && uy >= 0 && uy < UVW)
             {
@@ -246,7 +258,19 @@ acnet_legacy_fp32_kernel(const __grid_constant__ AcnetLegacyWeights W, const __g
     __syncthreads();
     layer8<7>(W, S.fa, S.fb, ix0, ix1, iy0, iy1);
     __syncthreads();
-    layer_last<T, C>(W, S.fb, out, uvs, A.ph, gx0, gy0, ix0, ix1, iy0, iy1);
+    float* H = reinterpret_cast<float*>(&S.fa[0][0][0]);  // dead after layer 7
+    if constexpr (C > 1)
+    {
+        // horizontal pass of the x2 chroma resample for the tile (region rows
+        // x output columns), shared by the per-pixel vertical passes
+        for (int e = threadIdx.x; e < UVW * 2 * TW; e += THREADS)
+        {
+            const int r = e / (2 * TW), ox = e - r * (2 * TW);
+            chroma_hpass<T, C - 1>(uvs + r * UVW * (C - 1), ox >> 1, ox & 1, A.ph, H + e * (C - 1));
+        }
+        __syncthreads();
+    }
+    layer_last<T, C>(W, S.fb, out, H, lut, A.ph, gx0, gy0, ix0, ix1, iy0, iy1);
 }
 
 }  // namespace fp32

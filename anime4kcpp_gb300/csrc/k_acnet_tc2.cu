@@ -89,6 +89,7 @@ static_assert(IN_OFF % 128 == 0, "TMA destination must be 128-byte aligned");
 
 constexpr int UVW = TW + 4, UVH = TH + 4;  // chroma region: the tile plus 2 pixels each side
 constexpr int UVX0 = HALO - 2, UVY0 = HALO - 2;  // its origin in window coordinates
+static_assert(UVH * 2 * TW * 3 * 4 <= 2 * PLANE_BYTES, "horizontal chroma sums must fit the activation planes");
 
 template <typename T, int C>
 struct Layout
@@ -164,6 +165,8 @@ acnet_tc2_kernel(const __grid_constant__ CUtensorMap in_map, const __grid_consta
         tc::fence_mbar_init();
         *abort_flag = 0;
     }
+    if constexpr (sizeof(T) == 1)
+        if (tid < 256) lut[tid] = __fdiv_rn(static_cast<float>(tid), 255.0f);
     __syncthreads();
     if (tid == 0)
     {
@@ -188,7 +191,7 @@ acnet_tc2_kernel(const __grid_constant__ CUtensorMap in_map, const __grid_consta
 #pragma unroll
             for (int c = 0; c < C; c++) px[c] = src[c];
             T yq, uvq[C - 1];
-            rgb_to_yuv_q<T, C>(px, yq, uvq);
+            rgb_to_yuv_q_lut<T, C>(px, yq, uvq, lut);
             raw[wy * InBox<T>::w + wx] = yq;
             const int ux = wx - UVX0, uy = wy - UVY0;
             if (ux >= 0 && ux < UVW && uy >= 0 && uy < UVH)
@@ -203,8 +206,6 @@ acnet_tc2_kernel(const __grid_constant__ CUtensorMap in_map, const __grid_consta
         const uint32_t one = BF16 ? 0x3F80u : 0x3C00u;
         reinterpret_cast<uint4*>(smem + ONES_OFF)[tid] = make_uint4(one | (one << 16), 0, 0, 0);
     }
-    if constexpr (sizeof(T) == 1)
-        if (tid < 256) lut[tid] = __fdiv_rn(static_cast<float>(tid), 255.0f);
     __syncthreads();
     // CTA-uniform outcome of the bounded wait for the input tile and weights
     if (!__syncthreads_and(tc::mbar_wait_ns(mbar_in, 0, 2000000000ull) ? 1 : 0))
@@ -289,6 +290,21 @@ acnet_tc2_kernel(const __grid_constant__ CUtensorMap in_map, const __grid_consta
         phase ^= 1;
         if (!done && tid == 0) *abort_flag = 1;
         tc::fence_after_sync();
+        float* H = reinterpret_cast<float*>(smem + E_OFF);  // last layer: the activations are dead
+        if constexpr (C > 1)
+        {
+            if (done && l == NL)
+            {
+                // horizontal pass of the x2 chroma resample for the whole tile,
+                // shared by the vertical passes of the epilogue below
+                for (int e = tid; e < UVH * 2 * TW; e += THREADS)
+                {
+                    const int r = e / (2 * TW), ox = e - r * (2 * TW);
+                    chroma_hpass<T, C - 1>(uvs + r * UVW * (C - 1), ox >> 1, ox & 1, P.ph, H + e * (C - 1));
+                }
+                __syncthreads();
+            }
+        }
         if (done)
         {
             for (int b = b0 + group; b <= b1; b += 4)
@@ -353,8 +369,7 @@ acnet_tc2_kernel(const __grid_constant__ CUtensorMap in_map, const __grid_consta
                             row1[0] = o[1][0];
                             row1[1] = o[1][1];
                         }
-                        else
-                            merge_block2<T, C>(uvs, UVW, x - UVX0, y - UVY0, P.ph, o, row0, row1);
+                        else merge_block2_h<T, C>(H, 2 * TW, x - HALO, y - HALO, P.ph, o, row0, row1, lut);
                     }
                 }
             }
