@@ -83,6 +83,12 @@ cudaError_t launch_yuv2rgb_packed(const Plane& yuv, const Plane& rgb, cudaStream
 cudaError_t launch_merge_resize(const Plane& y, const Plane& uv, ResizeAxis ax, ResizeAxis ay, const Plane& rgb,
                                 cudaStream_t stream);
 
+// ARNet<8> x2 pass in plain FP32 (one kernel per layer): parameters in the
+// reference blob layout (ARNet.hpp:26-70), `blocks` residual blocks, four
+// [h][w][8] float work maps of the input size.
+cudaError_t launch_arnet_fp32(const float* kernels, const float* biases, const float* alphas, int blocks, const Plane& in,
+                              const Plane& out, float* const maps[4], cudaStream_t stream);
+
 // Merge for chroma resampled by exactly `factor` (2 or 4) on both axes:
 // phase_weights[k*4 + t] is the Catmull-Rom weight of tap t of output phase k,
 // whose first tap is source index + merge_int_phase_offset(factor, k).

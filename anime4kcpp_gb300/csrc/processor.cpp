@@ -312,6 +312,7 @@ GB300Processor::~GB300Processor()
         ts.la.release();
         ts.lb.release();
         ts.out.release();
+        for (auto& m : ts.maps) m.release();
         for (auto& t : ts.tables) t.second.dev.release();
         for (auto& e : ts.events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
         for (auto& e : ts.pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -427,7 +428,20 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
         cudaEventRecord(ev.first, stream);
     }
     cudaError_t err = cudaErrorNotSupported;
-    if (spec_.family == Family::ACNetLegacy)
+    if (spec_.family == Family::ARNet)
+    {
+        // ARNet runs the plain FP32 layer pipeline in every precision form.
+        const size_t bytes = static_cast<size_t>(in.w) * in.h * 8 * sizeof(float);
+        float* maps[4];
+        for (int i = 0; i < 4; i++)
+        {
+            if ((err = ts.maps[i].ensure(bytes)) != cudaSuccess) return err;
+            maps[i] = static_cast<float*>(ts.maps[i].ptr);
+        }
+        const ModelParams& mp = model_params(spec_);
+        err = launch_arnet_fp32(mp.kernels.data(), mp.biases.data(), mp.alphas.data(), spec_.blocks, in, out, maps, stream);
+    }
+    else if (spec_.family == Family::ACNetLegacy)
     {
         if (precision_ == Precision::FP32) err = launch_acnet_legacy_fp32(*acnet_, in, out, ph, stream);
         else
@@ -521,7 +535,6 @@ bool GB300Processor::validate(ThreadState& ts, int w, int h, int c, int type, do
     int power = factor > 2.0 ? ceil_log2(factor) : 1;
     double lw = static_cast<double>(w) * (1 << power), lh = static_cast<double>(h) * (1 << power);
     if (lw * lh * c * (type & 0xff) > 2147483647.0) return fail(ts, "output image too large");
-    if (spec_.family != Family::ACNetLegacy) return fail(ts, "model not available in this build: " + spec_.name);
     return true;
 }
 
@@ -537,7 +550,8 @@ bool GB300Processor::run(ThreadState& ts, const DeviceImage& src, const DeviceIm
 
     // Fused path: RGB(A) x2 in one kernel (split, CNN, chroma resample and
     // merge), when the chroma resample is the exact x2 Catmull-Rom.
-    if (c > 1 && power == 1 && fxy == 1.0 && dst.w == 2 * src.w && dst.h == 2 * src.h && fused_)
+    if (c > 1 && power == 1 && fxy == 1.0 && dst.w == 2 * src.w && dst.h == 2 * src.h && fused_ &&
+        spec_.family == Family::ACNetLegacy)
     {
         Phase2 ph;
         if (phase_weights(2, &ph.w[0][0]))

@@ -69,6 +69,7 @@ private:
     {
         cudaStream_t stream = nullptr;
         DeviceBuffer src, y, uv, la, lb, out;
+        DeviceBuffer maps[4];  // ARNet feature maps
         std::map<std::tuple<int, int, int>, AxisTable> tables;
         bool ok = true;
         std::string err = "NO ERROR";

@@ -52,10 +52,7 @@ def run(model, x, factor, precision="fp32"):
     return out
 
 
-ACNET_CASES = [c for c in META if "arnet" not in c["model"]]
-
-
-@pytest.mark.parametrize("case", ACNET_CASES, ids=[c["name"] for c in ACNET_CASES])
+@pytest.mark.parametrize("case", META, ids=[c["name"] for c in META])
 def test_golden_fp32(case):
     x = GOLD[case["name"] + "/in"]
     want = GOLD[case["name"] + "/generic"]
@@ -169,3 +166,29 @@ def test_launch_counter_advances():
     before = ac.launch_count()
     run("acnet-legacy-hdn0", synthetic.rgb_u8(32, 32, seed=0), 4.0)
     assert ac.launch_count() - before == 4  # split, two CNN passes, x4 merge
+
+
+@pytest.mark.parametrize("model", ["arnet-b8", "arnet-hdn-b16", "arnet-box-b32", "arnet-box-hdn-b64"])
+@pytest.mark.parametrize("dtype", ["uint8", "uint16", "float32"])
+def test_arnet_vs_oracle(model, dtype):
+    """ARNet<8> (seeded synthetic parameters) through the C ABI."""
+    h, w = 37, 53
+    if dtype == "float32":
+        x = synthetic.f32_luma_uniform(h, w, seed=3)
+    elif dtype == "uint16":
+        x = (synthetic.luma(h, w, np.uint16, seed=3, noise=4.0, bits=10) << 6).astype(np.uint16)
+    else:
+        x = synthetic.luma(h, w, np.uint8, seed=3)
+    want = oracle.process(x, 2.0, model)
+    got = run(model, x, 2.0)
+    check_close(got, want, x.dtype)
+
+
+def test_arnet_x4_u16_video_recipe():
+    """The video recipe of the reference CLI (cli/src/Main.cpp:183-206): 10-bit
+    luma shifted up by 6, x4 as two chained x2 passes."""
+    y10 = synthetic.luma(68, 120, np.uint16, seed=11, noise=4.0, bits=10)
+    x = (y10 << 6).astype(np.uint16)
+    want = oracle.process(x, 4.0, "arnet-b8")
+    got = run("arnet-b8", x, 4.0)
+    check_close(got, want, x.dtype)
