@@ -328,7 +328,8 @@ def run_gb300(args, rank, world, local_rank):
     traffic = None
     tr_path = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tr_path):
-        traffic = json.load(open(tr_path)).get(form)
+        rec_t = json.load(open(tr_path)).get(form)
+        traffic = rec_t.get("bytes") if isinstance(rec_t, dict) else rec_t
     if form == "fp32":
         roofline = {"bound": "fp32-core", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                     "frac": achieved / fp32_peak, "traffic": traffic,
