@@ -72,6 +72,14 @@ cudaError_t launch_acnet_legacy_tc2(const AcnetLegacyWeights& wts, const void* p
                                     const Plane& out, const Phase2* phase2, cudaStream_t stream);
 void pack_acnet_tc2_weights(const AcnetLegacyWeights& wts, bool bf16, std::vector<uint16_t>& packed);
 
+// Persistent warp-specialised tensor-core form over a tile queue of n images
+// (same type and channel count, every output 2x its input); packed2 as for
+// the pair-interleaved form.  `counter` is a device int (zeroed by the call
+// on `stream`); `ctas` = CTAs to launch (one per SM).
+int acnet_tc3_max_images();
+cudaError_t launch_acnet_legacy_tc3(const AcnetLegacyWeights& wts, const void* packed2, bool bf16, int n, const Plane* in,
+                                    const Plane* out, const Phase2* phase2, int* counter, int ctas, cudaStream_t stream);
+
 // RGB(A) -> Y + UV(A) (rgb2yuv / rgba2yuva of core/src/ImageProcess.cpp).
 cudaError_t launch_rgb2yuv_split(const Plane& rgb, const Plane& y, const Plane& uv, cudaStream_t stream);
 // Interleaved 3/4-channel RGB(A) -> interleaved YUV(A) in place or not.

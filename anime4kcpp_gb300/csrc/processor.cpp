@@ -248,7 +248,11 @@ const char* Processor::listInfo() { return info(CUDA); }
 GB300Processor::GB300Processor(int device, const ModelSpec& spec) : spec_(spec)
 {
     precision_ = default_precision();
-    if (const char* k = std::getenv("AC_GB300_TC_KERNEL")) tcKernel_ = std::atoi(k) == 1 ? 1 : 2;
+    if (const char* k = std::getenv("AC_GB300_TC_KERNEL"))
+    {
+        const int v = std::atoi(k);
+        tcKernel_ = (v == 1 || v == 2) ? v : 3;
+    }
     if (const char* f = std::getenv("AC_GB300_FUSED")) fused_ = std::atoi(f) != 0;
     int n = 0;
     cudaError_t err = cudaGetDeviceCount(&n);
@@ -313,6 +317,7 @@ GB300Processor::~GB300Processor()
         ts.lb.release();
         ts.out.release();
         for (auto& m : ts.maps) m.release();
+        ts.counter.release();
         for (auto& t : ts.tables) t.second.dev.release();
         for (auto& e : ts.events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
         for (auto& e : ts.pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -447,15 +452,27 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
         else
         {
             const bool bf16 = precision_ == Precision::BF16;
-            // The pair-interleaved form stages 1-channel input by TMA (16-byte
-            // aligned plane) and runs the fused RGB(A) path; other 1-channel
-            // planes take the one-pixel-per-row form.
-            const bool v2 = (tcKernel_ != 1 || in.channels > 1) && acnet_tc2_supported(in);
-            const void* w = tcWeights(precision_, v2);
-            if (!w) err = cudaErrorMemoryAllocation;
-            else if (v2) err = launch_acnet_legacy_tc2(*acnet_, w, bf16, in, out, ph, stream);
-            else if (in.channels == 1) err = launch_acnet_legacy_tc(*acnet_, w, bf16, in, out, stream);
-            else err = cudaErrorInvalidValue;
+            if (tcKernel_ == 3)
+            {
+                // persistent warp-specialised form (default)
+                const void* w = tcWeights(precision_, true);
+                if (!w) err = cudaErrorMemoryAllocation;
+                else if ((err = ts.counter.ensure(256)) == cudaSuccess)
+                    err = launch_acnet_legacy_tc3(*acnet_, w, bf16, 1, &in, &out, ph, static_cast<int*>(ts.counter.ptr),
+                                                  smCount_, stream);
+            }
+            else
+            {
+                // The pair-interleaved form stages 1-channel input by TMA
+                // (16-byte aligned plane) and runs the fused RGB(A) path; other
+                // 1-channel planes take the one-pixel-per-row form.
+                const bool v2 = (tcKernel_ != 1 || in.channels > 1) && acnet_tc2_supported(in);
+                const void* w = tcWeights(precision_, v2);
+                if (!w) err = cudaErrorMemoryAllocation;
+                else if (v2) err = launch_acnet_legacy_tc2(*acnet_, w, bf16, in, out, ph, stream);
+                else if (in.channels == 1) err = launch_acnet_legacy_tc(*acnet_, w, bf16, in, out, stream);
+                else err = cudaErrorInvalidValue;
+            }
         }
     }
     if (profiling_)

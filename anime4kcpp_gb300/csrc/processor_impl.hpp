@@ -70,6 +70,7 @@ private:
         cudaStream_t stream = nullptr;
         DeviceBuffer src, y, uv, la, lb, out;
         DeviceBuffer maps[4];  // ARNet feature maps
+        DeviceBuffer counter;  // tile-queue counter of the persistent kernel
         std::map<std::tuple<int, int, int>, AxisTable> tables;
         bool ok = true;
         std::string err = "NO ERROR";
@@ -98,7 +99,7 @@ private:
     std::unique_ptr<AcnetLegacyWeights> acnet_;
     DeviceBuffer deviceWeights_[4];  // TC weights: {one-pixel, pair} x {FP16, BF16}
     bool fused_ = true;              // RGB(A) x2 in one fused kernel (AC_GB300_FUSED=0 disables)
-    int tcKernel_ = 2;               // 1 forces the one-pixel-per-row TC kernel (AC_GB300_TC_KERNEL=1)
+    int tcKernel_ = 3;               // tensor-core kernel: 3 persistent (default), 2 pair-interleaved, 1 one-pixel-per-row (AC_GB300_TC_KERNEL)
     std::mutex mutex_;
     std::unordered_map<std::thread::id, std::unique_ptr<ThreadState>> states_;
 };

@@ -178,6 +178,18 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
                  : "memory");
 }
 
+// ---- shared-memory counters with release / acquire semantics ----
+__device__ __forceinline__ void smem_add_release(uint32_t* p, uint32_t v)
+{
+    asm volatile("red.release.cta.shared::cta.add.u32 [%0], %1;" ::"r"(smem_u32(p)), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t smem_load_acquire(const uint32_t* p)
+{
+    uint32_t v;
+    asm volatile("ld.acquire.cta.shared::cta.u32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)) : "memory");
+    return v;
+}
+
 // ---- packing ----
 __device__ __forceinline__ uint32_t pack_relu_f16x2(float lo, float hi)
 {
