@@ -189,6 +189,11 @@ __global__ void __launch_bounds__(THREADS, 1) acnet_tc3_kernel(const __grid_cons
         const uint32_t one = BF16 ? 0x3F80u : 0x3C00u;
         reinterpret_cast<uint4*>(smem + ONES_OFF)[tid] = make_uint4(one | (one << 16), 0, 0, 0);
     }
+    // Both activation buffers start at zero.  Each MMA also reads the
+    // neighbouring pair slot of an edge pixel with a zero weight, and a
+    // left-over non-finite bit pattern there would turn 0 x Inf into NaN;
+    // every value the epilogue writes later is finite.
+    for (int i = tid; i < 2 * ACT_BYTES / 16; i += THREADS) reinterpret_cast<uint4*>(smem)[i] = make_uint4(0, 0, 0, 0);
     __syncthreads();
     if (tid == 0)
     {
@@ -252,9 +257,12 @@ __global__ void __launch_bounds__(THREADS, 1) acnet_tc3_kernel(const __grid_cons
             }
         }
         __syncthreads();
-        for (int i = tid; i < (WW - 2) * (WH - 2); i += THREADS)
+        // With chroma the previous tile's horizontal pass left float data in
+        // act0, so layer 0 then covers the whole window (its border included).
+        constexpr int L0B = C > 1 ? 0 : 1;
+        for (int i = tid; i < (WW - 2 * L0B) * (WH - 2 * L0B); i += THREADS)
         {
-            const int y = 1 + i / (WW - 2), x = 1 + i % (WW - 2);
+            const int y = L0B + i / (WW - 2 * L0B), x = L0B + i % (WW - 2 * L0B);
             const int cy = clampi(y, iy0, iy1), cx = clampi(x, ix0, ix1);
             const int ty[3] = {max(cy - 1, iy0), cy, min(cy + 1, iy1)};
             const int tx[3] = {max(cx - 1, ix0), cx, min(cx + 1, ix1)};

@@ -251,9 +251,10 @@ GB300Processor::GB300Processor(int device, const ModelSpec& spec) : spec_(spec)
     if (const char* k = std::getenv("AC_GB300_TC_KERNEL"))
     {
         const int v = std::atoi(k);
-        tcKernel_ = (v == 1 || v == 2) ? v : 3;
+        tcKernel_ = (v == 1 || v == 3) ? v : 2;
     }
     if (const char* f = std::getenv("AC_GB300_FUSED")) fused_ = std::atoi(f) != 0;
+    if (const char* n = std::getenv("AC_GB300_TC3_CTAS")) tc3Ctas_ = std::atoi(n);
     int n = 0;
     cudaError_t err = cudaGetDeviceCount(&n);
     if (err != cudaSuccess || n == 0)
@@ -459,7 +460,7 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
                 if (!w) err = cudaErrorMemoryAllocation;
                 else if ((err = ts.counter.ensure(256)) == cudaSuccess)
                     err = launch_acnet_legacy_tc3(*acnet_, w, bf16, 1, &in, &out, ph, static_cast<int*>(ts.counter.ptr),
-                                                  smCount_, stream);
+                                                  tc3Ctas_ > 0 ? tc3Ctas_ : smCount_, stream);
             }
             else
             {

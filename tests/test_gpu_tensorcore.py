@@ -145,3 +145,25 @@ def test_fused_colour_path_matches_unfused(form, c, dtype, monkeypatch):
         outs.append(p.process(x, 2.0))
         assert p.ok(), p.error()
     assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("c", [1, 3])
+def test_persistent_kernel_independent_of_cta_count(c, monkeypatch):
+    """The persistent kernel's tile queue: any number of CTAs, each taking a
+    varying number of tiles (3 x 4 tiles here), gives the same bytes."""
+    monkeypatch.setenv("AC_GB300_TC_KERNEL", "3")
+    if c == 1:
+        x = synthetic.luma(131, 150, np.uint8, seed=17)
+    else:
+        x = synthetic.rgb_u8(131, 150, seed=17)
+    outs = []
+    for ctas in ("1", "2", "5", "0"):
+        monkeypatch.setenv("AC_GB300_TC3_CTAS", ctas)
+        p = ac.Processor("cuda", 0, "acnet-legacy-hdn1", precision="fp16")
+        outs.append(p.process(x, 2.0))
+        assert p.ok(), p.error()
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+    ref32 = oracle.process(x, 2.0, "acnet-legacy-hdn1")
+    d = np.abs(outs[0].astype(int) - ref32.astype(int))
+    assert (d <= 1).mean() >= 0.99 and d.max() <= 6
