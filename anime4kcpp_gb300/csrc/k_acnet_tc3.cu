@@ -7,24 +7,30 @@
 // the fused colour prologue/epilogue that of colour.cuh.  What changes is the
 // schedule:
 //
-//  * One CTA per SM loops over tiles taken from a global atomic counter; the
-//    tiles of every image of a batch form one queue (images of different
-//    sizes in one launch).  The packed weights are copied to shared memory
-//    once per CTA (bulk copy) and the 512 tensor-memory columns are allocated
-//    once.
-//  * Accumulators are double-buffered by layer parity in tensor memory
-//    (2 x 16 blocks x 16 columns) and activations by layer parity in shared
-//    memory (two E/O plane pairs), so layer l+1 can start on block b while
-//    layer l is still being drained elsewhere in the window.
-//  * Warp 16 issues the MMAs.  For layer l and pair block b it waits until
-//    the epilogues of layer l-1 have finished blocks b-2 .. b+2 (the rows the
-//    3x3 taps and the edge replicas touch), issues the block's seven MMAs and
-//    commits them to that block's mbarrier.  Warps 0..15 are the epilogue:
-//    four groups of four warps (one warp per tensor-memory lane quarter),
-//    group g drains blocks g, g+4, g+8, g+12 of every layer, each as soon as
-//    its MMAs completed, and publishes completion through per-block counters
-//    (release/acquire).  The tensor core and the CUDA cores thus work on
-//    different blocks at the same time instead of alternating.
+//  * Two CTAs per SM (one activation buffer and 256 tensor-memory columns
+//    each) loop over tiles taken from a global atomic counter; the tiles of
+//    every image of a batch form one queue (images of different sizes in one
+//    launch).  The packed weights are copied to shared memory once per CTA
+//    and the tensor memory is allocated once.  Two CTAs give the SM two MMA
+//    issuing threads and two tiles in flight, so one tile's prologue or
+//    epilogue overlaps the other's MMAs.
+//  * Warps 8 and 9 issue the MMAs (one issuing thread reaches only about
+//    half the tensor core's rate for these small MMAs; two saturate it), a
+//    round of four pair blocks (4 x 128 GEMM rows) at a time, two blocks
+//    each: for layer l and round r both wait on one mbarrier saying the
+//    epilogues of layer l-1 have finished round r+1 (and with it every block
+//    up to 4r+7; the taps and edge replicas of round r reach blocks 4r-1 ..
+//    4r+4), then issue six MMAs per block, block after block (an
+//    accumulator's MMAs back to back issue fastest), with descriptors
+//    precomputed up to one add, and commit each block to its mbarrier.
+//  * Warps 0..7 are the epilogue: two groups of four warps (one warp per
+//    tensor-memory lane quarter); group g drains blocks 4r+g and 4r+g+2 of
+//    every round as soon as their MMAs completed, adds the bias in FP32 and
+//    writes the next layer's activations in place.  In-place is safe because
+//    a block's epilogue also waits until the MMAs of the blocks before and
+//    after it have completed (they read the rows it overwrites; they may come
+//    from the other issuer), and a block's accumulator
+//    is overwritten by the next layer only after the round barrier above.
 //  * Every wait is bounded by %globaltimer; a timeout raises a CTA-wide abort
 //    flag and the status word, all roles fall through their loops without
 //    touching tensor memory, and the CTA frees its tensor memory and exits.
@@ -32,6 +38,8 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "colour.cuh"
@@ -46,28 +54,29 @@ constexpr int TW = 48, TH = 44, HALO = 9;
 constexpr int WW = TW + 2 * HALO, WH = TH + 2 * HALO;  // 66 x 62 window
 constexpr int PPR = WW / 2;                             // pairs per window row
 constexpr int NBLK = 16;                                // 16 x 128 pairs >= 2046
+constexpr int NROUND = NBLK / 4;
 constexpr int PADP = 40;
 constexpr int PLANE_BYTES = (PADP + NBLK * 128 + PADP) * 16;
-constexpr int ACT_BYTES = 2 * PLANE_BYTES;  // one activation buffer: E plane + O plane
+constexpr int ACT_BYTES = 2 * PLANE_BYTES;  // the activation buffer: E plane + O plane
 constexpr int BL_BYTES = 14 * 256;
 constexpr int NL = 8;
 constexpr int B_BYTES = NL * BL_BYTES;
-constexpr int NEPI = 16;                 // epilogue warps
-constexpr int THREADS = (NEPI + 1) * 32;  // + the MMA warp
-constexpr uint32_t TMEM_COLS = 512;
+constexpr int NEPI = 8;                   // epilogue warps: two groups of four
+constexpr int NISS = 2;                   // MMA issuing warps
+constexpr int THREADS = (NEPI + NISS) * 32;
+constexpr uint32_t TMEM_COLS = 256;
 constexpr int UVW = TW + 4, UVH = TH + 4;
 constexpr int UVX0 = HALO - 2;
 constexpr uint64_t kWaitNs = 2000000000ull;
 constexpr int kMaxImages = 64;
 static_assert(WW * WH / 2 <= NBLK * 128, "window must fit the pair blocks");
-static_assert(UVH * 2 * TW * 3 * 4 <= ACT_BYTES, "chroma sums must fit one activation buffer");
+static_assert(UVH * 2 * TW * 3 * 4 <= ACT_BYTES, "chroma sums must fit the activation buffer");
+static_assert(NBLK * 16 <= static_cast<int>(TMEM_COLS), "one 16-column accumulator per block");
+static_assert(PADP >= PPR + 1, "row above block 0 must stay inside the plane");
 
-constexpr int ACT0_OFF = 0;
-constexpr int ACT1_OFF = ACT_BYTES;
-constexpr int B_OFF = 2 * ACT_BYTES;
-constexpr int ONES_OFF = B_OFF + B_BYTES;
-constexpr int ONES_BYTES = 129 * 16 + 112;
-constexpr int RAW_OFF = ONES_OFF + ONES_BYTES;
+constexpr int ACT_OFF = 0;
+constexpr int B_OFF = ACT_BYTES;
+constexpr int RAW_OFF = B_OFF + B_BYTES;
 
 template <typename T, int C>
 struct Layout
@@ -94,6 +103,7 @@ struct Params
     float k0[72];
     float b0[8];
     float k2[32];
+    float bias[NL][8];  // layers 1..8, added in the epilogue
     Phase2 ph;
     int nimg;
     int ntiles;
@@ -151,49 +161,59 @@ __device__ __forceinline__ bool wait_count(const uint32_t* cnt, uint32_t target,
     return true;
 }
 
+// Pair blocks whose rows hold the valid pixels of layer l (1..8).
+struct LayerRange
+{
+    int ry0, ry1, rx0, rx1, b0, b1;
+    __device__ LayerRange(int l, int ix0, int ix1, int iy0, int iy1)
+    {
+        ry0 = max(l + 1, iy0);
+        ry1 = min(WH - 2 - l, iy1);
+        rx0 = max(l + 1, ix0);
+        rx1 = min(WW - 2 - l, ix1);
+        b0 = ((ry0 * WW + rx0) >> 1) >> 7;
+        b1 = ((ry1 * WW + rx1) >> 1) >> 7;
+    }
+};
+
 template <typename T, int C, bool BF16>
-__global__ void __launch_bounds__(THREADS, 1) acnet_tc3_kernel(const __grid_constant__ Params P)
+__global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_constant__ Params P)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     using L = Layout<T, C>;
     T* raw = reinterpret_cast<T*>(smem + RAW_OFF);
     T* uvs = reinterpret_cast<T*>(smem + L::uv_off);
     float* lut = reinterpret_cast<float*>(smem + L::lut_off);
-    uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + L::misc_off);     // [NBLK]
-    uint32_t* epi_cnt = reinterpret_cast<uint32_t*>(smem + L::misc_off + 128);  // [NBLK]
+    uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + L::misc_off);         // [NBLK]
+    uint64_t* round_bar = reinterpret_cast<uint64_t*>(smem + L::misc_off + 128);  // [NROUND]
     uint64_t* wbar = reinterpret_cast<uint64_t*>(smem + L::misc_off + 192);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L::misc_off + 200);
     volatile int* tile_slot = reinterpret_cast<volatile int*>(smem + L::misc_off + 204);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + L::misc_off + 208);
     uint32_t* gbar = reinterpret_cast<uint32_t*>(smem + L::misc_off + 212);
-    unsigned char* act0 = smem + ACT0_OFF;
-    unsigned char* act1 = smem + ACT1_OFF;
+    unsigned char* act = smem + ACT_OFF;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const bool mma_warp = warp == NEPI;
+    const bool mma_warp = warp >= NEPI;
 
     // ---- one-time set-up ----
     if (tid == 0)
     {
         for (int b = 0; b < NBLK; b++) tc::mbar_init(&mma_bar[b], 1);
+        // four blocks x four lane-quarter warps arrive per round and layer
+        for (int r = 0; r < NROUND; r++) tc::mbar_init(&round_bar[r], 16);
         tc::mbar_init(wbar, 1);
         tc::fence_mbar_init();
-        for (int b = 0; b < NBLK; b++) epi_cnt[b] = 0;
         *abort_flag = 0;
         *gbar = 0;
     }
     if constexpr (sizeof(T) == 1)
         if (tid < 256) lut[tid] = __fdiv_rn(static_cast<float>(tid), 255.0f);
-    if (tid < 129)
-    {
-        const uint32_t one = BF16 ? 0x3F80u : 0x3C00u;
-        reinterpret_cast<uint4*>(smem + ONES_OFF)[tid] = make_uint4(one | (one << 16), 0, 0, 0);
-    }
-    // Both activation buffers start at zero.  Each MMA also reads the
+    // The activation buffer starts at zero.  Each MMA also reads the
     // neighbouring pair slot of an edge pixel with a zero weight, and a
     // left-over non-finite bit pattern there would turn 0 x Inf into NaN;
     // every value the epilogue writes later is finite.
-    for (int i = tid; i < 2 * ACT_BYTES / 16; i += THREADS) reinterpret_cast<uint4*>(smem)[i] = make_uint4(0, 0, 0, 0);
+    for (int i = tid; i < ACT_BYTES / 16; i += THREADS) reinterpret_cast<uint4*>(act)[i] = make_uint4(0, 0, 0, 0);
     __syncthreads();
     if (tid == 0)
     {
@@ -211,9 +231,6 @@ __global__ void __launch_bounds__(THREADS, 1) acnet_tc3_kernel(const __grid_cons
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_slot;
     if (!wok && tid == 0) *abort_flag = 1;
-    const uint32_t act0_a = tc::smem_u32(act0), act1_a = tc::smem_u32(act1);
-    const uint32_t ones_a = tc::smem_u32(smem + ONES_OFF);
-    const uint32_t b_a = tc::smem_u32(smem + B_OFF);
     constexpr uint32_t IDESC = tc::idesc_f16(128, 16, BF16);
 
     uint32_t layers_done = 0;  // layers completed by this CTA over all its tiles
@@ -234,31 +251,49 @@ __global__ void __launch_bounds__(THREADS, 1) acnet_tc3_kernel(const __grid_cons
         const int iy0 = max(0, -gy0), iy1 = min(WH - 1, H - 1 - gy0);
 
         // ---- prologue (all warps): window luma (+ chroma region), layer 0 ----
-        for (int i = tid; i < WW * WH; i += THREADS)
+        // Loads are issued in batches of four pixels per thread before any
+        // of them is converted, so their latencies overlap.
+        constexpr int PER = (WW * WH + THREADS - 1) / THREADS;
+        for (int k0 = 0; k0 < PER; k0 += 4)
         {
-            const int wy = i / WW, wx = i - wy * WW;
-            const int gx = clampi(gx0 + wx, 0, W - 1), gy = clampi(gy0 + wy, 0, H - 1);
-            const T* src = row_ptr<T>(I.in.ptr, I.in.pitch, gy) + gx * C;
-            if constexpr (C == 1) raw[i] = src[0];
-            else
+            T px[4][C];
+#pragma unroll
+            for (int k = 0; k < 4; k++)
             {
-                T px[C];
-#pragma unroll
-                for (int c = 0; c < C; c++) px[c] = src[c];
-                T yq, uvq[C - 1];
-                rgb_to_yuv_q_lut<T, C>(px, yq, uvq, lut);
-                raw[i] = yq;
-                const int ux = wx - UVX0, uy = wy - UVX0;
-                if (ux >= 0 && ux < UVW && uy >= 0 && uy < UVH)
+                const int i = tid + (k0 + k) * THREADS;
+                if (i < WW * WH)
                 {
+                    const int wy = i / WW, wx = i - wy * WW;
+                    const int gx = clampi(gx0 + wx, 0, W - 1), gy = clampi(gy0 + wy, 0, H - 1);
+                    const T* src = row_ptr<T>(I.in.ptr, I.in.pitch, gy) + gx * C;
 #pragma unroll
-                    for (int c = 0; c < C - 1; c++) uvs[(uy * UVW + ux) * (C - 1) + c] = uvq[c];
+                    for (int c = 0; c < C; c++) px[k][c] = src[c];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+            {
+                const int i = tid + (k0 + k) * THREADS;
+                if (i >= WW * WH) continue;
+                if constexpr (C == 1) raw[i] = px[k][0];
+                else
+                {
+                    const int wy = i / WW, wx = i - wy * WW;
+                    T yq, uvq[C - 1];
+                    rgb_to_yuv_q_lut<T, C>(px[k], yq, uvq, lut);
+                    raw[i] = yq;
+                    const int ux = wx - UVX0, uy = wy - UVX0;
+                    if (ux >= 0 && ux < UVW && uy >= 0 && uy < UVH)
+                    {
+#pragma unroll
+                        for (int c = 0; c < C - 1; c++) uvs[(uy * UVW + ux) * (C - 1) + c] = uvq[c];
+                    }
                 }
             }
         }
         __syncthreads();
         // With chroma the previous tile's horizontal pass left float data in
-        // act0, so layer 0 then covers the whole window (its border included).
+        // the buffer, so layer 0 then covers the whole window (border too).
         constexpr int L0B = C > 1 ? 0 : 1;
         for (int i = tid; i < (WW - 2 * L0B) * (WH - 2 * L0B); i += THREADS)
         {
@@ -278,7 +313,7 @@ __global__ void __launch_bounds__(THREADS, 1) acnet_tc3_kernel(const __grid_cons
                 for (int t = 1; t < 9; t++) s = fmaf(r[t], P.k0[n * 9 + t], s);
                 a[n] = s + P.b0[n];
             }
-            *slot(act0, y * WW + x) = pack8<BF16>(a);
+            *slot(act, y * WW + x) = pack8<BF16>(a);
         }
         tc::fence_proxy_async_smem();
         tc::fence_before_sync();
@@ -289,38 +324,39 @@ __global__ void __launch_bounds__(THREADS, 1) acnet_tc3_kernel(const __grid_cons
         {
             if (lane == 0)
             {
+                // descriptors: A for (block b, tap row dy, half h) = a_desc0 +
+                // 128 b + PPR dy + h; B for (layer l, dy, h) = b_desc0 +
+                // (BL_BYTES (l-1) + 512 (2 dy + h)) / 16
+                const uint64_t a_desc0 = tc::smem_desc(tc::smem_u32(act) + (PADP - PPR) * 16, PLANE_BYTES - 16, 128);
+                const uint64_t b_desc0 = tc::smem_desc(tc::smem_u32(smem + B_OFF), 256, 128);
                 for (int l = 1; l <= NL; l++)
                 {
-                    const int ry0 = max(l + 1, iy0), ry1 = min(WH - 2 - l, iy1);
-                    const int rx0 = max(l + 1, ix0), rx1 = min(WW - 2 - l, ix1);
-                    const int b0 = ((ry0 * WW + rx0) >> 1) >> 7, b1 = ((ry1 * WW + rx1) >> 1) >> 7;
-                    const uint32_t in_a = ((l - 1) & 1) ? act1_a : act0_a;
-                    const uint32_t bl = b_a + static_cast<uint32_t>((l - 1) * BL_BYTES);
-                    const uint32_t dbase = tmem + static_cast<uint32_t>((l & 1) * 256);
-                    // epilogue counters after layer l-1 of this tile
-                    const uint32_t target = 4u * (layers_done + static_cast<uint32_t>(l - 1));
-                    for (int b = 0; b < NBLK; b++)
+                    const LayerRange R(l, ix0, ix1, iy0, iy1);
+                    const uint64_t b_desc = b_desc0 + static_cast<uint64_t>(((l - 1) * BL_BYTES) >> 4);
+                    // round barriers: phase of layer l-1 of this tile
+                    const uint32_t rpar = (layers_done + static_cast<uint32_t>(l) - 2u) & 1u;
+                    for (int r = 0; r < NROUND; r++)
                     {
                         bool ok = true;
-                        if (l >= 2)
-                            for (int bb = max(0, b - 2); bb <= min(NBLK - 1, b + 2); bb++)
-                                ok = ok && wait_count(&epi_cnt[bb], target, abort_flag);
+                        if (l >= 2) ok = wait_bar(&round_bar[min(r + 1, NROUND - 1)], rpar, abort_flag);
                         tc::fence_after_sync();
-                        if (ok && b >= b0 && b <= b1)
-                        {
-                            const uint32_t d = dbase + static_cast<uint32_t>(b * 16);
-#pragma unroll
-                            for (int dy = 0; dy < 3; dy++)
+                        const int mine = 4 * r + 2 * (warp - NEPI);  // this issuer's two blocks
+                        const int lo = max(mine, R.b0), hi = min(mine + 1, R.b1);
+                        if (ok)
+                            for (int b = lo; b <= hi; b++)
                             {
-                                const uint32_t a0 = in_a + static_cast<uint32_t>((PADP + b * 128 + (dy - 1) * PPR) * 16);
-                                tc::mma_f16(d, tc::smem_desc(a0, PLANE_BYTES - 16, 128),
-                                            tc::smem_desc(bl + (2 * dy) * 512, 256, 128), IDESC, dy > 0 ? 1u : 0u);
-                                tc::mma_f16(d, tc::smem_desc(a0 + 16, PLANE_BYTES - 16, 128),
-                                            tc::smem_desc(bl + (2 * dy + 1) * 512, 256, 128), IDESC, 1u);
+                                const uint64_t a_desc = a_desc0 + static_cast<uint64_t>(b * 128);
+                                const uint32_t d = tmem + static_cast<uint32_t>(b * 16);
+#pragma unroll
+                                for (int dy = 0; dy < 3; dy++)
+#pragma unroll
+                                    for (int h = 0; h < 2; h++)
+                                        tc::mma_f16(d, a_desc + static_cast<uint64_t>(dy * PPR + h),
+                                                    b_desc + static_cast<uint64_t>((2 * dy + h) * 32), IDESC,
+                                                    (dy | h) ? 1u : 0u);
                             }
-                            tc::mma_f16(d, tc::smem_desc(ones_a, 16, 128), tc::smem_desc(bl + 6 * 512, 256, 128), IDESC, 1u);
-                        }
-                        tc::mma_commit(&mma_bar[b]);
+                        tc::mma_commit(&mma_bar[mine]);
+                        tc::mma_commit(&mma_bar[mine + 1]);
                     }
                 }
             }
@@ -332,25 +368,24 @@ __global__ void __launch_bounds__(THREADS, 1) acnet_tc3_kernel(const __grid_cons
             for (int l = 1; l <= NL; l++)
             {
                 const uint32_t parity = (layers_done + static_cast<uint32_t>(l) - 1u) & 1u;
-                const int ry0 = max(l + 1, iy0), ry1 = min(WH - 2 - l, iy1);
-                const int rx0 = max(l + 1, ix0), rx1 = min(WW - 2 - l, ix1);
-                const int b0 = ((ry0 * WW + rx0) >> 1) >> 7, b1 = ((ry1 * WW + rx1) >> 1) >> 7;
-                unsigned char* out_act = (l & 1) ? act1 : act0;
-                float* Hs = reinterpret_cast<float*>(act0);  // last layer: act0 held layer 6, free once layer 8 runs
+                const LayerRange R(l, ix0, ix1, iy0, iy1);
+                float* Hs = reinterpret_cast<float*>(act);  // last layer: the activations are dead once its MMAs completed
                 if constexpr (C > 1)
                 {
                     if (l == NL)
                     {
-                        // the horizontal chroma pass once MMA(8, block 0) completed (so all
-                        // layer-7 MMAs, the last readers of act0, completed too)
-                        const bool ok = __all_sync(0xffffffffu, wait_bar(&mma_bar[0], parity, abort_flag) ? 1 : 0);
+                        // the horizontal chroma pass once every layer-8 MMA completed
+                        // (the last commit of each issuer)
+                        bool last = true;
+                        for (int i = 0; i < NISS; i++) last = wait_bar(&mma_bar[NBLK - 3 + 2 * i], parity, abort_flag) && last;
+                        const bool ok = __all_sync(0xffffffffu, last ? 1 : 0);
                         if (ok)
                             for (int e = tid; e < UVH * 2 * TW; e += NEPI * 32)
                             {
                                 const int r = e / (2 * TW), ox = e - r * (2 * TW);
                                 chroma_hpass<T, C - 1>(uvs + r * UVW * (C - 1), ox >> 1, ox & 1, P.ph, Hs + e * (C - 1));
                             }
-                        // bounded barrier of the sixteen epilogue warps
+                        // bounded barrier of the epilogue warps
                         __syncwarp();
                         gbar_gen++;
                         if (lane == 0) tc::smem_add_release(gbar, 1);
@@ -358,80 +393,91 @@ __global__ void __launch_bounds__(THREADS, 1) acnet_tc3_kernel(const __grid_cons
                         __syncwarp();
                     }
                 }
-                for (int b = g; b < NBLK; b += 4)
-                {
-                    const bool done = __all_sync(0xffffffffu, wait_bar(&mma_bar[b], parity, abort_flag) ? 1 : 0);
-                    tc::fence_after_sync();
-                    if (done && b >= b0 && b <= b1)
+                const float* bias = P.bias[l - 1];
+                for (int rr = 0; rr < NROUND; rr++)
+#pragma unroll
+                    for (int k2 = 0; k2 < 2; k2++)
                     {
-                        float v[16];
-                        tc::tmem_ld16(tmem + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>((l & 1) * 256 + b * 16), v);
-                        tc::tmem_wait_ld();
-                        const int r = b * 128 + q * 32 + lane;
-#pragma unroll
-                        for (int k = 0; k < 2; k++)
+                        const int b = 4 * rr + g + 2 * k2;
+                        // in-place update: blocks b-1 and b+1 read rows that b overwrites
+                        bool got = wait_bar(&mma_bar[b], parity, abort_flag);
+                        if (b > 0) got = wait_bar(&mma_bar[b - 1], parity, abort_flag) && got;
+                        if (b + 1 < NBLK) got = wait_bar(&mma_bar[b + 1], parity, abort_flag) && got;
+                        const bool done = __all_sync(0xffffffffu, got ? 1 : 0);
+                        tc::fence_after_sync();
+                        if (done && b >= R.b0 && b <= R.b1)
                         {
-                            const int p = 2 * r + k;
-                            const int y = p / WW, x = p - y * WW;
-                            if (y < ry0 || y > ry1 || x < rx0 || x > rx1) continue;
-                            if (l < NL)
+                            float v[16];
+                            tc::tmem_ld16(tmem + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(b * 16), v);
+                            tc::tmem_wait_ld();
+#pragma unroll
+                            for (int c = 0; c < 16; c++) v[c] += bias[c & 7];
+                            const int r = b * 128 + q * 32 + lane;
+#pragma unroll
+                            for (int k = 0; k < 2; k++)
                             {
-                                const uint4 val = pack8<BF16>(v + 8 * k);
-                                *slot(out_act, p) = val;
-                                const bool xl = x == ix0 && x > 0, xr = x == ix1 && x < WW - 1;
-                                const bool yt = y == iy0 && y > 0, yb = y == iy1 && y < WH - 1;
-                                if (xl) *slot(out_act, p - 1) = val;
-                                if (xr) *slot(out_act, p + 1) = val;
-                                if (yt)
+                                const int p = 2 * r + k;
+                                const int y = p / WW, x = p - y * WW;
+                                if (y < R.ry0 || y > R.ry1 || x < R.rx0 || x > R.rx1) continue;
+                                if (l < NL)
                                 {
-                                    *slot(out_act, p - WW) = val;
-                                    if (xl) *slot(out_act, p - WW - 1) = val;
-                                    if (xr) *slot(out_act, p - WW + 1) = val;
-                                }
-                                if (yb)
-                                {
-                                    *slot(out_act, p + WW) = val;
-                                    if (xl) *slot(out_act, p + WW - 1) = val;
-                                    if (xr) *slot(out_act, p + WW + 1) = val;
-                                }
-                            }
-                            else
-                            {
-                                float s[8];
-#pragma unroll
-                                for (int c = 0; c < 8; c++) s[c] = fmaxf(v[8 * k + c], 0.0f);
-                                T o[2][2];
-#pragma unroll
-                                for (int dy = 0; dy < 2; dy++)
-#pragma unroll
-                                    for (int dx = 0; dx < 2; dx++)
+                                    const uint4 val = pack8<BF16>(v + 8 * k);
+                                    *slot(act, p) = val;
+                                    // clamp-to-edge for the next layer
+                                    const bool xl = x == ix0 && x > 0, xr = x == ix1 && x < WW - 1;
+                                    const bool yt = y == iy0 && y > 0, yb = y == iy1 && y < WH - 1;
+                                    if (xl) *slot(act, p - 1) = val;
+                                    if (xr) *slot(act, p + 1) = val;
+                                    if (yt)
                                     {
-                                        const int ko = 8 * (dy * 2 + dx);
-                                        float d = s[0] * P.k2[ko];
-#pragma unroll
-                                        for (int c = 1; c < 8; c++) d = fmaf(s[c], P.k2[ko + c], d);
-                                        o[dy][dx] = from_float<T>(d);
+                                        *slot(act, p - WW) = val;
+                                        if (xl) *slot(act, p - WW - 1) = val;
+                                        if (xr) *slot(act, p - WW + 1) = val;
                                     }
-                                const int ox = 2 * (gx0 + x), oy = 2 * (gy0 + y);
-                                T* row0 = row_ptr_w<T>(I.out.ptr, I.out.pitch, oy) + ox * C;
-                                T* row1 = row_ptr_w<T>(I.out.ptr, I.out.pitch, oy + 1) + ox * C;
-                                if constexpr (C == 1)
-                                {
-                                    row0[0] = o[0][0];
-                                    row0[1] = o[0][1];
-                                    row1[0] = o[1][0];
-                                    row1[1] = o[1][1];
+                                    if (yb)
+                                    {
+                                        *slot(act, p + WW) = val;
+                                        if (xl) *slot(act, p + WW - 1) = val;
+                                        if (xr) *slot(act, p + WW + 1) = val;
+                                    }
                                 }
-                                else merge_block2_h<T, C>(Hs, 2 * TW, x - HALO, y - HALO, P.ph, o, row0, row1, lut);
+                                else
+                                {
+                                    float s[8];
+#pragma unroll
+                                    for (int c = 0; c < 8; c++) s[c] = fmaxf(v[8 * k + c], 0.0f);
+                                    T o[2][2];
+#pragma unroll
+                                    for (int dy = 0; dy < 2; dy++)
+#pragma unroll
+                                        for (int dx = 0; dx < 2; dx++)
+                                        {
+                                            const int ko = 8 * (dy * 2 + dx);
+                                            float d = s[0] * P.k2[ko];
+#pragma unroll
+                                            for (int c = 1; c < 8; c++) d = fmaf(s[c], P.k2[ko + c], d);
+                                            o[dy][dx] = from_float<T>(d);
+                                        }
+                                    const int ox = 2 * (gx0 + x), oy = 2 * (gy0 + y);
+                                    T* row0 = row_ptr_w<T>(I.out.ptr, I.out.pitch, oy) + ox * C;
+                                    T* row1 = row_ptr_w<T>(I.out.ptr, I.out.pitch, oy + 1) + ox * C;
+                                    if constexpr (C == 1)
+                                    {
+                                        row0[0] = o[0][0];
+                                        row0[1] = o[0][1];
+                                        row1[0] = o[1][0];
+                                        row1[1] = o[1][1];
+                                    }
+                                    else merge_block2_h<T, C>(Hs, 2 * TW, x - HALO, y - HALO, P.ph, o, row0, row1, lut);
+                                }
                             }
                         }
+                        // publish: activations visible to the tensor core, tensor-memory reads done
+                        tc::fence_proxy_async_smem();
+                        tc::fence_before_sync();
+                        __syncwarp();
+                        if (lane == 0) tc::mbar_arrive(&round_bar[rr]);
                     }
-                    // publish: activations visible to the tensor core, tensor-memory reads done
-                    tc::fence_proxy_async_smem();
-                    tc::fence_before_sync();
-                    __syncwarp();
-                    if (lane == 0) tc::smem_add_release(&epi_cnt[b], 1);
-                }
             }
         }
         layers_done += NL;
@@ -448,15 +494,35 @@ __global__ void __launch_bounds__(THREADS, 1) acnet_tc3_kernel(const __grid_cons
 template <typename T, int C, bool BF16>
 cudaError_t launch_typed(const Params& p, int grid, cudaStream_t stream)
 {
-    static bool configured = false;
-    if (!configured)
+    static int per_sm = 0;
+    if (per_sm == 0)
     {
         cudaError_t err = cudaFuncSetAttribute(acnet_tc3_kernel<T, C, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                Layout<T, C>::smem);
         if (err != cudaSuccess) return err;
-        configured = true;
+        err = cudaFuncSetAttribute(acnet_tc3_kernel<T, C, BF16>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                   cudaSharedmemCarveoutMaxShared);
+        if (err != cudaSuccess) return err;
+        // CTAs per SM from shared memory, registers and threads.  (The
+        // occupancy calculator reports one CTA per SM for any kernel that
+        // allocates tensor memory; two CTAs of 256 columns each do run
+        // side by side.)
+        cudaFuncAttributes fa;
+        err = cudaFuncGetAttributes(&fa, acnet_tc3_kernel<T, C, BF16>);
+        if (err != cudaSuccess) return err;
+        int dev = 0, smem_sm = 0, reserved = 0, regs_sm = 0;
+        if ((err = cudaGetDevice(&dev)) != cudaSuccess) return err;
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+        cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+        const int regs_cta = (fa.numRegs + 7) / 8 * 8 * THREADS;
+        const int need_smem = Layout<T, C>::smem + static_cast<int>(fa.sharedSizeBytes) + reserved;
+        per_sm = (2 * need_smem <= smem_sm && 2 * regs_cta <= regs_sm && 2 * TMEM_COLS <= 512) ? 2 : 1;
+        if (std::getenv("AC_GB300_DEBUG"))
+            std::fprintf(stderr, "tc3 <%d,%d,%d>: %d CTAs per SM, %d bytes shared, %d registers\n", static_cast<int>(sizeof(T)),
+                         C, BF16 ? 1 : 0, per_sm, Layout<T, C>::smem, fa.numRegs);
     }
-    acnet_tc3_kernel<T, C, BF16><<<grid, THREADS, Layout<T, C>::smem, stream>>>(p);
+    acnet_tc3_kernel<T, C, BF16><<<grid * per_sm, THREADS, Layout<T, C>::smem, stream>>>(p);
     return cudaGetLastError();
 }
 
@@ -480,14 +546,14 @@ int acnet_tc3_max_images() { return tcv3::kMaxImages; }
 
 // One persistent launch over all tiles of n images (same element type and
 // channel count; each output exactly 2x its input).  `counter` is a device
-// int the call zeroes on `stream` before the launch; `ctas` CTAs (one per SM
-// at most is resident) drain the queue.
+// int the call zeroes on `stream` before the launch; `ctas` SMs' worth of
+// CTAs (one or two per SM, as many as fit) drain the queue.
 cudaError_t launch_acnet_legacy_tc3(const AcnetLegacyWeights& wts, const void* packed2, bool bf16, int n, const Plane* in,
                                     const Plane* out, const Phase2* phase2, int* counter, int ctas, cudaStream_t stream)
 {
     using namespace tcv3;
     if (n <= 0) return cudaSuccess;
-    if (n > kMaxImages || !packed2 || !counter) return cudaErrorInvalidValue;
+    if (n > kMaxImages || !packed2 || !counter || ctas <= 0) return cudaErrorInvalidValue;
     const int c = in[0].channels, type = in[0].type;
     if (c > 1 && !phase2) return cudaErrorInvalidValue;
     Params p;
@@ -496,6 +562,8 @@ cudaError_t launch_acnet_legacy_tc3(const AcnetLegacyWeights& wts, const void* p
     for (int i = 0; i < 72; i++) p.k0[i] = wts.k[i];
     for (int i = 0; i < 8; i++) p.b0[i] = wts.b[i];
     for (int i = 0; i < 32; i++) p.k2[i] = wts.k[72 + 576 * 8 + i];
+    for (int l = 0; l < NL; l++)
+        for (int k = 0; k < 8; k++) p.bias[l][k] = wts.b[8 * (l + 1) + k];
     if (phase2) p.ph = *phase2;
     int tiles = 0;
     for (int i = 0; i < n; i++)

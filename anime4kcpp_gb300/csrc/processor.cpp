@@ -251,7 +251,7 @@ GB300Processor::GB300Processor(int device, const ModelSpec& spec) : spec_(spec)
     if (const char* k = std::getenv("AC_GB300_TC_KERNEL"))
     {
         const int v = std::atoi(k);
-        tcKernel_ = (v == 1 || v == 3) ? v : 2;
+        tcKernel_ = (v == 1 || v == 2) ? v : 3;
     }
     if (const char* f = std::getenv("AC_GB300_FUSED")) fused_ = std::atoi(f) != 0;
     if (const char* n = std::getenv("AC_GB300_TC3_CTAS")) tc3Ctas_ = std::atoi(n);

@@ -100,7 +100,7 @@ private:
     DeviceBuffer deviceWeights_[4];  // TC weights: {one-pixel, pair} x {FP16, BF16}
     int tc3Ctas_ = 0;                // CTAs of the persistent kernel (0: one per SM; AC_GB300_TC3_CTAS)
     bool fused_ = true;              // RGB(A) x2 in one fused kernel (AC_GB300_FUSED=0 disables)
-    int tcKernel_ = 2;               // tensor-core kernel: 2 pair-interleaved (default), 3 persistent, 1 one-pixel-per-row (AC_GB300_TC_KERNEL)
+    int tcKernel_ = 3;               // tensor-core kernel: 3 persistent (default), 2 pair-interleaved, 1 one-pixel-per-row (AC_GB300_TC_KERNEL)
     std::mutex mutex_;
     std::unordered_map<std::thread::id, std::unique_ptr<ThreadState>> states_;
 };

@@ -144,6 +144,12 @@ __device__ __forceinline__ bool mbar_wait_ns(uint64_t* mbar, uint32_t phase, uin
     return true;
 }
 
+// Plain arrive (release semantics at CTA scope).
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
+
 // ---- TMA / bulk copies ----
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes)
 {
