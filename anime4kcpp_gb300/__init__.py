@@ -58,7 +58,7 @@ EXPORTS = (
     "ac_processor_type_name", "ac_processor_info", "ac_processor_list_info",
     "ac_gb300_set_precision", "ac_gb300_get_precision", "ac_gb300_output_shape", "ac_gb300_process_device",
     "ac_gb300_launch_count", "ac_gb300_model_params", "ac_gb300_profile_enable", "ac_gb300_profile_collect",
-    "ac_gb300_tc_selftest",
+    "ac_gb300_tc_selftest", "ac_gb300_process_device_noalloc",
 )
 
 _lock = threading.Lock()
@@ -93,6 +93,7 @@ def native():
             "ac_gb300_set_precision": (I, [pproc, I]), "ac_gb300_get_precision": (I, [pproc]),
             "ac_gb300_output_shape": (I, [I, I, I, D, P(I), P(I)]),
             "ac_gb300_process_device": (I, [pproc, P(ACGB300DeviceImage), P(ACGB300DeviceImage), D, V, I]),
+            "ac_gb300_process_device_noalloc": (I, [pproc, I, P(ACGB300DeviceImage), P(ACGB300DeviceImage), V, I]),
             "ac_gb300_launch_count": (ctypes.c_uint64, []),
             "ac_gb300_model_params": (I, [ctypes.c_char_p, V, I, V, I, V, I, P(I)]),
             "ac_gb300_profile_enable": (I, [pproc, I]),
@@ -222,6 +223,20 @@ class Processor:
                                               ctypes.c_void_p(stream or 0), 1 if sync else 0)
         if rc != AC_SUCCESS:
             raise RuntimeError(self.error())
+
+    def process_device_noalloc(self, srcs, dsts, stream=None, sync=True):
+        """x2 of several device images in one launch without allocating
+        (``ac_gb300_process_device_noalloc``): FP16/BF16 ACNetLegacy, at most
+        64 images of one channel count and element type, after one ordinary
+        call in the same precision.  Returns the C status code (AC_SUCCESS,
+        or an error code with the message in ``error()``)."""
+        n = len(srcs)
+        if len(dsts) != n:
+            raise ValueError("srcs and dsts differ in length")
+        arr = ACGB300DeviceImage * max(n, 1)
+        s, d = arr(*[_dev(x) for x in srcs]), arr(*[_dev(x) for x in dsts])
+        return native().ac_gb300_process_device_noalloc(ctypes.byref(self._p), n, s, d, ctypes.c_void_p(stream or 0),
+                                                        1 if sync else 0)
 
     def profile(self, enable=True):
         native().ac_gb300_profile_enable(ctypes.byref(self._p), 1 if enable else 0)

@@ -334,6 +334,23 @@ int ac_gb300_process_device(ACProcessor* processor, const ACGB300DeviceImage* sr
     return rc == 0 ? AC_SUCCESS : AC_ERROR(AC_EPROCESSOR);
 }
 
+int ac_gb300_process_device_noalloc(ACProcessor* processor, int count, const ACGB300DeviceImage* src,
+                                    const ACGB300DeviceImage* dst, void* stream, int sync)
+{
+    auto* g = gpu_of(processor);
+    if (!g || !src || !dst) return AC_ERROR(AC_EINVAL);
+    if (count < 1 || count > 64)  // rejected with a message by the processor
+        return g->processDeviceNoAlloc(count, nullptr, nullptr, static_cast<cudaStream_t>(stream), false), AC_ERROR(AC_EINVAL);
+    acgb::DeviceImage s[64], d[64];
+    for (int i = 0; i < count; i++)
+    {
+        s[i] = acgb::DeviceImage{src[i].ptr, src[i].width, src[i].height, src[i].channels, src[i].stride, src[i].element_type};
+        d[i] = acgb::DeviceImage{dst[i].ptr, dst[i].width, dst[i].height, dst[i].channels, dst[i].stride, dst[i].element_type};
+    }
+    const int rc = g->processDeviceNoAlloc(count, s, d, static_cast<cudaStream_t>(stream), sync != 0);
+    return rc == 0 ? AC_SUCCESS : (rc == -2 ? AC_ERROR(AC_EINVAL) : AC_ERROR(AC_EPROCESSOR));
+}
+
 uint64_t ac_gb300_launch_count(void) { return acgb::launch_count(); }
 
 int ac_gb300_profile_enable(ACProcessor* processor, int enable)

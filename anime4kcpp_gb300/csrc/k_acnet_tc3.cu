@@ -41,6 +41,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 
 #include "colour.cuh"
 #include "device_common.cuh"
@@ -544,16 +545,16 @@ int* tc_status_buffer();
 
 int acnet_tc3_max_images() { return tcv3::kMaxImages; }
 
-// One persistent launch over all tiles of n images (same element type and
-// channel count; each output exactly 2x its input).  `counter` is a device
-// int the call zeroes on `stream` before the launch; `ctas` SMs' worth of
-// CTAs (one or two per SM, as many as fit) drain the queue.
-cudaError_t launch_acnet_legacy_tc3(const AcnetLegacyWeights& wts, const void* packed2, bool bf16, int n, const Plane* in,
-                                    const Plane* out, const Phase2* phase2, int* counter, int ctas, cudaStream_t stream)
+namespace {
+
+// One persistent launch over all tiles of n images; `counter` (zeroed here
+// on `stream`) is the tile queue, `status` the word a timed-out wait sets.
+cudaError_t launch_tc3(const AcnetLegacyWeights& wts, const void* packed2, bool bf16, int n, const Plane* in, const Plane* out,
+                       const Phase2* phase2, int* counter, int* status, int ctas, cudaStream_t stream)
 {
     using namespace tcv3;
     if (n <= 0) return cudaSuccess;
-    if (n > kMaxImages || !packed2 || !counter || ctas <= 0) return cudaErrorInvalidValue;
+    if (n > kMaxImages || !packed2 || !counter || !status || ctas <= 0) return cudaErrorInvalidValue;
     const int c = in[0].channels, type = in[0].type;
     if (c > 1 && !phase2) return cudaErrorInvalidValue;
     Params p;
@@ -578,8 +579,7 @@ cudaError_t launch_acnet_legacy_tc3(const AcnetLegacyWeights& wts, const void* p
     p.nimg = n;
     p.ntiles = tiles;
     p.tile_counter = counter;
-    p.status = tc_status_buffer();
-    if (!p.status) return cudaErrorMemoryAllocation;
+    p.status = status;
     cudaError_t err = cudaMemsetAsync(counter, 0, sizeof(int), stream);
     if (err != cudaSuccess) return err;
     const int grid = tiles < ctas ? tiles : ctas;
@@ -592,6 +592,73 @@ cudaError_t launch_acnet_legacy_tc3(const AcnetLegacyWeights& wts, const void* p
     }
     if (err == cudaSuccess) count_launch();
     return err;
+}
+
+// Scratch of the allocation-free entry: word 0 is the tile-queue counter,
+// word 1 the status word; a call zeroes both on its stream before the launch
+// and uses 8 of the 256 bytes whatever the batch.  Calls that overlap in
+// time on one device share it and race.
+constexpr int kNoAllocScratchInts = 64;
+constexpr int kNoAllocMaxDevices = 64;
+static __device__ __align__(256) int g_tc3_noalloc_scratch[kNoAllocScratchInts];
+
+// Device address of the scratch on the current device, resolved once per
+// device (the set-up step of the first call on that device).
+cudaError_t noalloc_scratch(int** out)
+{
+    static std::mutex m;
+    static int* addr[kNoAllocMaxDevices] = {};
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess) return err;
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(m);
+    if (!addr[dev])
+    {
+        void* p = nullptr;
+        err = cudaGetSymbolAddress(&p, g_tc3_noalloc_scratch);
+        if (err != cudaSuccess) return err;
+        addr[dev] = static_cast<int*>(p);
+    }
+    *out = addr[dev];
+    return cudaSuccess;
+}
+
+}  // namespace
+
+// One persistent launch over all tiles of n images (same element type and
+// channel count; each output exactly 2x its input).  `counter` is a device
+// int the call zeroes on `stream` before the launch; `ctas` SMs' worth of
+// CTAs (one or two per SM, as many as fit) drain the queue.
+cudaError_t launch_acnet_legacy_tc3(const AcnetLegacyWeights& wts, const void* packed2, bool bf16, int n, const Plane* in,
+                                    const Plane* out, const Phase2* phase2, int* counter, int ctas, cudaStream_t stream)
+{
+    int* status = tc_status_buffer();
+    if (!status) return cudaErrorMemoryAllocation;
+    return launch_tc3(wts, packed2, bf16, n, in, out, phase2, counter, status, ctas, stream);
+}
+
+// The same launch with its counter and status word in the file's static
+// scratch: allocates no memory (first call per device: symbol look-up).
+cudaError_t launch_acnet_legacy_tc3_noalloc(const AcnetLegacyWeights& wts, const void* packed2, bool bf16, int n,
+                                            const Plane* in, const Plane* out, const Phase2* phase2, int ctas,
+                                            cudaStream_t stream)
+{
+    int* s = nullptr;
+    cudaError_t err = noalloc_scratch(&s);
+    if (err != cudaSuccess) return err;
+    if ((err = cudaMemsetAsync(s, 0, 2 * sizeof(int), stream)) != cudaSuccess) return err;
+    return launch_tc3(wts, packed2, bf16, n, in, out, phase2, s, s + 1, ctas, stream);
+}
+
+// Status word of the allocation-free launches on the current device: 0, or
+// 1 when a bounded wait gave up.  Read it after the stream synchronised.
+cudaError_t acnet_tc3_noalloc_status(int* value)
+{
+    int* s = nullptr;
+    cudaError_t err = noalloc_scratch(&s);
+    if (err != cudaSuccess) return err;
+    return cudaMemcpy(value, s + 1, sizeof(int), cudaMemcpyDeviceToHost);
 }
 
 }  // namespace acgb

@@ -75,10 +75,18 @@ void pack_acnet_tc2_weights(const AcnetLegacyWeights& wts, bool bf16, std::vecto
 // Persistent warp-specialised tensor-core form over a tile queue of n images
 // (same type and channel count, every output 2x its input); packed2 as for
 // the pair-interleaved form.  `counter` is a device int (zeroed by the call
-// on `stream`); `ctas` = CTAs to launch (one per SM).
+// on `stream`); `ctas` = SMs' worth of CTAs to launch.
 int acnet_tc3_max_images();
 cudaError_t launch_acnet_legacy_tc3(const AcnetLegacyWeights& wts, const void* packed2, bool bf16, int n, const Plane* in,
                                     const Plane* out, const Phase2* phase2, int* counter, int ctas, cudaStream_t stream);
+// The same launch with its tile counter and status word in a static device
+// array of that file (256 bytes): no allocation; concurrent calls on one
+// device race.  acnet_tc3_noalloc_status reads its status word (0, or 1
+// after a timed-out wait) once the stream has synchronised.
+cudaError_t launch_acnet_legacy_tc3_noalloc(const AcnetLegacyWeights& wts, const void* packed2, bool bf16, int n,
+                                            const Plane* in, const Plane* out, const Phase2* phase2, int ctas,
+                                            cudaStream_t stream);
+cudaError_t acnet_tc3_noalloc_status(int* value);
 
 // RGB(A) -> Y + UV(A) (rgb2yuv / rgba2yuva of core/src/ImageProcess.cpp).
 cudaError_t launch_rgb2yuv_split(const Plane& rgb, const Plane& y, const Plane& uv, cudaStream_t stream);

@@ -741,4 +741,80 @@ int GB300Processor::processDevice(const DeviceImage& src, const DeviceImage& dst
     return 0;
 }
 
+// The allocation-free batch entry.  Its success path allocates no device or
+// host memory: the tile queue lives in the persistent kernel's static
+// scratch, the weights must already be resident (an ordinary call in the
+// same precision uploaded them), and the per-thread error record is only
+// touched when it exists already or a call fails.
+int GB300Processor::processDeviceNoAlloc(int n, const DeviceImage* src, const DeviceImage* dst, cudaStream_t stream, bool sync)
+{
+    auto failed = [&](const std::string& what, cudaError_t err = cudaSuccess) {
+        fail(state(), what, err);
+        return -1;
+    };
+    auto rejected = [&](const std::string& what) {
+        fail(state(), what);
+        return -2;
+    };
+    if (!initError_.empty()) return failed(initError_);
+    if (spec_.family != Family::ACNetLegacy || precision_ == Precision::FP32)
+        return rejected("allocation-free call: needs an ACNetLegacy model in the FP16 or BF16 form");
+    const int maxImages = std::min(acnet_tc3_max_images(), 64);  // the Plane tables below
+    if (n < 1 || n > maxImages || !src || !dst)
+        return rejected("allocation-free call: " + std::to_string(n) + " images in one call; 1 to " + std::to_string(maxImages) +
+                      " are allowed");
+    const int c = src[0].c, type = src[0].type, es = type & 0xff;
+    if (c != 1 && c != 3 && c != 4) return rejected("unsupported channel count (1, 3 or 4)");
+    if (type != Image::UInt8 && type != Image::UInt16 && type != Image::Float32)
+        return rejected("unsupported element type (u8, u16 or f32)");
+    Plane in[64], out[64];
+    for (int i = 0; i < n; i++)
+    {
+        const DeviceImage& a = src[i];
+        const DeviceImage& b = dst[i];
+        if (!a.ptr || !b.ptr) return rejected("null device pointer");
+        if (a.c != c || a.type != type || b.c != c || b.type != type)
+            return rejected("allocation-free call: every image needs the first image's channel count and element type");
+        if (a.w <= 0 || a.h <= 0 || b.w != 2 * a.w || b.h != 2 * a.h)
+            return rejected("allocation-free call: every dst must be exactly 2x its src");
+        if (a.stride < a.w * c * es || b.stride < b.w * c * es) return rejected("stride smaller than a row");
+        if (static_cast<double>(b.stride) * b.h > 2147483647.0) return rejected("output image too large");
+        in[i] = plane_of(a);
+        out[i] = plane_of(b);
+    }
+    Phase2 ph;
+    if (c > 1 && !phase_weights(2, &ph.w[0][0])) return failed("chroma resample weights");
+    const bool bf16 = precision_ == Precision::BF16;
+    const void* w = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(mutex_);
+        w = deviceWeights_[2 + (bf16 ? 1 : 0)].ptr;
+    }
+    if (!w)
+        return rejected("allocation-free call: the tensor-core weights of this precision are not on the device yet; make one "
+                      "ordinary process call in this precision first");
+    cudaError_t err = cudaSetDevice(device_);
+    if (err != cudaSuccess) return failed("cudaSetDevice", err);
+    err = launch_acnet_legacy_tc3_noalloc(*acnet_, w, bf16, n, in, out, c > 1 ? &ph : nullptr,
+                                          tc3Ctas_ > 0 ? tc3Ctas_ : smCount_, stream);
+    if (err != cudaSuccess) return failed("allocation-free upscale", err);
+    if (sync)
+    {
+        if ((err = cudaStreamSynchronize(stream)) != cudaSuccess) return failed("kernel execution", err);
+        int status = 0;
+        if ((err = acnet_tc3_noalloc_status(&status)) != cudaSuccess) return failed("status read", err);
+        if (status != 0) return failed("tensor-core wait timed out");
+    }
+    {
+        std::lock_guard<std::mutex> lock(mutex_);
+        auto it = states_.find(std::this_thread::get_id());
+        if (it != states_.end() && it->second)
+        {
+            it->second->ok = true;
+            it->second->err = "NO ERROR";
+        }
+    }
+    return 0;
+}
+
 }  // namespace acgb

@@ -43,6 +43,11 @@ public:
     // (details through ok()/error()).
     int processDevice(const DeviceImage& src, const DeviceImage& dst, double factor, cudaStream_t stream, bool sync);
 
+    // Allocation-free x2 of n device images in one persistent tensor-core
+    // launch on `stream` (ACNetLegacy, FP16/BF16 form).  Returns 0, -1 when
+    // the work failed, -2 when the request was rejected.
+    int processDeviceNoAlloc(int n, const DeviceImage* src, const DeviceImage* dst, cudaStream_t stream, bool sync);
+
     // Kernel timing of the luma passes with CUDA events recorded on the
     // launching stream around each launch (for roofline figures).
     void setProfiling(bool on);

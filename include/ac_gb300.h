@@ -49,6 +49,33 @@ AC_C_API int ac_gb300_output_shape(int width, int height, int channels, double f
 AC_C_API int ac_gb300_process_device(ACProcessor* processor, const ACGB300DeviceImage* src, const ACGB300DeviceImage* dst,
                                      double factor, void* stream, int sync);
 
+/* Allocation-free x2 upscale of `count` device images in ONE persistent
+ * tensor-core launch.  No reference counterpart: the reference's processors
+ * allocate their work buffers inside each call.  It is for callers that must
+ * not allocate device memory once running: a real-time video or rendering
+ * pipeline whose device memory is planned up front, or a host application
+ * that forbids allocation (and the synchronisation an allocation can imply)
+ * on its frame thread.  The call allocates no device memory and, when it
+ * succeeds, no host memory.
+ *
+ * Requirements and limits: an ACNetLegacy processor in the FP16 or BF16 form
+ * whose packed weights are already on the device (make one ordinary process
+ * call in that form first); 1 to 64 images per call, all with the first
+ * image's channel count (1, 3 or 4) and element type; every dst exactly 2x
+ * its src.  Anything else is rejected with AC_ERROR(AC_EINVAL) and a message
+ * in ac_processor_error().  Scratch: a 256-byte static device array in the
+ * library, of which a call uses 8 bytes (the tile-queue counter and a status
+ * word, both zeroed on `stream` at the start of every call).
+ *
+ * The first call on a device does set-up (it looks up the scratch address
+ * and configures the kernel): make that first call before any stream
+ * capture.  Calls that overlap in time on one device share the scratch and
+ * race: serialise them (one stream, or events).  `stream` NULL is the legacy
+ * default stream.  With sync != 0 the call waits and reports a timed-out
+ * tensor-core wait as AC_ERROR(AC_EPROCESSOR). */
+AC_C_API int ac_gb300_process_device_noalloc(ACProcessor* processor, int count, const ACGB300DeviceImage* src,
+                                             const ACGB300DeviceImage* dst, void* stream, int sync);
+
 /* Kernel timing of the luma network passes: when enabled, the processor
  * records a CUDA event pair on the launching stream around every luma-pass
  * launch of the calling thread; ac_gb300_profile_collect waits for them and
