@@ -58,7 +58,8 @@ EXPORTS = (
     "ac_processor_type_name", "ac_processor_info", "ac_processor_list_info",
     "ac_gb300_set_precision", "ac_gb300_get_precision", "ac_gb300_output_shape", "ac_gb300_process_device",
     "ac_gb300_launch_count", "ac_gb300_model_params", "ac_gb300_profile_enable", "ac_gb300_profile_collect",
-    "ac_gb300_tc_selftest", "ac_gb300_process_device_noalloc",
+    "ac_gb300_tc_selftest", "ac_gb300_process_device_noalloc", "ac_gb300_process_batch_device",
+    "ac_gb300_graph_replays",
 )
 
 _lock = threading.Lock()
@@ -94,6 +95,8 @@ def native():
             "ac_gb300_output_shape": (I, [I, I, I, D, P(I), P(I)]),
             "ac_gb300_process_device": (I, [pproc, P(ACGB300DeviceImage), P(ACGB300DeviceImage), D, V, I]),
             "ac_gb300_process_device_noalloc": (I, [pproc, I, P(ACGB300DeviceImage), P(ACGB300DeviceImage), V, I]),
+            "ac_gb300_process_batch_device": (I, [pproc, I, P(ACGB300DeviceImage), P(ACGB300DeviceImage), D, V, I]),
+            "ac_gb300_graph_replays": (ctypes.c_uint64, []),
             "ac_gb300_launch_count": (ctypes.c_uint64, []),
             "ac_gb300_model_params": (I, [ctypes.c_char_p, V, I, V, I, V, I, P(I)]),
             "ac_gb300_profile_enable": (I, [pproc, I]),
@@ -224,6 +227,20 @@ class Processor:
         if rc != AC_SUCCESS:
             raise RuntimeError(self.error())
 
+    def process_batch_device(self, srcs, dsts, factor=2.0, stream=None, sync=True):
+        """Upscale many device images in one call (``ac_gb300_process_batch_device``):
+        ACNetLegacy x2 in the FP16/BF16 form runs each group of one channel
+        count and element type as one persistent launch."""
+        n = len(srcs)
+        if len(dsts) != n:
+            raise ValueError("srcs and dsts differ in length")
+        arr = ACGB300DeviceImage * max(n, 1)
+        s, d = arr(*[_dev(x) for x in srcs]), arr(*[_dev(x) for x in dsts])
+        rc = native().ac_gb300_process_batch_device(ctypes.byref(self._p), n, s, d, float(factor),
+                                                    ctypes.c_void_p(stream or 0), 1 if sync else 0)
+        if rc != AC_SUCCESS:
+            raise RuntimeError(self.error())
+
     def process_device_noalloc(self, srcs, dsts, stream=None, sync=True):
         """x2 of several device images in one launch without allocating
         (``ac_gb300_process_device_noalloc``): FP16/BF16 ACNetLegacy, at most
@@ -249,6 +266,11 @@ class Processor:
         return ms.value, n.value, px.value
 
     InfoList = property(lambda self: (native().ac_processor_info(0).decode(), native().ac_processor_info(2).decode()))
+
+
+def graph_replays():
+    """Batched launches replayed from captured CUDA graphs in this process."""
+    return int(native().ac_gb300_graph_replays())
 
 
 def _dev(t):

@@ -4,6 +4,7 @@
 #include <cstring>
 #include <memory>
 #include <new>
+#include <vector>
 
 #include "ac_core.h"
 #include "ac_gb300.h"
@@ -333,6 +334,23 @@ int ac_gb300_process_device(ACProcessor* processor, const ACGB300DeviceImage* sr
     int rc = g->processDevice(s, d, factor, static_cast<cudaStream_t>(stream), sync != 0);
     return rc == 0 ? AC_SUCCESS : AC_ERROR(AC_EPROCESSOR);
 }
+
+int ac_gb300_process_batch_device(ACProcessor* processor, int count, const ACGB300DeviceImage* src,
+                                  const ACGB300DeviceImage* dst, double factor, void* stream, int sync)
+{
+    auto* g = gpu_of(processor);
+    if (!g || count < 0 || (count > 0 && (!src || !dst))) return AC_ERROR(AC_EINVAL);
+    std::vector<acgb::DeviceImage> s(count), d(count);
+    for (int i = 0; i < count; i++)
+    {
+        s[i] = acgb::DeviceImage{src[i].ptr, src[i].width, src[i].height, src[i].channels, src[i].stride, src[i].element_type};
+        d[i] = acgb::DeviceImage{dst[i].ptr, dst[i].width, dst[i].height, dst[i].channels, dst[i].stride, dst[i].element_type};
+    }
+    const int rc = g->processBatchDevice(count, s.data(), d.data(), factor, static_cast<cudaStream_t>(stream), sync != 0);
+    return rc == 0 ? AC_SUCCESS : AC_ERROR(AC_EPROCESSOR);
+}
+
+uint64_t ac_gb300_graph_replays(void) { return acgb::graph_replays(); }
 
 int ac_gb300_process_device_noalloc(ACProcessor* processor, int count, const ACGB300DeviceImage* src,
                                     const ACGB300DeviceImage* dst, void* stream, int sync)

@@ -76,9 +76,14 @@ void pack_acnet_tc2_weights(const AcnetLegacyWeights& wts, bool bf16, std::vecto
 // (same type and channel count, every output 2x its input); packed2 as for
 // the pair-interleaved form.  `counter` is a device int (zeroed by the call
 // on `stream`); `ctas` = SMs' worth of CTAs to launch.
+// `shape` picks the tile geometry (0: 48x44, 1: 64x31, 2: 32x63; the same
+// bytes come out of each) and `per_sm_cap` caps the CTAs per SM (1 or 2).
+constexpr int kTc3Shapes = 3;
 int acnet_tc3_max_images();
+void acnet_tc3_shape(int shape, int* tw, int* th);
 cudaError_t launch_acnet_legacy_tc3(const AcnetLegacyWeights& wts, const void* packed2, bool bf16, int n, const Plane* in,
-                                    const Plane* out, const Phase2* phase2, int* counter, int ctas, cudaStream_t stream);
+                                    const Plane* out, const Phase2* phase2, int* counter, int ctas, cudaStream_t stream,
+                                    int shape = 0, int per_sm_cap = 2);
 // The same launch with its tile counter and status word in a static device
 // array of that file (256 bytes): no allocation; concurrent calls on one
 // device race.  acnet_tc3_noalloc_status reads its status word (0, or 1

@@ -14,6 +14,7 @@
 #include "processor_impl.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cctype>
 #include <cmath>
 #include <cstring>
@@ -255,6 +256,10 @@ GB300Processor::GB300Processor(int device, const ModelSpec& spec) : spec_(spec)
     }
     if (const char* f = std::getenv("AC_GB300_FUSED")) fused_ = std::atoi(f) != 0;
     if (const char* n = std::getenv("AC_GB300_TC3_CTAS")) tc3Ctas_ = std::atoi(n);
+    if (const char* v = std::getenv("AC_GB300_TC3_SHAPE")) tc3Shape_ = std::atoi(v);
+    if (tc3Shape_ >= kTc3Shapes) tc3Shape_ = -1;
+    if (const char* v = std::getenv("AC_GB300_TC3_PER_SM")) tc3PerSm_ = std::atoi(v);
+    if (const char* v = std::getenv("AC_GB300_AUTOTUNE")) autotune_ = std::atoi(v) != 0;
     int n = 0;
     cudaError_t err = cudaGetDeviceCount(&n);
     if (err != cudaSuccess || n == 0)
@@ -322,6 +327,11 @@ GB300Processor::~GB300Processor()
         for (auto& t : ts.tables) t.second.dev.release();
         for (auto& e : ts.events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
         for (auto& e : ts.pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+        for (auto& g : ts.graphs)
+        {
+            if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+            if (g.second.graph) cudaGraphDestroy(g.second.graph);
+        }
         if (ts.stream) cudaStreamDestroy(ts.stream);
     }
     states_.clear();
@@ -459,8 +469,14 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
                 const void* w = tcWeights(precision_, true);
                 if (!w) err = cudaErrorMemoryAllocation;
                 else if ((err = ts.counter.ensure(256)) == cudaSuccess)
-                    err = launch_acnet_legacy_tc3(*acnet_, w, bf16, 1, &in, &out, ph, static_cast<int*>(ts.counter.ptr),
-                                                  tc3Ctas_ > 0 ? tc3Ctas_ : smCount_, stream);
+                {
+                    int* counter = static_cast<int*>(ts.counter.ptr);
+                    bool ran = false;
+                    const Tc3Plan plan = tc3Plan(1, &in, &out, ph, w, bf16, counter, stream, ran, err);
+                    if (err == cudaSuccess && !ran)
+                        err = launch_acnet_legacy_tc3(*acnet_, w, bf16, 1, &in, &out, ph, counter,
+                                                      tc3Ctas_ > 0 ? tc3Ctas_ : smCount_, stream, plan.shape, plan.perSm);
+                }
             }
             else
             {
@@ -527,6 +543,80 @@ const void* GB300Processor::tcWeights(Precision p, bool pairForm)
         }
     }
     return deviceWeights_[idx].ptr;
+}
+
+static std::atomic<uint64_t> g_graph_replays{0};
+uint64_t graph_replays() { return g_graph_replays.load(); }
+
+static int ilog2(double v)
+{
+    int k = 0;
+    while (v >= 2.0 && k < 62) v *= 0.5, k++;
+    return k;
+}
+
+GB300Processor::Tc3Plan GB300Processor::tc3Plan(int n, const Plane* in, const Plane* out, const Phase2* ph, const void* w,
+                                                bool bf16, int* counter, cudaStream_t stream, bool& ran, cudaError_t& err)
+{
+    ran = false;
+    err = cudaSuccess;
+    Tc3Plan plan;
+    if (tc3Shape_ >= 0) plan.shape = tc3Shape_;
+    if (tc3PerSm_ > 0) plan.perSm = tc3PerSm_;
+    if (!autotune_ || tc3Shape_ >= 0 || tc3PerSm_ > 0) return plan;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) return plan;
+    double total = 0.0, sw = 0.0, sh = 0.0;
+    for (int i = 0; i < n; i++)
+    {
+        total += static_cast<double>(in[i].w) * in[i].h;
+        sw += in[i].w;
+        sh += in[i].h;
+    }
+    const auto key = std::make_tuple(in[0].type, in[0].channels, bf16 ? 1 : 0, ilog2(total), ilog2(sw / n), ilog2(sh / n));
+    {
+        std::lock_guard<std::mutex> lock(mutex_);
+        auto it = plans_.find(key);
+        if (it != plans_.end()) return it->second;
+    }
+    // Measure every shape x {2, 1} CTAs per SM: one warm launch, then two
+    // timed ones with events on the launching stream.  Each candidate writes
+    // the same bytes, so the output is valid afterwards.
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if ((err = cudaEventCreate(&e0)) != cudaSuccess) return plan;
+    if ((err = cudaEventCreate(&e1)) != cudaSuccess)
+    {
+        cudaEventDestroy(e0);
+        return plan;
+    }
+    const int ctas = tc3Ctas_ > 0 ? tc3Ctas_ : smCount_;
+    float best = 1e30f;
+    Tc3Plan bestPlan = plan;
+    for (int shape = 0; shape < kTc3Shapes && err == cudaSuccess; shape++)
+        for (int perSm = 2; perSm >= 1 && err == cudaSuccess; perSm--)
+        {
+            err = launch_acnet_legacy_tc3(*acnet_, w, bf16, n, in, out, ph, counter, ctas, stream, shape, perSm);
+            if (err == cudaSuccess) err = cudaEventRecord(e0, stream);
+            for (int r = 0; r < 2 && err == cudaSuccess; r++)
+                err = launch_acnet_legacy_tc3(*acnet_, w, bf16, n, in, out, ph, counter, ctas, stream, shape, perSm);
+            if (err == cudaSuccess) err = cudaEventRecord(e1, stream);
+            if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+            float ms = 0.0f;
+            if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+            if (err == cudaSuccess && ms < best)
+            {
+                best = ms;
+                bestPlan.shape = shape;
+                bestPlan.perSm = perSm;
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (err != cudaSuccess) return plan;
+    ran = true;
+    std::lock_guard<std::mutex> lock(mutex_);
+    plans_[key] = bestPlan;
+    return bestPlan;
 }
 
 static inline int align_pitch(int bytes) { return (bytes + 255) & ~255; }
@@ -732,6 +822,140 @@ int GB300Processor::processDevice(const DeviceImage& src, const DeviceImage& dst
     if (dst.w != ow || dst.h != oh || dst.c != src.c || dst.type != src.type) return fail(ts, "dst has the wrong shape or type"), -1;
     cudaStream_t s = stream ? stream : ts.stream;
     if (!run(ts, src, dst, factor, s)) return -1;
+    if (sync)
+    {
+        cudaError_t err = cudaStreamSynchronize(s);
+        if (err != cudaSuccess) return fail(ts, "kernel execution", err), -1;
+        if (precision_ != Precision::FP32 && tc_status_reset() != 0) return fail(ts, "tensor-core wait timed out"), -1;
+    }
+    return 0;
+}
+
+int GB300Processor::processBatchDevice(int n, const DeviceImage* src, const DeviceImage* dst, double factor, cudaStream_t stream,
+                                       bool sync)
+{
+    ThreadState& ts = state();
+    if (!begin(ts)) return -1;
+    if (n < 0 || (n > 0 && (!src || !dst))) return fail(ts, "batch: bad image arrays"), -1;
+    cudaStream_t s = stream ? stream : ts.stream;
+    for (int i = 0; i < n; i++)
+    {
+        if (!src[i].ptr || !dst[i].ptr) return fail(ts, "null device pointer"), -1;
+        if (!validate(ts, src[i].w, src[i].h, src[i].c, src[i].type, factor)) return -1;
+        int ow, oh;
+        output_shape(src[i].w, src[i].h, src[i].c, factor, ow, oh);
+        if (src[i].c == 1 && factor / static_cast<double>(1 << (factor > 2.0 ? ceil_log2(factor) : 1)) != 1.0)
+        {
+            ow = dst[i].w;
+            oh = dst[i].h;
+        }
+        if (dst[i].w != ow || dst[i].h != oh || dst[i].c != src[i].c || dst[i].type != src[i].type)
+            return fail(ts, "dst has the wrong shape or type"), -1;
+    }
+    const bool batched = spec_.family == Family::ACNetLegacy && precision_ != Precision::FP32 && tcKernel_ == 3 &&
+                         factor == 2.0 && fused_;
+    if (!batched)
+    {
+        for (int i = 0; i < n; i++)
+            if (!run(ts, src[i], dst[i], factor, s)) return -1;
+    }
+    else
+    {
+        const bool bf16 = precision_ == Precision::BF16;
+        const void* w = tcWeights(precision_, true);
+        if (!w) return fail(ts, "tensor-core weights", cudaErrorMemoryAllocation), -1;
+        cudaError_t err = ts.counter.ensure(256);
+        if (err != cudaSuccess) return fail(ts, "device allocation", err), -1;
+        int* counter = static_cast<int*>(ts.counter.ptr);
+        Phase2 ph;
+        if (!phase_weights(2, &ph.w[0][0])) return fail(ts, "chroma resample weights"), -1;
+        const int maxImages = std::min(acnet_tc3_max_images(), 64);
+        std::vector<int> order(n);
+        for (int i = 0; i < n; i++) order[i] = i;
+        // groups of one channel count and element type, in chunks of at most 64 images
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            return std::make_pair(src[a].c, src[a].type) < std::make_pair(src[b].c, src[b].type);
+        });
+        Plane in[64], out[64];
+        for (int g0 = 0; g0 < n;)
+        {
+            int g1 = g0;
+            while (g1 < n && g1 - g0 < maxImages && src[order[g1]].c == src[order[g0]].c &&
+                   src[order[g1]].type == src[order[g0]].type)
+                g1++;
+            const int m = g1 - g0;
+            uint64_t sig = 1469598103934665603ull;  // FNV-1a over the launch's arguments
+            auto mix = [&sig](uint64_t v) {
+                for (int b = 0; b < 8; b++) sig = (sig ^ ((v >> (8 * b)) & 0xff)) * 1099511628211ull;
+            };
+            mix(static_cast<uint64_t>(m));
+            mix(static_cast<uint64_t>(bf16));
+            mix(reinterpret_cast<uint64_t>(w));
+            for (int j = 0; j < m; j++)
+            {
+                const DeviceImage& a = src[order[g0 + j]];
+                const DeviceImage& b = dst[order[g0 + j]];
+                in[j] = plane_of(a);
+                out[j] = plane_of(b);
+                mix(reinterpret_cast<uint64_t>(a.ptr));
+                mix(reinterpret_cast<uint64_t>(b.ptr));
+                mix((static_cast<uint64_t>(a.w) << 32) | static_cast<uint32_t>(a.h));
+                mix((static_cast<uint64_t>(a.stride) << 32) | static_cast<uint32_t>(b.stride));
+                mix((static_cast<uint64_t>(a.c) << 32) | static_cast<uint32_t>(a.type));
+            }
+            const Phase2* php = in[0].channels > 1 ? &ph : nullptr;
+            bool ran = false;
+            const Tc3Plan plan = tc3Plan(m, in, out, php, w, bf16, counter, s, ran, err);
+            if (err != cudaSuccess) return fail(ts, "batched upscale", err), -1;
+            mix(static_cast<uint64_t>(plan.shape * 4 + plan.perSm));
+            const int ctas = tc3Ctas_ > 0 ? tc3Ctas_ : smCount_;
+            cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+            if ((err = cudaStreamIsCapturing(s, &cap)) != cudaSuccess) return fail(ts, "stream state", err), -1;
+            auto git = ts.graphs.find(sig);
+            if (ran)
+            {
+            }
+            else if (cap == cudaStreamCaptureStatusNone && git != ts.graphs.end())
+            {
+                // the same batch again: replay its graph (memset + persistent kernel)
+                if ((err = cudaGraphLaunch(git->second.exec, s)) != cudaSuccess) return fail(ts, "graph launch", err), -1;
+                count_launch();
+                g_graph_replays++;
+            }
+            else if (cap == cudaStreamCaptureStatusNone && ts.seen.count(sig) && ts.graphs.size() < 64)
+            {
+                // second sighting: capture the launch into a graph, then replay it
+                GraphEntry ge;
+                if ((err = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+                    return fail(ts, "stream capture", err), -1;
+                const cudaError_t lerr = launch_acnet_legacy_tc3(*acnet_, w, bf16, m, in, out, php, counter, ctas, s,
+                                                                 plan.shape, plan.perSm);
+                err = cudaStreamEndCapture(s, &ge.graph);
+                if (lerr != cudaSuccess || err != cudaSuccess)
+                {
+                    if (ge.graph) cudaGraphDestroy(ge.graph);
+                    return fail(ts, "stream capture", lerr != cudaSuccess ? lerr : err), -1;
+                }
+                if ((err = cudaGraphInstantiate(&ge.exec, ge.graph, 0)) != cudaSuccess)
+                {
+                    cudaGraphDestroy(ge.graph);
+                    return fail(ts, "graph instantiation", err), -1;
+                }
+                ts.graphs[sig] = ge;
+                if ((err = cudaGraphLaunch(ge.exec, s)) != cudaSuccess) return fail(ts, "graph launch", err), -1;
+                g_graph_replays++;
+            }
+            else
+            {
+                if (ts.seen.size() >= 4096) ts.seen.clear();
+                ts.seen[sig] = 1;
+                if ((err = launch_acnet_legacy_tc3(*acnet_, w, bf16, m, in, out, php, counter, ctas, s, plan.shape,
+                                                   plan.perSm)) != cudaSuccess)
+                    return fail(ts, "batched upscale", err), -1;
+            }
+            g0 = g1;
+        }
+    }
     if (sync)
     {
         cudaError_t err = cudaStreamSynchronize(s);

@@ -2,6 +2,7 @@
 // C ABI translation unit).
 #pragma once
 
+#include <cstdint>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -18,6 +19,8 @@ namespace acgb {
 int ceil_log2(double v);
 void make_axis_table(int n_in, int n_out, int mode, std::vector<int>& first, std::vector<float>& weights, int& taps);
 bool phase_weights(int F, float* w);
+// CUDA graphs of batched launches replayed in this process so far.
+uint64_t graph_replays();
 
 // Grow-only device allocation.
 struct DeviceBuffer
@@ -42,6 +45,13 @@ public:
     // `stream` (the calling thread's own stream when null).  Returns 0 or -1
     // (details through ok()/error()).
     int processDevice(const DeviceImage& src, const DeviceImage& dst, double factor, cudaStream_t stream, bool sync);
+
+    // Processor::process over n device images.  ACNetLegacy x2 in a
+    // tensor-core form runs each group of images with one channel count and
+    // element type as ONE persistent launch (tile shape and CTAs per SM from
+    // the autotuner; a repeated identical batch replays a captured CUDA
+    // graph); anything else runs image by image.  Returns 0 or -1.
+    int processBatchDevice(int n, const DeviceImage* src, const DeviceImage* dst, double factor, cudaStream_t stream, bool sync);
 
     // Allocation-free x2 of n device images in one persistent tensor-core
     // launch on `stream` (ACNetLegacy, FP16/BF16 form).  Returns 0, -1 when
@@ -70,6 +80,16 @@ private:
         DeviceBuffer dev;
         ResizeAxis axis;
     };
+    struct Tc3Plan
+    {
+        int shape = 0;  // tile geometry of the persistent kernel
+        int perSm = 2;  // CTAs per SM (cap)
+    };
+    struct GraphEntry
+    {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+    };
     struct ThreadState
     {
         cudaStream_t stream = nullptr;
@@ -82,6 +102,8 @@ private:
         std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;  // recorded pairs
         std::vector<double> eventPixels;                           // output pixels per pair
         std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pool;     // free pairs
+        std::unordered_map<uint64_t, GraphEntry> graphs;           // captured batches by signature
+        std::unordered_map<uint64_t, int> seen;                    // batch signatures launched directly so far
     };
 
     static Precision default_precision();
@@ -93,6 +115,13 @@ private:
     const ResizeAxis* axis(ThreadState& ts, int n_in, int n_out, int mode, cudaStream_t stream, cudaError_t& err);
     cudaError_t luma_pass(ThreadState& ts, const Plane& in, const Plane& out, const Phase2* ph, cudaStream_t stream);
     const void* tcWeights(Precision p, bool pairForm);
+    // Tile shape and CTAs per SM for a persistent launch over these images:
+    // forced by AC_GB300_TC3_SHAPE / AC_GB300_TC3_PER_SM, else measured once
+    // per batch class (element type, channels, form, log2 of the total and
+    // mean image sizes) over every shape x {2, 1} CTAs per SM.  When it
+    // measured, the launches already produced the output (`ran`).
+    Tc3Plan tc3Plan(int n, const Plane* in, const Plane* out, const Phase2* ph, const void* w, bool bf16, int* counter,
+                    cudaStream_t stream, bool& ran, cudaError_t& err);
 
     int device_ = -1;
     int smCount_ = 0;
@@ -106,6 +135,10 @@ private:
     int tc3Ctas_ = 0;                // CTAs of the persistent kernel (0: one per SM; AC_GB300_TC3_CTAS)
     bool fused_ = true;              // RGB(A) x2 in one fused kernel (AC_GB300_FUSED=0 disables)
     int tcKernel_ = 3;               // tensor-core kernel: 3 persistent (default), 2 pair-interleaved, 1 one-pixel-per-row (AC_GB300_TC_KERNEL)
+    int tc3Shape_ = -1;              // forced tile shape (AC_GB300_TC3_SHAPE), -1: autotuned
+    int tc3PerSm_ = 0;               // forced CTAs per SM (AC_GB300_TC3_PER_SM), 0: autotuned
+    bool autotune_ = true;           // AC_GB300_AUTOTUNE=0: default shape, two CTAs per SM
+    std::map<std::tuple<int, int, int, int, int, int>, Tc3Plan> plans_;
     std::mutex mutex_;
     std::unordered_map<std::thread::id, std::unique_ptr<ThreadState>> states_;
 };

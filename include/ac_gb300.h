@@ -49,6 +49,22 @@ AC_C_API int ac_gb300_output_shape(int width, int height, int channels, double f
 AC_C_API int ac_gb300_process_device(ACProcessor* processor, const ACGB300DeviceImage* src, const ACGB300DeviceImage* dst,
                                      double factor, void* stream, int sync);
 
+/* Processor::process over `count` device images at once, each src/dst pair
+ * as for ac_gb300_process_device.  An ACNetLegacy model at factor 2 in the
+ * FP16 or BF16 form runs every group of images with one channel count and
+ * element type (up to 64 per launch, any mix of sizes) as ONE persistent
+ * tensor-core launch over a shared tile queue.  The tile shape and CTAs per
+ * SM come from a measured autotune the first time a batch class (element
+ * type, channels, form, total and mean image size) is seen; a repeated
+ * identical batch (same buffers and shapes) replays a captured CUDA graph.
+ * Other models, factors and forms process the images one after another.
+ * Returns AC_SUCCESS or AC_ERROR(AC_EPROCESSOR) / AC_ERROR(AC_EINVAL). */
+AC_C_API int ac_gb300_process_batch_device(ACProcessor* processor, int count, const ACGB300DeviceImage* src,
+                                           const ACGB300DeviceImage* dst, double factor, void* stream, int sync);
+
+/* Number of batched launches this process has run as CUDA graph replays. */
+AC_C_API uint64_t ac_gb300_graph_replays(void);
+
 /* Allocation-free x2 upscale of `count` device images in ONE persistent
  * tensor-core launch.  No reference counterpart: the reference's processors
  * allocate their work buffers inside each call.  It is for callers that must

@@ -1,0 +1,124 @@
+"""Batched persistent launches over a shared tile queue, the tile-shape
+variants, the autotuner and CUDA-graph replay (GPU required).
+
+Every tile shape computes each output pixel from the same window with the
+same arithmetic, so all of them, the batched launch and the per-image path
+must give identical bytes.
+"""
+import numpy as np
+import pytest
+
+import anime4kcpp_gb300 as ac
+import oracle
+from anime4kcpp_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from anime4kcpp_gb300 import build
+    build.build()
+    oracle.build()
+
+
+def _frames():
+    rng = np.random.default_rng(11)
+    imgs = []
+    for i in range(7):
+        h, w = int(rng.integers(40, 300)), int(rng.integers(40, 400))
+        imgs.append(synthetic.rgb_u8(h, w, seed=100 + i))
+    for i in range(3):
+        imgs.append(synthetic.luma(int(rng.integers(20, 200)), int(rng.integers(20, 200)), np.uint8, seed=200 + i))
+    for i in range(2):
+        imgs.append(synthetic.rgb_u8(int(rng.integers(30, 120)), int(rng.integers(30, 120)), seed=300 + i, alpha=True))
+    return imgs
+
+
+def _out_like(s):
+    return torch.empty((2 * s.shape[0], 2 * s.shape[1]) + tuple(s.shape[2:]), dtype=s.dtype, device="cuda")
+
+
+def _per_image(p, srcs):
+    outs = []
+    for s in srcs:
+        d = _out_like(s)
+        p.process_device(s, d, 2.0)
+        outs.append(d.cpu().numpy())
+    return outs
+
+
+@pytest.mark.parametrize("form", ["fp16", "bf16"])
+def test_batch_matches_per_image_and_replays_graphs(form):
+    frames = _frames()
+    p = ac.Processor("cuda", 0, "acnet-legacy-hdn1", precision=form)
+    srcs = [torch.from_numpy(f).cuda() for f in frames]
+    want = _per_image(p, srcs)
+    dsts = [_out_like(s) for s in srcs]
+    groups = 3  # RGB, gray and RGBA images form one launch each
+    for call in range(4):
+        for d in dsts:
+            d.zero_()
+        before = ac.graph_replays()
+        p.process_batch_device(srcs, dsts, 2.0)
+        for d, w in zip(dsts, want):
+            assert np.array_equal(d.cpu().numpy(), w)
+        replays = ac.graph_replays() - before
+        # call 0 measures the plan, call 1 launches directly, calls 2 and 3
+        # capture once and replay the graph
+        assert replays == (groups if call >= 2 else 0)
+    ref = oracle.process(frames[0], 2.0, "acnet-legacy-hdn1").astype(int)
+    d = np.abs(want[0].astype(int) - ref)
+    assert (d <= 1).mean() >= 0.99
+
+
+@pytest.mark.parametrize("c", [1, 3, 4])
+def test_tile_shapes_and_cta_caps_give_identical_bytes(c, monkeypatch):
+    if c == 1:
+        x = synthetic.luma(131, 150, np.uint16, seed=9)
+    else:
+        x = synthetic.rgb_u8(131, 150, seed=9, alpha=(c == 4))
+    src = torch.from_numpy(x).cuda()
+    outs = []
+    for shape in ("0", "1", "2"):
+        for per_sm in ("1", "2"):
+            monkeypatch.setenv("AC_GB300_TC3_SHAPE", shape)
+            monkeypatch.setenv("AC_GB300_TC3_PER_SM", per_sm)
+            p = ac.Processor("cuda", 0, "acnet-legacy-hdn2", precision="fp16")
+            d = _out_like(src)
+            p.process_device(src, d, 2.0)
+            outs.append(d.cpu().numpy())
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+
+
+def test_autotuned_equals_untuned(monkeypatch):
+    x = synthetic.rgb_u8(300, 500, seed=21)
+    src = torch.from_numpy(x).cuda()
+    outs = []
+    for tune in ("1", "0"):
+        monkeypatch.setenv("AC_GB300_AUTOTUNE", tune)
+        p = ac.Processor("cuda", 0, "acnet-legacy-hdn0", precision="fp16")
+        d = _out_like(src)
+        p.process_device(src, d, 2.0)
+        outs.append(d.cpu().numpy())
+    assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("form,factor", [("fp32", 2.0), ("fp16", 4.0)])
+def test_batch_falls_back_per_image(form, factor):
+    frames = [synthetic.rgb_u8(41, 67, seed=1), synthetic.luma(33, 29, np.uint8, seed=2)]
+    p = ac.Processor("cuda", 0, "acnet-legacy-hdn0", precision=form)
+    srcs = [torch.from_numpy(f).cuda() for f in frames]
+    want = []
+    dsts = []
+    for s in srcs:
+        f = int(factor)
+        d = torch.empty((f * s.shape[0], f * s.shape[1]) + tuple(s.shape[2:]), dtype=s.dtype, device="cuda")
+        p.process_device(s, d, factor)
+        want.append(d.cpu().numpy())
+        dsts.append(torch.empty_like(d))
+    p.process_batch_device(srcs, dsts, factor)
+    for d, w in zip(dsts, want):
+        assert np.array_equal(d.cpu().numpy(), w)
