@@ -14,6 +14,11 @@ Voronoi-edge images (no public dataset is attached to this workload).
          D2H copies inside the timed region (several host threads share one
          processor, as the reference CLI does)
 
+  batch  the batching workload: 64 RGB u8 images of uneven sizes (w in
+         [256, 2048], h in [256, 1536]) x2 with ACNetLegacy HDN1, FP16 as one
+         persistent launch per step (autotuned tile shape, CUDA-graph replay)
+         against FP32 per-image launches
+
 --impl reference times the reference CPU path instead (the reference CPU
 processor built from its sources where available, else the project's C
 restatement of it) on the host cores, one frame per step.
@@ -257,6 +262,68 @@ def time_e2e(ac, torch, proc, frames_host, outs_host, frames, steps, warmup, thr
     return time.perf_counter() - t0
 
 
+BATCH_MODEL = "acnet-legacy-hdn1"
+
+
+def batch_images(n=64, seed=3):
+    """n RGB u8 images with width uniform in [256, 2048] and height uniform in
+    [256, 1536] (seeded), cut at seeded offsets from four 2048x1536 Voronoi-edge
+    canvases (256 cells each)."""
+    from anime4kcpp_gb300 import synthetic
+    canvases = [synthetic.rgb_u8(1536, 2048, cells=256, seed=seed * 10 + i) for i in range(4)]
+    rng = np.random.default_rng(seed)
+    out = []
+    for i, (h, w) in enumerate(synthetic.uneven_sizes(n, seed=seed)):
+        c = canvases[i % 4]
+        y0, x0 = int(rng.integers(0, 1536 - h + 1)), int(rng.integers(0, 2048 - w + 1))
+        out.append(np.ascontiguousarray(c[y0:y0 + h, x0:x0 + w]))
+    return out
+
+
+def time_batch(ac, torch, args):
+    """The batching workload: 64 uneven RGB u8 images x2 with ACNetLegacy HDN1.
+    FP16: one persistent launch per step over all images (autotuned tile
+    shape, replayed CUDA graph); FP32: one launch per image.  Output Mpx/s
+    with inputs resident in HBM, CUDA events on the launching stream."""
+    imgs = batch_images()
+    srcs = [torch.from_numpy(x).cuda() for x in imgs]
+    dsts = [torch.empty((2 * x.shape[0], 2 * x.shape[1], 3), dtype=torch.uint8, device="cuda") for x in imgs]
+    out_px = sum(4 * x.shape[0] * x.shape[1] for x in imgs)
+    stream = torch.cuda.Stream()
+    res = {"workload": "64 RGB u8 images, w~U[256,2048], h~U[256,1536] (seed 3), x2 ACNetLegacy HDN1",
+           "out_mpx_per_step": out_px / 1e6}
+    for form, steps in (("fp16", max(3, args.batch_steps)), ("fp32", max(3, args.batch_steps // 4))):
+        proc = ac.Processor("cuda", 0, BATCH_MODEL, precision=form)
+        with torch.cuda.stream(stream):
+            h = stream.cuda_stream
+
+            def step():
+                if form == "fp32":
+                    for a, b in zip(srcs, dsts):
+                        proc.process_device(a, b, 2.0, stream=h, sync=False)
+                else:
+                    proc.process_batch_device(srcs, dsts, 2.0, stream=h, sync=False)
+
+            for _ in range(max(3, args.warmup)):
+                step()
+            torch.cuda.synchronize()
+            l0, r0 = ac.launch_count(), ac.graph_replays()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if not proc.ok():
+            raise RuntimeError(proc.error())
+        res[form] = {"value": out_px * steps / (ms / 1e3) / 1e6, "unit": "Mpx/s", "ms_per_batch": ms / steps,
+                     "steps": steps, "launches_per_batch": (ac.launch_count() - l0) / steps,
+                     "graph_replays_per_batch": (ac.graph_replays() - r0) / steps}
+    res["fp16_over_fp32"] = res["fp16"]["value"] / res["fp32"]["value"]
+    return res
+
+
 def run_gb300(args, rank, world, local_rank):
     import torch
 
@@ -360,6 +427,8 @@ def run_gb300(args, rank, world, local_rank):
                 out["%s_over_fp32" % tc] = forms[tc]["value"] / forms["fp32"]["value"]
     clocks = sampler.summary() if sampler else None
     out["clocks"] = clocks
+    if rank == 0 and world == 1 and not args.no_batch:
+        out["batch"] = time_batch(ac, torch, args)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     return out
@@ -376,6 +445,8 @@ def main():
     ap.add_argument("--e2e-threads", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-image batching workload")
+    ap.add_argument("--batch-steps", type=int, default=12)
     args = ap.parse_args()
     args.forms = [f for f in args.forms.split(",") if f]
     args.warmup = max(args.warmup, 3)
