@@ -145,7 +145,8 @@ __device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity, volatil
 {
     if (tc::mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = tc::global_timer_ns();
-    while (!tc::mbar_try_wait(bar, parity))
+    // waiting warps sleep in the barrier unit rather than taking issue slots
+    while (!tc::mbar_try_wait_hint(bar, parity, 20000u))
     {
         if (*abort_flag) return false;
         if (tc::global_timer_ns() - t0 > kWaitNs)
@@ -266,6 +267,7 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
         const int W = I.in.w, H = I.in.h;
         const int ix0 = max(0, -gx0), ix1 = min(WW - 1, W - 1 - gx0);
         const int iy0 = max(0, -gy0), iy1 = min(WH - 1, H - 1 - gy0);
+        const bool edges = ix0 > 0 || ix1 < WW - 1 || iy0 > 0 || iy1 < WH - 1;  // an image edge inside the window
 
         // ---- prologue (all warps): window luma (+ chroma region), layer 0 ----
         // Loads are issued in batches of four pixels per thread before any
@@ -440,7 +442,8 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
                                 {
                                     const uint4 val = pack8<BF16>(v + 8 * k);
                                     *slot<G>(act, p) = val;
-                                    // clamp-to-edge for the next layer
+                                    // clamp-to-edge for the next layer (only tiles at an image edge)
+                                    if (!edges) continue;
                                     const bool xl = x == ix0 && x > 0, xr = x == ix1 && x < WW - 1;
                                     const bool yt = y == iy0 && y > 0, yb = y == iy1 && y < WH - 1;
                                     if (xl) *slot<G>(act, p - 1) = val;

@@ -120,6 +120,21 @@ __device__ __forceinline__ uint32_t mbar_try_wait(uint64_t* mbar, uint32_t phase
         : "memory");
     return ok;
 }
+// try_wait with a suspend-time hint: the thread is suspended until the phase
+// completes or about `ns` nanoseconds pass, instead of re-issuing polls.
+__device__ __forceinline__ uint32_t mbar_try_wait_hint(uint64_t* mbar, uint32_t phase, uint32_t ns)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t"
+        "}"
+        : "=r"(ok)
+        : "r"(smem_u32(mbar)), "r"(phase), "r"(ns)
+        : "memory");
+    return ok;
+}
 // Bounded wait: gives up after `limit` polls and returns false.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mbar, uint32_t phase, uint32_t limit)
 {
