@@ -59,7 +59,7 @@ EXPORTS = (
     "ac_gb300_set_precision", "ac_gb300_get_precision", "ac_gb300_output_shape", "ac_gb300_process_device",
     "ac_gb300_launch_count", "ac_gb300_model_params", "ac_gb300_profile_enable", "ac_gb300_profile_collect",
     "ac_gb300_tc_selftest", "ac_gb300_process_device_noalloc", "ac_gb300_process_batch_device",
-    "ac_gb300_graph_replays",
+    "ac_gb300_graph_replays", "ac_gb300_process_yuv_device",
 )
 
 _lock = threading.Lock()
@@ -97,6 +97,7 @@ def native():
             "ac_gb300_process_device_noalloc": (I, [pproc, I, P(ACGB300DeviceImage), P(ACGB300DeviceImage), V, I]),
             "ac_gb300_process_batch_device": (I, [pproc, I, P(ACGB300DeviceImage), P(ACGB300DeviceImage), D, V, I]),
             "ac_gb300_graph_replays": (ctypes.c_uint64, []),
+            "ac_gb300_process_yuv_device": (I, [pproc, I, I, P(ACGB300DeviceImage), P(ACGB300DeviceImage), D, I, V, I]),
             "ac_gb300_launch_count": (ctypes.c_uint64, []),
             "ac_gb300_model_params": (I, [ctypes.c_char_p, V, I, V, I, V, I, P(I)]),
             "ac_gb300_profile_enable": (I, [pproc, I]),
@@ -238,6 +239,25 @@ class Processor:
         s, d = arr(*[_dev(x) for x in srcs]), arr(*[_dev(x) for x in dsts])
         rc = native().ac_gb300_process_batch_device(ctypes.byref(self._p), n, s, d, float(factor),
                                                     ctypes.c_void_p(stream or 0), 1 if sync else 0)
+        if rc != AC_SUCCESS:
+            raise RuntimeError(self.error())
+
+    def process_yuv_device(self, frames, outs, factor=2.0, shift=0, stream=None, sync=True):
+        """The reference CLI's planar video recipe on device frames
+        (``ac_gb300_process_yuv_device``): ``frames`` and ``outs`` are lists
+        of per-frame plane tuples (Y, U, V) or (Y, UV); Y is shifted left by
+        ``shift``, upscaled and shifted back, the other planes are resized to
+        their out planes' sizes with Catmull-Rom."""
+        if len(frames) != len(outs) or not frames:
+            raise ValueError("frames and outs must be non-empty lists of equal length")
+        planes = len(frames[0])
+        if any(len(f) != planes for f in frames) or any(len(o) != planes for o in outs):
+            raise ValueError("every frame needs the same number of planes")
+        arr = ACGB300DeviceImage * (len(frames) * planes)
+        s = arr(*[_dev(p) for f in frames for p in f])
+        d = arr(*[_dev(p) for o in outs for p in o])
+        rc = native().ac_gb300_process_yuv_device(ctypes.byref(self._p), len(frames), planes, s, d, float(factor), int(shift),
+                                                  ctypes.c_void_p(stream or 0), 1 if sync else 0)
         if rc != AC_SUCCESS:
             raise RuntimeError(self.error())
 

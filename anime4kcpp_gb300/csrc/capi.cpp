@@ -352,6 +352,23 @@ int ac_gb300_process_batch_device(ACProcessor* processor, int count, const ACGB3
 
 uint64_t ac_gb300_graph_replays(void) { return acgb::graph_replays(); }
 
+int ac_gb300_process_yuv_device(ACProcessor* processor, int frames, int planes, const ACGB300DeviceImage* src,
+                                const ACGB300DeviceImage* dst, double factor, int shift, void* stream, int sync)
+{
+    auto* g = gpu_of(processor);
+    if (!g || frames < 1 || planes < 1 || planes > 4 || !src || !dst) return AC_ERROR(AC_EINVAL);
+    const int n = frames * planes;
+    std::vector<acgb::DeviceImage> s(n), d(n);
+    for (int i = 0; i < n; i++)
+    {
+        s[i] = acgb::DeviceImage{src[i].ptr, src[i].width, src[i].height, src[i].channels, src[i].stride, src[i].element_type};
+        d[i] = acgb::DeviceImage{dst[i].ptr, dst[i].width, dst[i].height, dst[i].channels, dst[i].stride, dst[i].element_type};
+    }
+    const int rc = g->processYuvDevice(frames, planes, s.data(), d.data(), factor, shift, static_cast<cudaStream_t>(stream),
+                                       sync != 0);
+    return rc == 0 ? AC_SUCCESS : AC_ERROR(AC_EPROCESSOR);
+}
+
 int ac_gb300_process_device_noalloc(ACProcessor* processor, int count, const ACGB300DeviceImage* src,
                                     const ACGB300DeviceImage* dst, void* stream, int sync)
 {

@@ -239,6 +239,19 @@ __global__ void resize_kernel(Plane src, Plane dst, ResizeAxis ax, ResizeAxis ay
     for (int c = 0; c < NC; c++) out[c] = encode_resampled<T>(resample<T, NC>(src, ax, ay, x, y, c));
 }
 
+// Element-wise shift of an integer plane, shl / shr of
+// core/src/ImageProcess.cpp:601-616: n > 0 shifts left, n < 0 right; the
+// result is stored back in the element type (a left shift drops high bits).
+// In place when src and dst are the same plane.
+template <typename T>
+__global__ void shift_kernel(Plane src, Plane dst, int n)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x >= src.w * src.channels) return;
+    const unsigned v = row_ptr<T>(src.ptr, src.pitch, y)[x];
+    row_ptr_w<T>(dst.ptr, dst.pitch, y)[x] = static_cast<T>(n >= 0 ? (v << n) : (v >> (-n)));
+}
+
 namespace {
 
 dim3 row_grid(int w, int h, int block) { return dim3((w + block - 1) / block, h); }
@@ -322,6 +335,21 @@ cudaError_t launch_merge_int(const Plane& y, const Plane& uv, int factor, const 
     if (factor == 2) return launch_merge_int_f<2>(y, uv, phase_weights, rgb, stream);
     if (factor == 4) return launch_merge_int_f<4>(y, uv, phase_weights, rgb, stream);
     return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_shift(const Plane& src, const Plane& dst, int n, cudaStream_t stream)
+{
+    if (src.w <= 0 || src.h <= 0 || n == 0) return cudaSuccess;
+    if (n <= -16 || n >= 16) return cudaErrorInvalidValue;
+    dim3 grid = row_grid(src.w * src.channels, src.h, 256);
+    switch (src.type)
+    {
+    case kU8: shift_kernel<uint8_t><<<grid, 256, 0, stream>>>(src, dst, n); break;
+    case kU16: shift_kernel<uint16_t><<<grid, 256, 0, stream>>>(src, dst, n); break;
+    default: return cudaErrorInvalidValue;
+    }
+    count_launch();
+    return cudaGetLastError();
 }
 
 cudaError_t launch_resize(const Plane& src, const Plane& dst, ResizeAxis ax, ResizeAxis ay, cudaStream_t stream)

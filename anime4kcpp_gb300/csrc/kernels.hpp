@@ -117,6 +117,10 @@ cudaError_t launch_merge_int(const Plane& y, const Plane& uv, int factor, const 
                              cudaStream_t stream);
 int merge_int_phase_offset(int factor, int k);
 
+// Element-wise shl (n > 0) / shr (n < 0) of a u8 or u16 plane; src == dst
+// allowed (core/src/ImageProcess.cpp:601-616).
+cudaError_t launch_shift(const Plane& src, const Plane& dst, int n, cudaStream_t stream);
+
 // General separable resize of an interleaved plane (any channel count).
 cudaError_t launch_resize(const Plane& src, const Plane& dst, ResizeAxis ax, ResizeAxis ay, cudaStream_t stream);
 

@@ -324,6 +324,8 @@ GB300Processor::~GB300Processor()
         ts.out.release();
         for (auto& m : ts.maps) m.release();
         ts.counter.release();
+        ts.batchTmp.release();
+        ts.yuvTmp.release();
         for (auto& t : ts.tables) t.second.dev.release();
         for (auto& e : ts.events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
         for (auto& e : ts.pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -831,44 +833,51 @@ int GB300Processor::processDevice(const DeviceImage& src, const DeviceImage& dst
     return 0;
 }
 
-int GB300Processor::processBatchDevice(int n, const DeviceImage* src, const DeviceImage* dst, double factor, cudaStream_t stream,
-                                       bool sync)
+// Validated images: the batched persistent launches (ACNetLegacy x2, or x4
+// of 1-channel planes as two chained batched x2 passes, in a tensor-core
+// form), else image by image.
+bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, const DeviceImage* dst, double factor,
+                              cudaStream_t s)
 {
-    ThreadState& ts = state();
-    if (!begin(ts)) return -1;
-    if (n < 0 || (n > 0 && (!src || !dst))) return fail(ts, "batch: bad image arrays"), -1;
-    cudaStream_t s = stream ? stream : ts.stream;
-    for (int i = 0; i < n; i++)
+    const bool tcBatch = spec_.family == Family::ACNetLegacy && precision_ != Precision::FP32 && tcKernel_ == 3 && fused_;
+    bool gray4 = tcBatch && factor == 4.0 && n > 0;
+    for (int i = 0; i < n && gray4; i++)
+        gray4 = src[i].c == 1 && dst[i].w == 4 * src[i].w && dst[i].h == 4 * src[i].h;
+    if (gray4)
     {
-        if (!src[i].ptr || !dst[i].ptr) return fail(ts, "null device pointer"), -1;
-        if (!validate(ts, src[i].w, src[i].h, src[i].c, src[i].type, factor)) return -1;
-        int ow, oh;
-        output_shape(src[i].w, src[i].h, src[i].c, factor, ow, oh);
-        if (src[i].c == 1 && factor / static_cast<double>(1 << (factor > 2.0 ? ceil_log2(factor) : 1)) != 1.0)
+        // x4 of 1-channel planes: two chained batched x2 passes through
+        // 2x temporaries (the reference's power-of-two pass loop)
+        std::vector<DeviceImage> mid(n);
+        std::vector<size_t> off(n);
+        size_t total = 0;
+        for (int i = 0; i < n; i++)
         {
-            ow = dst[i].w;
-            oh = dst[i].h;
+            const int es = src[i].type & 0xff, pitch = align_pitch(2 * src[i].w * es);
+            off[i] = total;
+            total += (static_cast<size_t>(pitch) * 2 * src[i].h + 255) & ~static_cast<size_t>(255);
+            mid[i] = DeviceImage{nullptr, 2 * src[i].w, 2 * src[i].h, 1, pitch, src[i].type};
         }
-        if (dst[i].w != ow || dst[i].h != oh || dst[i].c != src[i].c || dst[i].type != src[i].type)
-            return fail(ts, "dst has the wrong shape or type"), -1;
+        cudaError_t err = ts.batchTmp.ensure(total);
+        if (err != cudaSuccess) return fail(ts, "device allocation", err), false;
+        for (int i = 0; i < n; i++) mid[i].ptr = static_cast<char*>(ts.batchTmp.ptr) + off[i];
+        return batchRun(ts, n, src, mid.data(), 2.0, s) && batchRun(ts, n, mid.data(), dst, 2.0, s);
     }
-    const bool batched = spec_.family == Family::ACNetLegacy && precision_ != Precision::FP32 && tcKernel_ == 3 &&
-                         factor == 2.0 && fused_;
+    const bool batched = tcBatch && factor == 2.0;
     if (!batched)
     {
         for (int i = 0; i < n; i++)
-            if (!run(ts, src[i], dst[i], factor, s)) return -1;
+            if (!run(ts, src[i], dst[i], factor, s)) return false;
     }
     else
     {
         const bool bf16 = precision_ == Precision::BF16;
         const void* w = tcWeights(precision_, true);
-        if (!w) return fail(ts, "tensor-core weights", cudaErrorMemoryAllocation), -1;
+        if (!w) return fail(ts, "tensor-core weights", cudaErrorMemoryAllocation), false;
         cudaError_t err = ts.counter.ensure(256);
-        if (err != cudaSuccess) return fail(ts, "device allocation", err), -1;
+        if (err != cudaSuccess) return fail(ts, "device allocation", err), false;
         int* counter = static_cast<int*>(ts.counter.ptr);
         Phase2 ph;
-        if (!phase_weights(2, &ph.w[0][0])) return fail(ts, "chroma resample weights"), -1;
+        if (!phase_weights(2, &ph.w[0][0])) return fail(ts, "chroma resample weights"), false;
         const int maxImages = std::min(acnet_tc3_max_images(), 64);
         std::vector<int> order(n);
         for (int i = 0; i < n; i++) order[i] = i;
@@ -906,11 +915,11 @@ int GB300Processor::processBatchDevice(int n, const DeviceImage* src, const Devi
             const Phase2* php = in[0].channels > 1 ? &ph : nullptr;
             bool ran = false;
             const Tc3Plan plan = tc3Plan(m, in, out, php, w, bf16, counter, s, ran, err);
-            if (err != cudaSuccess) return fail(ts, "batched upscale", err), -1;
+            if (err != cudaSuccess) return fail(ts, "batched upscale", err), false;
             mix(static_cast<uint64_t>(plan.shape * 4 + plan.perSm));
             const int ctas = tc3Ctas_ > 0 ? tc3Ctas_ : smCount_;
             cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-            if ((err = cudaStreamIsCapturing(s, &cap)) != cudaSuccess) return fail(ts, "stream state", err), -1;
+            if ((err = cudaStreamIsCapturing(s, &cap)) != cudaSuccess) return fail(ts, "stream state", err), false;
             auto git = ts.graphs.find(sig);
             if (ran)
             {
@@ -918,7 +927,7 @@ int GB300Processor::processBatchDevice(int n, const DeviceImage* src, const Devi
             else if (cap == cudaStreamCaptureStatusNone && git != ts.graphs.end())
             {
                 // the same batch again: replay its graph (memset + persistent kernel)
-                if ((err = cudaGraphLaunch(git->second.exec, s)) != cudaSuccess) return fail(ts, "graph launch", err), -1;
+                if ((err = cudaGraphLaunch(git->second.exec, s)) != cudaSuccess) return fail(ts, "graph launch", err), false;
                 count_launch();
                 g_graph_replays++;
             }
@@ -927,22 +936,22 @@ int GB300Processor::processBatchDevice(int n, const DeviceImage* src, const Devi
                 // second sighting: capture the launch into a graph, then replay it
                 GraphEntry ge;
                 if ((err = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
-                    return fail(ts, "stream capture", err), -1;
+                    return fail(ts, "stream capture", err), false;
                 const cudaError_t lerr = launch_acnet_legacy_tc3(*acnet_, w, bf16, m, in, out, php, counter, ctas, s,
                                                                  plan.shape, plan.perSm);
                 err = cudaStreamEndCapture(s, &ge.graph);
                 if (lerr != cudaSuccess || err != cudaSuccess)
                 {
                     if (ge.graph) cudaGraphDestroy(ge.graph);
-                    return fail(ts, "stream capture", lerr != cudaSuccess ? lerr : err), -1;
+                    return fail(ts, "stream capture", lerr != cudaSuccess ? lerr : err), false;
                 }
                 if ((err = cudaGraphInstantiate(&ge.exec, ge.graph, 0)) != cudaSuccess)
                 {
                     cudaGraphDestroy(ge.graph);
-                    return fail(ts, "graph instantiation", err), -1;
+                    return fail(ts, "graph instantiation", err), false;
                 }
                 ts.graphs[sig] = ge;
-                if ((err = cudaGraphLaunch(ge.exec, s)) != cudaSuccess) return fail(ts, "graph launch", err), -1;
+                if ((err = cudaGraphLaunch(ge.exec, s)) != cudaSuccess) return fail(ts, "graph launch", err), false;
                 g_graph_replays++;
             }
             else
@@ -951,15 +960,122 @@ int GB300Processor::processBatchDevice(int n, const DeviceImage* src, const Devi
                 ts.seen[sig] = 1;
                 if ((err = launch_acnet_legacy_tc3(*acnet_, w, bf16, m, in, out, php, counter, ctas, s, plan.shape,
                                                    plan.perSm)) != cudaSuccess)
-                    return fail(ts, "batched upscale", err), -1;
+                    return fail(ts, "batched upscale", err), false;
             }
             g0 = g1;
         }
     }
+    return true;
+}
+
+int GB300Processor::processBatchDevice(int n, const DeviceImage* src, const DeviceImage* dst, double factor, cudaStream_t stream,
+                                       bool sync)
+{
+    ThreadState& ts = state();
+    if (!begin(ts)) return -1;
+    if (n < 0 || (n > 0 && (!src || !dst))) return fail(ts, "batch: bad image arrays"), -1;
+    cudaStream_t s = stream ? stream : ts.stream;
+    for (int i = 0; i < n; i++)
+    {
+        if (!src[i].ptr || !dst[i].ptr) return fail(ts, "null device pointer"), -1;
+        if (!validate(ts, src[i].w, src[i].h, src[i].c, src[i].type, factor)) return -1;
+        int ow, oh;
+        output_shape(src[i].w, src[i].h, src[i].c, factor, ow, oh);
+        if (src[i].c == 1 && factor / static_cast<double>(1 << (factor > 2.0 ? ceil_log2(factor) : 1)) != 1.0)
+        {
+            ow = dst[i].w;
+            oh = dst[i].h;
+        }
+        if (dst[i].w != ow || dst[i].h != oh || dst[i].c != src[i].c || dst[i].type != src[i].type)
+            return fail(ts, "dst has the wrong shape or type"), -1;
+    }
+    if (!batchRun(ts, n, src, dst, factor, s)) return -1;
     if (sync)
     {
         cudaError_t err = cudaStreamSynchronize(s);
         if (err != cudaSuccess) return fail(ts, "kernel execution", err), -1;
+        if (precision_ != Precision::FP32 && tc_status_reset() != 0) return fail(ts, "tensor-core wait timed out"), -1;
+    }
+    return 0;
+}
+
+int GB300Processor::processYuvDevice(int frames, int planes, const DeviceImage* src, const DeviceImage* dst, double factor,
+                                     int shift, cudaStream_t stream, bool sync)
+{
+    ThreadState& ts = state();
+    if (!begin(ts)) return -1;
+    if (frames < 1 || planes < 1 || planes > 4 || !src || !dst) return fail(ts, "yuv: bad frame arrays"), -1;
+    if (shift < 0 || shift > 15) return fail(ts, "yuv: shift must be in [0, 15]"), -1;
+    cudaStream_t s = stream ? stream : ts.stream;
+    std::vector<DeviceImage> ys(frames), yd(frames);
+    size_t tmpBytes = 0;
+    std::vector<size_t> tmpOff(frames);
+    for (int f = 0; f < frames; f++)
+    {
+        const DeviceImage& y = src[f * planes];
+        const DeviceImage& oy = dst[f * planes];
+        if (!y.ptr || !oy.ptr) return fail(ts, "null device pointer"), -1;
+        if (y.c != 1 || oy.c != 1) return fail(ts, "yuv: plane 0 (Y) must have one channel"), -1;
+        if (!validate(ts, y.w, y.h, 1, y.type, factor)) return -1;
+        int ow, oh;
+        output_shape(y.w, y.h, 1, factor, ow, oh);
+        if (factor / static_cast<double>(1 << (factor > 2.0 ? ceil_log2(factor) : 1)) != 1.0)
+        {
+            ow = oy.w;
+            oh = oy.h;
+        }
+        if (oy.w != ow || oy.h != oh || oy.type != y.type) return fail(ts, "dst Y plane has the wrong shape or type"), -1;
+        if (shift && y.type != Image::UInt8 && y.type != Image::UInt16)
+            return fail(ts, "yuv: a shift needs an integer element type"), -1;
+        for (int p = 1; p < planes; p++)
+        {
+            const DeviceImage& a = src[f * planes + p];
+            const DeviceImage& b = dst[f * planes + p];
+            if (!a.ptr || !b.ptr) return fail(ts, "null device pointer"), -1;
+            if (a.type != y.type || b.type != y.type || a.c != b.c || a.c < 1 || a.c > 4 || a.w <= 0 || a.h <= 0 ||
+                b.w <= 0 || b.h <= 0)
+                return fail(ts, "yuv: chroma planes need Y's element type, 1 to 4 channels and a size"), -1;
+        }
+        ys[f] = y;
+        yd[f] = oy;
+        tmpOff[f] = tmpBytes;
+        const int pitch = align_pitch(y.w * (y.type & 0xff));
+        tmpBytes += (static_cast<size_t>(pitch) * y.h + 255) & ~static_cast<size_t>(255);
+    }
+    cudaError_t err;
+    if (shift > 0)
+    {
+        // shl into temporaries (the caller's source planes stay untouched)
+        if ((err = ts.yuvTmp.ensure(tmpBytes)) != cudaSuccess) return fail(ts, "device allocation", err), -1;
+        for (int f = 0; f < frames; f++)
+        {
+            DeviceImage t = ys[f];
+            t.ptr = static_cast<char*>(ts.yuvTmp.ptr) + tmpOff[f];
+            t.stride = align_pitch(t.w * (t.type & 0xff));
+            if ((err = launch_shift(plane_of(ys[f]), plane_of(t), shift, s)) != cudaSuccess) return fail(ts, "shl", err), -1;
+            ys[f] = t;
+        }
+    }
+    if (!batchRun(ts, frames, ys.data(), yd.data(), factor, s)) return -1;
+    for (int f = 0; f < frames; f++)
+    {
+        if (shift > 0 && (err = launch_shift(plane_of(yd[f]), plane_of(yd[f]), -shift, s)) != cudaSuccess)
+            return fail(ts, "shr", err), -1;
+        for (int p = 1; p < planes; p++)
+        {
+            const DeviceImage& a = src[f * planes + p];
+            const DeviceImage& b = dst[f * planes + p];
+            const ResizeAxis* ax = axis(ts, a.w, b.w, 1, s, err);
+            if (!ax) return fail(ts, "resize table", err), -1;
+            const ResizeAxis* ay = axis(ts, a.h, b.h, 1, s, err);
+            if (!ay) return fail(ts, "resize table", err), -1;
+            if ((err = launch_resize(plane_of(a), plane_of(b), *ax, *ay, s)) != cudaSuccess)
+                return fail(ts, "chroma resize", err), -1;
+        }
+    }
+    if (sync)
+    {
+        if ((err = cudaStreamSynchronize(s)) != cudaSuccess) return fail(ts, "kernel execution", err), -1;
         if (precision_ != Precision::FP32 && tc_status_reset() != 0) return fail(ts, "tensor-core wait timed out"), -1;
     }
     return 0;

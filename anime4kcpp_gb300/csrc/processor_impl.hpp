@@ -53,6 +53,13 @@ public:
     // graph); anything else runs image by image.  Returns 0 or -1.
     int processBatchDevice(int n, const DeviceImage* src, const DeviceImage* dst, double factor, cudaStream_t stream, bool sync);
 
+    // The reference CLI's video recipe over `frames` planar frames of
+    // `planes` planes (src[f * planes + p]): Y shifted left by `shift`,
+    // upscaled (batched over the frames) and shifted back; the other planes
+    // resized to their dst sizes with Catmull-Rom.  Returns 0 or -1.
+    int processYuvDevice(int frames, int planes, const DeviceImage* src, const DeviceImage* dst, double factor, int shift,
+                         cudaStream_t stream, bool sync);
+
     // Allocation-free x2 of n device images in one persistent tensor-core
     // launch on `stream` (ACNetLegacy, FP16/BF16 form).  Returns 0, -1 when
     // the work failed, -2 when the request was rejected.
@@ -96,6 +103,8 @@ private:
         DeviceBuffer src, y, uv, la, lb, out;
         DeviceBuffer maps[4];  // ARNet feature maps
         DeviceBuffer counter;  // tile-queue counter of the persistent kernel
+        DeviceBuffer batchTmp; // x2 intermediates of batched x4 passes
+        DeviceBuffer yuvTmp;   // shifted Y planes of the YUV path
         std::map<std::tuple<int, int, int>, AxisTable> tables;
         bool ok = true;
         std::string err = "NO ERROR";
@@ -120,6 +129,7 @@ private:
     // per batch class (element type, channels, form, log2 of the total and
     // mean image sizes) over every shape x {2, 1} CTAs per SM.  When it
     // measured, the launches already produced the output (`ran`).
+    bool batchRun(ThreadState& ts, int n, const DeviceImage* src, const DeviceImage* dst, double factor, cudaStream_t s);
     Tc3Plan tc3Plan(int n, const Plane* in, const Plane* out, const Phase2* ph, const void* w, bool bf16, int* counter,
                     cudaStream_t stream, bool& ran, cudaError_t& err);
 

@@ -65,6 +65,20 @@ AC_C_API int ac_gb300_process_batch_device(ACProcessor* processor, int count, co
 /* Number of batched launches this process has run as CUDA graph replays. */
 AC_C_API uint64_t ac_gb300_graph_replays(void);
 
+/* The reference CLI's video recipe (cli/src/Main.cpp:183-206) on planar
+ * frames in device memory, `frames` frames of `planes` planes each, indexed
+ * src[f * planes + p]: plane 0 (Y, one channel) is shifted left by `shift`
+ * bits (ac::core::shl, core/src/ImageProcess.cpp:601-608), upscaled by
+ * `factor` through the network and shifted back (shr, :609-616) into dst
+ * plane 0; every further plane (U and V, or interleaved UV) is resized to its
+ * dst plane's size with Catmull-Rom, as ac::core::resize(src, dst, 0, 0).
+ * The source planes are not modified.  The Y planes of all frames run as one
+ * batch (ac_gb300_process_batch_device; an ACNetLegacy x4 in a tensor-core
+ * form as two chained batched x2 passes).  Returns AC_SUCCESS or
+ * AC_ERROR(AC_EPROCESSOR) / AC_ERROR(AC_EINVAL). */
+AC_C_API int ac_gb300_process_yuv_device(ACProcessor* processor, int frames, int planes, const ACGB300DeviceImage* src,
+                                         const ACGB300DeviceImage* dst, double factor, int shift, void* stream, int sync);
+
 /* Allocation-free x2 upscale of `count` device images in ONE persistent
  * tensor-core launch.  No reference counterpart: the reference's processors
  * allocate their work buffers inside each call.  It is for callers that must

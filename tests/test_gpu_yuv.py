@@ -1,0 +1,112 @@
+"""Planar YUV frames through the device path: the reference CLI's video
+recipe (cli/src/Main.cpp:183-206) -- Y shifted left, upscaled, shifted back;
+chroma planes resized to their destination size with Catmull-Rom -- checked
+against the oracle, and the batched x4 luma chain against the per-image path
+(GPU required)."""
+import numpy as np
+import pytest
+
+import anime4kcpp_gb300 as ac
+import oracle
+from anime4kcpp_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from anime4kcpp_gb300 import build
+    build.build()
+    oracle.build()
+
+
+def _frame10(h, w, seed):
+    """10-bit 4:2:0 planes stored LSB-aligned in u16."""
+    y = synthetic.luma(h, w, np.uint16, seed=seed, noise=4.0, bits=10)
+    u = synthetic.luma(h // 2, w // 2, np.uint16, seed=seed + 1, noise=4.0, bits=10)
+    v = synthetic.luma(h // 2, w // 2, np.uint16, seed=seed + 2, noise=4.0, bits=10)
+    return y, u, v
+
+
+def _dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _run(p, frames, factor, shift):
+    f = int(factor)
+    src = [tuple(_dev(pl) for pl in fr) for fr in frames]
+    outs = [tuple(torch.empty((f * pl.shape[0], f * pl.shape[1]) + tuple(pl.shape[2:]), dtype=pl.dtype, device="cuda")
+                  for pl in fr) for fr in src]
+    p.process_yuv_device(src, outs, factor, shift)
+    return [tuple(o.cpu().numpy() for o in fr) for fr in outs]
+
+
+def _oracle_frame(fr, factor, model, shift):
+    y, planes = fr[0], fr[1:]
+    ys = (y.astype(np.uint32) << shift).astype(np.uint16)
+    oy = oracle.process(ys, factor, model) >> shift
+    oc = [oracle.resize(pl, int(factor) * pl.shape[1], int(factor) * pl.shape[0], oracle.RESIZE_CATMULL_ROM) for pl in planes]
+    return [oy] + oc
+
+
+@pytest.mark.parametrize("model,factor", [("arnet-b8", 4.0), ("acnet-legacy-hdn0", 2.0)])
+def test_yuv420_10bit_fp32_vs_oracle(model, factor):
+    frames = [_frame10(68, 120, seed=5), _frame10(34, 46, seed=9)]
+    p = ac.Processor("cuda", 0, model, precision="fp32")
+    got = _run(p, frames, factor, 6)
+    for fr, g in zip(frames, got):
+        want = _oracle_frame(fr, factor, model, 6)
+        d = np.abs(g[0].astype(int) - want[0].astype(int))
+        assert d.max() <= 1
+        for gc, wc in zip(g[1:], want[1:]):
+            assert np.array_equal(gc, wc)
+
+
+def test_yuv_nv12_fp16_batch_of_frames():
+    """Y plus an interleaved UV plane, eight frames in one call, FP16 form."""
+    frames = []
+    for i in range(8):
+        y, u, v = _frame10(90, 160, seed=20 + i)
+        frames.append((y, np.ascontiguousarray(np.stack([u, v], axis=2))))
+    p = ac.Processor("cuda", 0, "acnet-legacy-hdn0", precision="fp16")
+    got = _run(p, frames, 2.0, 6)
+    for fr, g in zip(frames, got):
+        want = _oracle_frame(fr, 2.0, "acnet-legacy-hdn0", 6)
+        d = np.abs(g[0].astype(int) - want[0].astype(int))
+        assert (d <= 1).mean() >= 0.99 and d.max() <= 8
+        assert np.array_equal(g[1], want[1])
+
+
+def test_batched_x4_chain_equals_per_image():
+    imgs = [synthetic.luma(h, w, np.uint16, seed=h + w) for h, w in ((70, 97), (128, 64), (45, 1))]
+    p = ac.Processor("cuda", 0, "acnet-legacy-hdn3", precision="fp16")
+    srcs = [_dev(x) for x in imgs]
+    want = []
+    dsts = []
+    for s in srcs:
+        d = torch.empty((4 * s.shape[0], 4 * s.shape[1]), dtype=s.dtype, device="cuda")
+        p.process_device(s, d, 4.0)
+        want.append(d.cpu().numpy())
+        dsts.append(torch.empty_like(d))
+    for call in range(2):
+        launches = ac.launch_count()
+        p.process_batch_device(srcs, dsts, 4.0)
+        if call == 1:  # the first call also measured the plans of both passes
+            assert ac.launch_count() - launches == 2  # two batched x2 passes
+        for d, w in zip(dsts, want):
+            assert np.array_equal(d.cpu().numpy(), w)
+
+
+def test_yuv_rejects_bad_planes():
+    y = _dev(synthetic.luma(32, 32, np.uint16, seed=1))
+    uv = _dev(synthetic.luma(16, 16, np.uint16, seed=2))
+    p = ac.Processor("cuda", 0, "acnet-legacy-hdn0", precision="fp16")
+    rgb = _dev(synthetic.rgb_u8(32, 32, seed=3))
+    with pytest.raises(RuntimeError, match="one channel"):
+        p.process_yuv_device([(rgb, uv)], [(torch.empty((64, 64, 3), dtype=torch.uint8, device="cuda"),
+                                            torch.empty((32, 32), dtype=torch.uint16, device="cuda"))], 2.0, 0)
+    f32 = _dev(synthetic.f32_luma_uniform(32, 32, seed=4))
+    with pytest.raises(RuntimeError, match="shift"):
+        p.process_yuv_device([(f32,)], [(torch.empty((64, 64), dtype=torch.float32, device="cuda"),)], 2.0, 6)
+    del y
