@@ -48,6 +48,26 @@ class ACGB300DeviceImage(ctypes.Structure):
                 ("channels", ctypes.c_int), ("stride", ctypes.c_int), ("element_type", ctypes.c_int)]
 
 
+class ACGB300HostPlane(ctypes.Structure):
+    _fields_ = [("ptr", ctypes.c_void_p), ("width", ctypes.c_int), ("height", ctypes.c_int), ("channels", ctypes.c_int),
+                ("stride", ctypes.c_int), ("element_type", ctypes.c_int)]
+
+
+class ACGB300ServeJob(ctypes.Structure):
+    _fields_ = [("model", ctypes.c_char_p), ("factor", ctypes.c_double), ("planes", ctypes.c_int), ("shift", ctypes.c_int),
+                ("src", ACGB300HostPlane * 3), ("dst", ACGB300HostPlane * 3)]
+
+
+class ACGB300ServeResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("queue_ms", ctypes.c_double), ("device_ms", ctypes.c_double),
+                ("latency_ms", ctypes.c_double), ("batch", ctypes.c_int), ("error", ctypes.c_char * 160)]
+
+
+class ACGB300ServeStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "completed", "failed", "batches", "batched_jobs")] + \
+               [(n, ctypes.c_double) for n in ("budget_bytes", "in_use_bytes", "peak_bytes", "pool_bytes")]
+
+
 # Every symbol of include/ac_image.h, include/ac_processor.h and include/ac_gb300.h.
 EXPORTS = (
     "ac_image_alloc", "ac_image_free", "ac_image_ref", "ac_image_unref", "ac_image_create", "ac_image_map",
@@ -60,6 +80,8 @@ EXPORTS = (
     "ac_gb300_launch_count", "ac_gb300_model_params", "ac_gb300_profile_enable", "ac_gb300_profile_collect",
     "ac_gb300_tc_selftest", "ac_gb300_process_device_noalloc", "ac_gb300_process_batch_device",
     "ac_gb300_graph_replays", "ac_gb300_process_yuv_device",
+    "ac_gb300_server_create", "ac_gb300_server_error", "ac_gb300_server_submit", "ac_gb300_server_wait",
+    "ac_gb300_server_stats", "ac_gb300_server_destroy",
 )
 
 _lock = threading.Lock()
@@ -98,6 +120,12 @@ def native():
             "ac_gb300_process_batch_device": (I, [pproc, I, P(ACGB300DeviceImage), P(ACGB300DeviceImage), D, V, I]),
             "ac_gb300_graph_replays": (ctypes.c_uint64, []),
             "ac_gb300_process_yuv_device": (I, [pproc, I, I, P(ACGB300DeviceImage), P(ACGB300DeviceImage), D, I, V, I]),
+            "ac_gb300_server_create": (V, [I, I, D, I, I]),
+            "ac_gb300_server_error": (ctypes.c_char_p, [V]),
+            "ac_gb300_server_submit": (I, [V, P(ACGB300ServeJob), P(ctypes.c_uint64)]),
+            "ac_gb300_server_wait": (I, [V, ctypes.c_uint64, D, P(ACGB300ServeResult)]),
+            "ac_gb300_server_stats": (I, [V, P(ACGB300ServeStats)]),
+            "ac_gb300_server_destroy": (None, [V]),
             "ac_gb300_launch_count": (ctypes.c_uint64, []),
             "ac_gb300_model_params": (I, [ctypes.c_char_p, V, I, V, I, V, I, P(I)]),
             "ac_gb300_profile_enable": (I, [pproc, I]),
@@ -286,6 +314,84 @@ class Processor:
         return ms.value, n.value, px.value
 
     InfoList = property(lambda self: (native().ac_processor_info(0).decode(), native().ac_processor_info(2).decode()))
+
+
+class Server:
+    """The serving loop (``ac_gb300_server_*``): jobs of mixed resolutions,
+    factors, models and formats admitted by an HBM budget, batched as they
+    arrive and overlapped on the device.  Host arrays given to ``submit`` are
+    kept alive here until ``wait`` returns their job."""
+
+    def __init__(self, device=0, precision="fp16", hbm_budget_gb=80.0, workers=4, max_batch=64):
+        p = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        self._s = native().ac_gb300_server_create(int(device), p, float(hbm_budget_gb) * 1e9, int(workers), int(max_batch))
+        if not self._s:
+            raise MemoryError("ac_gb300_server_create")
+        err = native().ac_gb300_server_error(self._s)
+        if err:
+            self.close()
+            raise RuntimeError(err.decode())
+        self._keep = {}
+
+    @staticmethod
+    def _plane(a):
+        pl = ACGB300HostPlane()
+        pl.ptr = a.ctypes.data
+        pl.height, pl.width = a.shape[0], a.shape[1]
+        pl.channels = 1 if a.ndim == 2 else a.shape[2]
+        pl.stride = a.strides[0]
+        pl.element_type = _TYPE_OF[np.dtype(a.dtype)]
+        return pl
+
+    def submit(self, src, dst, model, factor=2.0, shift=0):
+        """``src``/``dst``: a numpy array (one interleaved image) or a tuple of
+        planes (planar YUV, Y first).  Returns a ticket."""
+        src = src if isinstance(src, (tuple, list)) else (src,)
+        dst = dst if isinstance(dst, (tuple, list)) else (dst,)
+        if len(src) != len(dst) or not 1 <= len(src) <= 3:
+            raise ValueError("src and dst need the same number of planes (1 to 3)")
+        for a in tuple(src) + tuple(dst):
+            if a.strides[-1] != a.itemsize or (a.ndim == 3 and a.strides[1] != a.itemsize * a.shape[2]):
+                raise ValueError("planes need contiguous rows")
+        job = ACGB300ServeJob()
+        mb = model.encode()
+        job.model, job.factor, job.planes, job.shift = mb, float(factor), len(src), int(shift)
+        for i, a in enumerate(src):
+            job.src[i] = self._plane(a)
+        for i, a in enumerate(dst):
+            job.dst[i] = self._plane(a)
+        t = ctypes.c_uint64()
+        if native().ac_gb300_server_submit(self._s, ctypes.byref(job), ctypes.byref(t)) != AC_SUCCESS:
+            raise RuntimeError("submit failed")
+        self._keep[t.value] = (src, dst)
+        return t.value
+
+    def wait(self, ticket, timeout=120.0):
+        r = ACGB300ServeResult()
+        rc = native().ac_gb300_server_wait(self._s, ctypes.c_uint64(ticket), float(timeout), ctypes.byref(r))
+        if rc == 1:
+            raise TimeoutError("job %d not done after %.1f s" % (ticket, timeout))
+        if rc != AC_SUCCESS:
+            raise RuntimeError("wait failed")
+        self._keep.pop(ticket, None)
+        return {"status": r.status, "queue_ms": r.queue_ms, "device_ms": r.device_ms, "latency_ms": r.latency_ms,
+                "batch": r.batch, "error": r.error.decode()}
+
+    def stats(self):
+        st = ACGB300ServeStats()
+        native().ac_gb300_server_stats(self._s, ctypes.byref(st))
+        return {n: getattr(st, n) for n, _ in ACGB300ServeStats._fields_}
+
+    def close(self):
+        if getattr(self, "_s", None):
+            native().ac_gb300_server_destroy(self._s)
+            self._s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def graph_replays():

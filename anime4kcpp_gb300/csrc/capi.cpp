@@ -1,5 +1,6 @@
 // The C ABI: the reference binding's entry points (binding/c/src/Binding.cpp)
 // over this backend's Image and Processor, plus the GB300 extensions.
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
@@ -9,6 +10,7 @@
 #include "ac_core.h"
 #include "ac_gb300.h"
 #include "processor_impl.hpp"
+#include "server.hpp"
 
 struct ACImageHandle
 {
@@ -433,3 +435,82 @@ int ac_gb300_model_params(const char* model, float* kernels, int kernels_len, fl
     }
     return AC_SUCCESS;
 }
+
+// ---- serving loop ----
+
+struct ACGB300Server
+{
+    std::unique_ptr<acgb::Server> server;
+};
+
+static acgb::HostPlane host_plane(const ACGB300HostPlane& p)
+{
+    return acgb::HostPlane{p.ptr, p.width, p.height, p.channels, p.stride, p.element_type};
+}
+
+ACGB300Server* ac_gb300_server_create(int device, int precision, double hbm_budget_bytes, int workers, int max_batch)
+{
+    auto* s = new (std::nothrow) ACGB300Server;
+    if (!s) return nullptr;
+    const acgb::Precision p = precision == AC_GB300_BF16 ? acgb::Precision::BF16
+                              : precision == AC_GB300_FP16 ? acgb::Precision::FP16
+                                                           : acgb::Precision::FP32;
+    const size_t budget = hbm_budget_bytes > 0.0 ? static_cast<size_t>(hbm_budget_bytes) : 0;
+    s->server.reset(new (std::nothrow) acgb::Server(device, p, budget, workers, max_batch));
+    return s;
+}
+
+const char* ac_gb300_server_error(const ACGB300Server* server)
+{
+    if (!server || !server->server) return "no server";
+    return server->server->initError().empty() ? nullptr : server->server->initError().c_str();
+}
+
+int ac_gb300_server_submit(ACGB300Server* server, const ACGB300ServeJob* job, uint64_t* ticket)
+{
+    if (!server || !server->server || !job || !job->model || !ticket) return AC_ERROR(AC_EINVAL);
+    acgb::ServeJob j;
+    j.model = job->model;
+    j.factor = job->factor;
+    j.planes = job->planes;
+    j.shift = job->shift;
+    for (int i = 0; i < 3; i++)
+    {
+        j.src[i] = host_plane(job->src[i]);
+        j.dst[i] = host_plane(job->dst[i]);
+    }
+    *ticket = server->server->submit(j);
+    return AC_SUCCESS;
+}
+
+int ac_gb300_server_wait(ACGB300Server* server, uint64_t ticket, double timeout_s, ACGB300ServeResult* result)
+{
+    if (!server || !server->server || !result) return AC_ERROR(AC_EINVAL);
+    acgb::ServeResult r;
+    if (!server->server->wait(ticket, timeout_s, r)) return 1;
+    result->status = r.status;
+    result->queue_ms = r.queueMs;
+    result->device_ms = r.deviceMs;
+    result->latency_ms = r.latencyMs;
+    result->batch = r.batch;
+    std::snprintf(result->error, sizeof(result->error), "%s", r.error.c_str());
+    return AC_SUCCESS;
+}
+
+int ac_gb300_server_stats(ACGB300Server* server, ACGB300ServeStats* stats)
+{
+    if (!server || !server->server || !stats) return AC_ERROR(AC_EINVAL);
+    const acgb::ServeStats s = server->server->stats();
+    stats->submitted = s.submitted;
+    stats->completed = s.completed;
+    stats->failed = s.failed;
+    stats->batches = s.batches;
+    stats->batched_jobs = s.batchedJobs;
+    stats->budget_bytes = s.budgetBytes;
+    stats->in_use_bytes = s.inUseBytes;
+    stats->peak_bytes = s.peakBytes;
+    stats->pool_bytes = s.poolBytes;
+    return AC_SUCCESS;
+}
+
+void ac_gb300_server_destroy(ACGB300Server* server) { delete server; }

@@ -132,4 +132,66 @@ AC_C_API uint64_t ac_gb300_launch_count(void);
 AC_C_API int ac_gb300_model_params(const char* model, float* kernels, int kernels_len, float* biases, int biases_len,
                                    float* alphas, int alphas_len, int* counts);
 
+/* ---- Serving loop (no reference counterpart: the reference serves one
+ * image per Processor::process call).  A server admits upscale jobs of mixed
+ * resolutions, factors, models and formats by an HBM budget, keeps weights
+ * and frame buffers resident on the device, batches compatible jobs as they
+ * arrive (ACNetLegacy x2 of interleaved images in a tensor-core form: one
+ * persistent launch) and overlaps the work of different jobs through
+ * `workers` streams.  A job's result is the same as ac_processor_process
+ * gives for it alone. */
+typedef struct ACGB300HostPlane
+{
+    void* ptr; /* host memory; pinned memory lets the copies overlap */
+    int width;
+    int height;
+    int channels;
+    int stride;
+    int element_type;
+} ACGB300HostPlane;
+
+typedef struct ACGB300ServeJob
+{
+    const char* model; /* as for ac_processor_create (read during submit) */
+    double factor;
+    int planes; /* 1: one interleaved image (1, 3 or 4 channels); 2 or 3: planar YUV, Y first */
+    int shift;  /* planar YUV: shl / shr bits of Y (ac_gb300_process_yuv_device) */
+    ACGB300HostPlane src[3];
+    ACGB300HostPlane dst[3]; /* src and dst must stay valid until the job is waited for */
+} ACGB300ServeJob;
+
+typedef struct ACGB300ServeResult
+{
+    int status;        /* 0 done, -1 failed, -2 rejected (malformed, or larger than the budget) */
+    double queue_ms;   /* submit -> admitted */
+    double device_ms;  /* first copy issued -> result in dst */
+    double latency_ms; /* submit -> result in dst */
+    int batch;         /* jobs that shared this job's launch */
+    char error[160];
+} ACGB300ServeResult;
+
+typedef struct ACGB300ServeStats
+{
+    uint64_t submitted, completed, failed, batches, batched_jobs;
+    double budget_bytes, in_use_bytes, peak_bytes, pool_bytes;
+} ACGB300ServeStats;
+
+typedef struct ACGB300Server ACGB300Server;
+
+/* precision: AC_GB300_FP32 / FP16 / BF16; hbm_budget_bytes caps the device
+ * bytes of admitted jobs (frame buffers plus a conservative estimate of their
+ * work buffers) and of the buffer pool; at most max_batch (<= 64) jobs share
+ * a launch.  Returns NULL only when out of host memory; then check
+ * ac_gb300_server_error. */
+AC_C_API ACGB300Server* ac_gb300_server_create(int device, int precision, double hbm_budget_bytes, int workers, int max_batch);
+/* NULL when the server is usable, else why it is not. */
+AC_C_API const char* ac_gb300_server_error(const ACGB300Server* server);
+AC_C_API int ac_gb300_server_submit(ACGB300Server* server, const ACGB300ServeJob* job, uint64_t* ticket);
+/* AC_SUCCESS once the job finished (its outcome in result->status), 1 when
+ * timeout_s passed first, AC_ERROR(AC_EINVAL) for a bad argument. */
+AC_C_API int ac_gb300_server_wait(ACGB300Server* server, uint64_t ticket, double timeout_s, ACGB300ServeResult* result);
+AC_C_API int ac_gb300_server_stats(ACGB300Server* server, ACGB300ServeStats* stats);
+/* Stops the server; jobs not yet run are dropped. */
+AC_C_API void ac_gb300_server_destroy(ACGB300Server* server);
+
 #endif
