@@ -71,6 +71,10 @@ public:
     int collectProfile(double& ms, int& launches, double& outPixels);
 
     void setPrecision(Precision p) { precision_ = p; }
+    // Off: the persistent kernel runs its default plan instead of measuring
+    // one the first time a batch class is seen (no measurement launches in a
+    // latency-sensitive request path).
+    void setAutotune(bool on) { autotune_ = on; }
     Precision precision() const { return precision_; }
     int device() const { return device_; }
     const ModelSpec& spec() const { return spec_; }

@@ -5,11 +5,15 @@
 // order, letting smaller later jobs past a job that does not fit yet unless
 // that job has waited 50 ms) and gives them device frame buffers from a
 // resident pool; each worker thread owns a CUDA stream and takes the next
-// ready job together with every other ready job it can batch with
+// ready job it serves together with every other ready job it can batch with
 // (ACNetLegacy x2 of interleaved images in a tensor-core form, same model,
 // channel count and element type), copies the inputs in, runs one launch for
 // the batch, copies the results out and synchronises its stream.  Several
-// workers keep several jobs' copies and kernels in flight at once.
+// workers keep several jobs' copies and kernels in flight at once.  Half of
+// the workers ("express") serve only small jobs (up to a 1080p x2 ACNetLegacy
+// job's output) on high-priority streams, so a small job's blocks are
+// scheduled ahead of the pending blocks of large jobs; the other workers take
+// large jobs first and small ones when no large job waits.
 #include "server.hpp"
 
 #include <algorithm>
@@ -47,10 +51,13 @@ Server::Server(int device, Precision precision, size_t budget, int workers, int 
         return;
     }
     workers = std::max(1, std::min(workers, 16));
+    express_ = workers / 2;
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) least = greatest = 0;
     for (int w = 0; w < workers; w++)
     {
         cudaStream_t s = nullptr;
-        if ((err = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess)
+        if ((err = cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, w < express_ ? greatest : least)) != cudaSuccess)
         {
             initError_ = std::string("cudaStreamCreate: ") + cudaGetErrorString(err);
             break;
@@ -98,6 +105,7 @@ GB300Processor* Server::processorFor(const std::string& model, std::string& err)
             return nullptr;
         }
         g->setPrecision(precision_);
+        g->setAutotune(false);  // the default tile plan: no measurement launches in the request path
         it = procs_.emplace(model, p).first;
     }
     return static_cast<GB300Processor*>(it->second.get());
@@ -159,6 +167,8 @@ bool Server::check(Job& j, std::string& err)
     }
     j.bytes = io + static_cast<size_t>(ws);
     j.batchable = fused && precision_ != Precision::FP32;
+    const double outPx = static_cast<double>(s.dst[0].w) * s.dst[0].h;  // the (luma) frame
+    j.express = spec.family == Family::ACNetLegacy ? outPx <= 1.3 * 3840.0 * 2160.0 : outPx <= 1.3 * 1708.0 * 960.0;
     j.batchKey = s.model + "/" + std::to_string(y.c) + "/" + std::to_string(y.type);
     return true;
 }
@@ -354,7 +364,7 @@ void Server::admitLoop()
             }
             std::lock_guard<std::mutex> lock(m_);
             ready_.push_back(std::move(j));
-            cvWork_.notify_one();
+            cvWork_.notify_all();  // the workers differ in which jobs they take
         }
     }
 }
@@ -368,10 +378,23 @@ void Server::workerLoop(int w)
         std::vector<std::unique_ptr<Job>> batch;
         {
             std::unique_lock<std::mutex> lock(m_);
-            cvWork_.wait(lock, [&] { return stop_ || !ready_.empty(); });
+            // express workers take small jobs only; the others large jobs first
+            const bool express = w < express_;
+            auto pick = [&]() {
+                auto it = ready_.begin();
+                if (express)
+                {
+                    while (it != ready_.end() && !(*it)->express) ++it;
+                    return it;
+                }
+                auto big = std::find_if(ready_.begin(), ready_.end(), [](const std::unique_ptr<Job>& j) { return !j->express; });
+                return big != ready_.end() ? big : ready_.begin();
+            };
+            cvWork_.wait(lock, [&] { return stop_ || pick() != ready_.end(); });
             if (stop_) return;
-            batch.push_back(std::move(ready_.front()));
-            ready_.pop_front();
+            auto first = pick();
+            batch.push_back(std::move(*first));
+            ready_.erase(first);
             if (batch[0]->batchable)
                 for (auto it = ready_.begin(); it != ready_.end() && static_cast<int>(batch.size()) < maxBatch_;)
                 {

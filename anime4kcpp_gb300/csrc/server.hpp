@@ -83,6 +83,7 @@ private:
         ServeJob job;
         size_t bytes = 0;  // admission charge
         bool batchable = false;
+        bool express = false;  // small job: served by the high-priority workers
         std::string batchKey;
         double tSubmit = 0.0, tAdmit = 0.0, tStart = 0.0;
         Block blocks[6];  // src planes then dst planes
@@ -125,6 +126,7 @@ private:
     size_t poolBytes_ = 0;               // cached + handed out
 
     std::vector<cudaStream_t> streams_;  // one per worker
+    int express_ = 0;                    // workers 0 .. express_-1 serve small jobs on high-priority streams
     std::thread admitter_;
     std::vector<std::thread> workers_;
 };

@@ -19,6 +19,10 @@ Voronoi-edge images (no public dataset is attached to this workload).
          persistent launch per step (autotuned tile shape, CUDA-graph replay)
          against FP32 per-image launches
 
+  serve  the serving workload: Poisson arrivals (200 jobs/s) of mixed sizes,
+         factors, models and formats through the serving loop; p50/p99
+         latency and output Mpx/s, FP16 against FP32
+
 --impl reference times the reference CPU path instead (the reference CPU
 processor built from its sources where available, else the project's C
 restatement of it) on the host cores, one frame per step.
@@ -324,6 +328,171 @@ def time_batch(ac, torch, args):
     return res
 
 
+SERVE_RES = [(480, 854), (720, 1280), (1080, 1920), (2160, 3840)]
+SERVE_RES_W = [1, 2, 2, 1]
+SERVE_MODELS = ["acnet-legacy-hdn0", "acnet-legacy-hdn1", "acnet-legacy-hdn2", "acnet-legacy-hdn3", "arnet-b8"]
+
+
+def time_serve(ac, torch, args, forms=("fp16", "fp32")):
+    """The serving workload: an open-loop Poisson stream of upscale jobs at
+    `args.serve_rate` jobs/s for `args.serve_seconds` s through the serving
+    loop (ac.Server, 80 GB HBM budget, 4 worker streams).  Sizes 854x480,
+    1280x720, 1920x1080, 3840x2160 in ratio 1:2:2:1; factor 2 or 4 in ratio
+    3:1; models ACNetLegacy HDN0-3 and ARNet B8 chosen uniformly; formats RGB
+    u8 or 10-bit YUV 4:2:0 u16 (planar, shift 6) in ratio 4:1.  Latency =
+    submit -> result in the caller's pinned host buffer."""
+    import queue
+    from anime4kcpp_gb300 import synthetic
+    rng = np.random.default_rng(7)
+    canvas = synthetic.rgb_u8(2160, 3840, cells=256, seed=70)
+    luma = synthetic.luma(2160, 3840, np.uint16, cells=256, seed=71, noise=4.0, bits=10)
+    chroma = [synthetic.luma(1080, 1920, np.uint16, cells=256, seed=72 + k, noise=4.0, bits=10) for k in range(2)]
+
+    def pinned(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+
+    inputs = {}
+    for ri, (h, w) in enumerate(SERVE_RES):
+        inputs[(ri, "rgb")] = pinned(canvas[:h, :w])
+        inputs[(ri, "yuv")] = (pinned(luma[:h, :w]), pinned(chroma[0][:h // 2, :w // 2]), pinned(chroma[1][:h // 2, :w // 2]))
+    rings, free = {}, {}
+    for ri, (h, w) in enumerate(SERVE_RES):
+        for f in (2, 4):
+            n = 3 if (ri == 3 and f == 4) else 10
+            rings[(ri, f, "rgb")] = [pinned(np.empty((f * h, f * w, 3), np.uint8)) for _ in range(n)]
+            rings[(ri, f, "yuv")] = [(pinned(np.empty((f * h, f * w), np.uint16)),
+                                      pinned(np.empty((f * h // 2, f * w // 2), np.uint16)),
+                                      pinned(np.empty((f * h // 2, f * w // 2), np.uint16))) for _ in range(n)]
+    for k, v in rings.items():
+        free[k] = queue.Queue()
+        for i in range(len(v)):
+            free[k].put(i)
+
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, size=int(args.serve_rate * args.serve_seconds * 1.5) + 10))
+    arrivals = arrivals[arrivals < args.serve_seconds]
+    picks = [(int(rng.choice(4, p=np.array(SERVE_RES_W) / 6.0)), 2 if rng.random() < 0.75 else 4,
+              SERVE_MODELS[int(rng.integers(0, 5))], "rgb" if rng.random() < 0.8 else "yuv") for _ in arrivals]
+    out = {"workload": "Poisson %.0f jobs/s for %.0f s; 480p:720p:1080p:2160p = 1:2:2:1; x2:x4 = 3:1; "
+                       "ACNetLegacy HDN0-3 / ARNet-B8 uniform; RGB u8 : 10-bit YUV420 u16 = 4:1; 80 GB budget, "
+                       "4 worker streams" % (args.serve_rate, args.serve_seconds),
+           "jobs": len(arrivals)}
+    for form in forms:
+        srv = ac.Server(0, form, hbm_budget_gb=80.0, workers=4)
+        # warm-up: every model, format and factor once (processors, weights)
+        warm = []
+        for m in SERVE_MODELS:
+            for fmt in ("rgb", "yuv"):
+                for f in (2, 4):
+                    slot = free[(0, f, fmt)].get()
+                    warm.append((srv.submit(inputs[(0, fmt)], rings[(0, f, fmt)][slot], m, float(f), 6 if fmt == "yuv" else 0),
+                                 (0, f, fmt), slot))
+        for t, key, slot in warm:
+            srv.wait(t)
+            free[key].put(slot)
+        done = queue.Queue()
+        tickets = queue.Queue()
+        stalls = [0]
+
+        def collect():
+            while True:
+                item = tickets.get()
+                if item is None:
+                    return
+                t, key, slot, meta = item
+                r = srv.wait(t, timeout=600.0)
+                free[key].put(slot)
+                done.put((r, meta))
+
+        collectors = [threading.Thread(target=collect, daemon=True) for _ in range(8)]
+        [c.start() for c in collectors]
+        t0 = time.perf_counter()
+        for at, (ri, f, m, fmt) in zip(arrivals, picks):
+            delay = t0 + at - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            key = (ri, f, fmt)
+            try:
+                slot = free[key].get_nowait()
+            except queue.Empty:
+                stalls[0] += 1
+                slot = free[key].get()
+            h, w = SERVE_RES[ri]
+            t = srv.submit(inputs[(ri, fmt)], rings[key][slot], m, float(f), 6 if fmt == "yuv" else 0)
+            tickets.put((t, key, slot, (ri, f, m, fmt, f * f * h * w)))
+        for _ in collectors:
+            tickets.put(None)
+        [c.join() for c in collectors]
+        wall = time.perf_counter() - t0
+        res = [done.get() for _ in range(done.qsize())]
+        lat = np.array([r["latency_ms"] for r, _ in res])
+        ok = [r for r, _ in res if r["status"] == 0]
+        lat1080 = np.array([r["latency_ms"] for r, m in res if m[0] == 2])
+        lat1080x2 = np.array([r["latency_ms"] for r, m in res if m[0] == 2 and m[1] == 2 and m[3] == "rgb" and "acnet" in m[2]])
+        st = srv.stats()
+        srv.close()
+        out[form] = {
+            "completed": len(ok), "failed": len(res) - len(ok),
+            "out_mpx_per_s": sum(m[4] for r, m in res if r["status"] == 0) / wall / 1e6,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "p50_ms_1080p": float(np.percentile(lat1080, 50)) if len(lat1080) else None,
+            "p99_ms_1080p": float(np.percentile(lat1080, 99)) if len(lat1080) else None,
+            "p99_ms_1080p_acnet_x2_rgb": float(np.percentile(lat1080x2, 99)) if len(lat1080x2) else None,
+            "mean_queue_ms": float(np.mean([r["queue_ms"] for r, _ in res])),
+            "batched_jobs": int(st["batched_jobs"]), "batches": int(st["batches"]),
+            "peak_admitted_gb": st["peak_bytes"] / 1e9, "wall_s": wall, "generator_stalls": stalls[0]}
+    return out
+
+
+def time_serve_saturation(ac, torch, args):
+    """Continuous batching under saturation: 1920x1080 RGB u8 x2 ACNetLegacy
+    HDN0 jobs (FP16) offered at `args.saturation_rate` jobs/s for 2 s through
+    the serving loop; reports the served rate, latency and how many jobs
+    shared launches."""
+    import queue
+    frame = torch.from_numpy(make_frames(1, seed=77)[0]).pin_memory().numpy()
+    ring = [torch.empty((OH, OW, 3), dtype=torch.uint8).pin_memory().numpy() for _ in range(48)]
+    free = queue.Queue()
+    for i in range(len(ring)):
+        free.put(i)
+    srv = ac.Server(0, "fp16", hbm_budget_gb=80.0, workers=4)
+    for _ in range(3):
+        srv.wait(srv.submit(frame, ring[0], MODEL, 2.0))
+    tickets, lats = queue.Queue(), []
+
+    def collect():
+        while True:
+            item = tickets.get()
+            if item is None:
+                return
+            r = srv.wait(item[0], timeout=600.0)
+            free.put(item[1])
+            lats.append((r["latency_ms"], r["batch"], r["status"]))
+
+    cs = [threading.Thread(target=collect, daemon=True) for _ in range(8)]
+    [c.start() for c in cs]
+    n = int(args.saturation_rate * 2.0)
+    t0 = time.perf_counter()
+    for i in range(n):
+        delay = t0 + i / args.saturation_rate - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        slot = free.get()
+        tickets.put((srv.submit(frame, ring[slot], MODEL, 2.0), slot))
+    for _ in cs:
+        tickets.put(None)
+    [c.join() for c in cs]
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    lat = np.array([x[0] for x in lats])
+    return {"workload": "1920x1080 RGB u8 x2 HDN0 FP16 jobs offered at %.0f/s for 2 s (48 pinned output slots)"
+                        % args.saturation_rate,
+            "served_jobs_per_s": n / wall, "out_mpx_per_s": n * OW * OH / wall / 1e6,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_batch": float(np.mean([x[1] for x in lats])), "batched_jobs": int(st["batched_jobs"]),
+            "failed": int(sum(1 for x in lats if x[2] != 0))}
+
+
 def run_gb300(args, rank, world, local_rank):
     import torch
 
@@ -429,6 +598,9 @@ def run_gb300(args, rank, world, local_rank):
     out["clocks"] = clocks
     if rank == 0 and world == 1 and not args.no_batch:
         out["batch"] = time_batch(ac, torch, args)
+    if rank == 0 and world == 1 and args.serve_seconds > 0:
+        out["serve"] = time_serve(ac, torch, args)
+        out["serve"]["saturation"] = time_serve_saturation(ac, torch, args)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     return out
@@ -447,6 +619,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-image batching workload")
     ap.add_argument("--batch-steps", type=int, default=12)
+    ap.add_argument("--serve-seconds", type=float, default=10.0, help="serving workload length per form (0: skip)")
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="serving workload arrival rate, jobs/s")
+    ap.add_argument("--saturation-rate", type=float, default=4000.0, help="offered rate of the saturation run, jobs/s")
     args = ap.parse_args()
     args.forms = [f for f in args.forms.split(",") if f]
     args.warmup = max(args.warmup, 3)
