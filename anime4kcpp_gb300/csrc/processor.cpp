@@ -472,7 +472,9 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
                 if (!w) err = cudaErrorMemoryAllocation;
                 else if ((err = ts.counter.ensure(256)) == cudaSuccess)
                 {
-                    int* counter = static_cast<int*>(ts.counter.ptr);
+                    // 64 counter slots used in turn: launches in flight on
+                    // different streams of one thread get different counters
+                    int* counter = static_cast<int*>(ts.counter.ptr) + (ts.counterSlot++ & 63);
                     bool ran = false;
                     const Tc3Plan plan = tc3Plan(1, &in, &out, ph, w, bf16, counter, stream, ran, err);
                     if (err == cudaSuccess && !ran)
@@ -875,7 +877,7 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
         if (!w) return fail(ts, "tensor-core weights", cudaErrorMemoryAllocation), false;
         cudaError_t err = ts.counter.ensure(256);
         if (err != cudaSuccess) return fail(ts, "device allocation", err), false;
-        int* counter = static_cast<int*>(ts.counter.ptr);
+        int* counter = static_cast<int*>(ts.counter.ptr) + (ts.counterSlot++ & 63);
         Phase2 ph;
         if (!phase_weights(2, &ph.w[0][0])) return fail(ts, "chroma resample weights"), false;
         const int maxImages = std::min(acnet_tc3_max_images(), 64);

@@ -106,7 +106,8 @@ private:
         cudaStream_t stream = nullptr;
         DeviceBuffer src, y, uv, la, lb, out;
         DeviceBuffer maps[4];  // ARNet feature maps
-        DeviceBuffer counter;  // tile-queue counter of the persistent kernel
+        DeviceBuffer counter;  // 64 tile-queue counters of the persistent kernel, used in turn
+        unsigned counterSlot = 0;
         DeviceBuffer batchTmp; // x2 intermediates of batched x4 passes
         DeviceBuffer yuvTmp;   // shifted Y planes of the YUV path
         std::map<std::tuple<int, int, int>, AxisTable> tables;
