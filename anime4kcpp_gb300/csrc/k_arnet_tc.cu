@@ -1,0 +1,451 @@
+// ARNet<8> x2 pass in a tensor-core form (FP16 or BF16 operands, FP32
+// accumulation), one launch per layer.
+//
+// Network and CPU order as k_arnet_fp32.cu (core/include/AC/Core/Model/ARNet.hpp:16-72,
+// core/src/processor/cpu/CPUProcessor.cpp:1464-1491, layer templates
+// core/internal/AC/Core/Internal/Processor/CPU/Common.hpp:116-197,223-342).
+// The first layer (conv 1->8) and the last (conv 8->4 + pixel shuffle +
+// nearest input) stay FP32 on CUDA cores; the 2B 3x3 8->8 convolutions run on
+// tcgen05 as the pair-interleaved implicit GEMM of the ACNetLegacy kernels:
+// one GEMM row = two adjacent pixels (N = 16), K = 3 tap rows x 4 pixels x 8
+// channels read as shifted views of an even/odd plane pair in shared memory,
+// six 128x16x16 MMAs per 128 pairs, accumulators in tensor memory.
+//
+// Between layers the 8-channel maps live in HBM as [h][w][8] 16-bit values
+// (16 bytes per pixel, as the reference's CUDA processor keeps FP16
+// intermediates, Kernel.cu:284-333).  A CTA of 128 threads computes a 62x30
+// tile from a 64x32 window (halo 1, clamped to the map's edge): 2,048 pixels
+// = 1,024 pairs = 8 blocks of 128 GEMM rows in 128 tensor-memory columns, four
+// CTAs per SM.  The epilogue adds the bias in FP32 and applies the layer's
+// ending: PReLU; 0.2 x conv + the block input (residual); or, for the last
+// block, the residual followed by the 1x1 conv 8->8 + PReLU + the head's
+// features.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <vector>
+
+#include "device_common.cuh"
+#include "kernels.hpp"
+#include "tc_ptx.cuh"
+
+namespace acgb {
+namespace arnettc {
+
+constexpr int TW = 62, TH = 30;
+constexpr int WW = TW + 2, WH = TH + 2;  // 64 x 32 window
+constexpr int PPR = WW / 2;
+constexpr int NBLK = WW * WH / 2 / 128;  // 8
+constexpr int PADP = 40;
+constexpr int PLANE_BYTES = (PADP + NBLK * 128 + PADP) * 16;
+constexpr int B_BYTES = 12 * 256;  // one layer's packed weights
+constexpr int THREADS = 128;
+constexpr uint32_t TMEM_COLS = 128;
+constexpr int SMEM = 2 * PLANE_BYTES + B_BYTES + 64;
+// Shared memory requested per CTA: at least a fifth of the SM's, so that at
+// most four CTAs (4 x 128 tensor-memory columns) are resident on an SM.
+constexpr int SMEM_REQ = SMEM > 48 * 1024 ? SMEM : 48 * 1024;
+constexpr uint64_t kWaitNs = 2000000000ull;
+static_assert(WW * WH / 2 == NBLK * 128, "the window is whole pair blocks");
+static_assert(PADP >= PPR + 2, "taps of the first and last rows stay inside the planes");
+
+enum Mode
+{
+    kPReLU = 0,     // prelu(conv + b)
+    kResidual = 1,  // 0.2 * (conv + b) + skip
+    kTail = 2,      // prelu(1x1(0.2 * (conv + b) + skip) + b1) + feat
+};
+
+struct ConvParams
+{
+    const uint4* in;  // [h][w] pixels of 8 16-bit channels
+    uint4* out;
+    const uint4* skip;
+    const uint4* feat;
+    const uint4* bw;  // packed B (12 chunks of 256 bytes)
+    int w, h, tiles_x;
+    float b[8], a[8];
+    float k1[64], b1[8], a1[8];
+    int* status;
+};
+
+template <bool BF16>
+__device__ __forceinline__ void unpack8(const uint4 u, float* v)
+{
+    const uint32_t r[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+    {
+        if constexpr (BF16)
+        {
+            v[2 * i] = __uint_as_float(r[i] << 16);
+            v[2 * i + 1] = __uint_as_float(r[i] & 0xFFFF0000u);
+        }
+        else
+        {
+            const __half2 h = *reinterpret_cast<const __half2*>(&r[i]);
+            const float2 f = __half22float2(h);
+            v[2 * i] = f.x;
+            v[2 * i + 1] = f.y;
+        }
+    }
+}
+
+template <bool BF16>
+__device__ __forceinline__ uint4 pack8(const float* v)
+{
+    if constexpr (BF16)
+        return make_uint4(tc::pack_bf16x2(v[0], v[1]), tc::pack_bf16x2(v[2], v[3]), tc::pack_bf16x2(v[4], v[5]),
+                          tc::pack_bf16x2(v[6], v[7]));
+    else
+        return make_uint4(tc::pack_f16x2(v[0], v[1]), tc::pack_f16x2(v[2], v[3]), tc::pack_f16x2(v[4], v[5]),
+                          tc::pack_f16x2(v[6], v[7]));
+}
+
+__device__ __forceinline__ float prelu(float v, float a) { return fmaxf(v, 0.0f) + a * fminf(v, 0.0f); }
+
+template <int MODE, bool BF16>
+__global__ void __launch_bounds__(THREADS, 4) conv_kernel(const __grid_constant__ ConvParams P)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* plane = smem;  // E plane, then O plane
+    unsigned char* bsm = smem + 2 * PLANE_BYTES;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + 2 * PLANE_BYTES + B_BYTES);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 2 * PLANE_BYTES + B_BYTES + 8);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int x0 = (blockIdx.x % P.tiles_x) * TW - 1, y0 = (blockIdx.x / P.tiles_x) * TH - 1;
+
+    if (tid == 0)
+    {
+        tc::mbar_init(mbar, 1);
+        tc::fence_mbar_init();
+    }
+    if (warp == 0)
+    {
+        tc::tmem_alloc(tmem_slot, TMEM_COLS);
+        tc::tmem_relinquish();
+    }
+    // weights and the 64x32 window (clamped to the map), loads batched per
+    // thread.  The planes' pad slots are zeroed: the first and last valid
+    // rows' MMAs read some of them with a zero weight, and a left-over
+    // non-finite bit pattern would turn 0 x Inf into NaN.
+    for (int i = tid; i < B_BYTES / 16; i += THREADS) reinterpret_cast<uint4*>(bsm)[i] = P.bw[i];
+    for (int i = tid; i < 4 * PADP; i += THREADS)
+    {
+        const int pl = i / (2 * PADP), k = i % (2 * PADP);
+        reinterpret_cast<uint4*>(plane + pl * PLANE_BYTES)[k < PADP ? k : NBLK * 128 + k] = make_uint4(0, 0, 0, 0);
+    }
+    constexpr int PER = WW * WH / THREADS;  // 16
+#pragma unroll
+    for (int k0 = 0; k0 < PER; k0 += 8)
+    {
+        uint4 px[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+        {
+            const int p = tid + (k0 + k) * THREADS;
+            const int wy = p / WW, wx = p - wy * WW;
+            const int gx = clampi(x0 + wx, 0, P.w - 1), gy = clampi(y0 + wy, 0, P.h - 1);
+            px[k] = P.in[static_cast<size_t>(gy) * P.w + gx];
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+        {
+            const int p = tid + (k0 + k) * THREADS;
+            reinterpret_cast<uint4*>(plane + ((p & 1) ? PLANE_BYTES : 0))[PADP + (p >> 1)] = px[k];
+        }
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+
+    if (tid == 0)
+    {
+        constexpr uint32_t IDESC = tc::idesc_f16(128, 16, BF16);
+        const uint64_t a_desc0 = tc::smem_desc(tc::smem_u32(plane) + (PADP - PPR) * 16, PLANE_BYTES - 16, 128);
+        const uint64_t b_desc0 = tc::smem_desc(tc::smem_u32(bsm), 256, 128);
+        for (int b = 0; b < NBLK; b++)
+        {
+            const uint64_t a_desc = a_desc0 + static_cast<uint64_t>(b * 128);
+#pragma unroll
+            for (int dy = 0; dy < 3; dy++)
+#pragma unroll
+                for (int h = 0; h < 2; h++)
+                    tc::mma_f16(tmem + static_cast<uint32_t>(b * 16), a_desc + static_cast<uint64_t>(dy * PPR + h),
+                                b_desc0 + static_cast<uint64_t>((2 * dy + h) * 32), IDESC, (dy | h) ? 1u : 0u);
+        }
+        tc::mma_commit(mbar);
+    }
+    __syncwarp();
+    const bool ok = __syncthreads_and(tc::mbar_wait_ns(mbar, 0, kWaitNs) ? 1 : 0) != 0;
+    tc::fence_after_sync();
+    if (!ok)
+    {
+        if (tid == 0) atomicExch(P.status, 1);
+    }
+    else
+        for (int b = 0; b < NBLK; b++)
+        {
+            float v[16];
+            tc::tmem_ld16(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(b * 16), v);
+            tc::tmem_wait_ld();
+            const int r = b * 128 + warp * 32 + lane;
+#pragma unroll
+            for (int k = 0; k < 2; k++)
+            {
+                const int p = 2 * r + k;
+                const int y = p / WW, x = p - y * WW;
+                const int gx = x0 + x, gy = y0 + y;
+                if (y < 1 || y > TH || x < 1 || x > TW || gx >= P.w || gy >= P.h) continue;
+                const size_t o = static_cast<size_t>(gy) * P.w + gx;
+                float s[8];
+#pragma unroll
+                for (int c = 0; c < 8; c++) s[c] = v[8 * k + c] + P.b[c];
+                if constexpr (MODE == kPReLU)
+                {
+#pragma unroll
+                    for (int c = 0; c < 8; c++) s[c] = prelu(s[c], P.a[c]);
+                }
+                else
+                {
+                    float sk[8];
+                    unpack8<BF16>(P.skip[o], sk);
+#pragma unroll
+                    for (int c = 0; c < 8; c++) s[c] = fmaf(s[c], 0.2f, sk[c]);
+                    if constexpr (MODE == kTail)
+                    {
+                        float f[8], t[8];
+                        unpack8<BF16>(P.feat[o], f);
+#pragma unroll
+                        for (int n = 0; n < 8; n++)
+                        {
+                            float u = P.b1[n];
+#pragma unroll
+                            for (int c = 0; c < 8; c++) u = fmaf(s[c], P.k1[n * 8 + c], u);
+                            t[n] = prelu(u, P.a1[n]) + f[n];
+                        }
+#pragma unroll
+                        for (int n = 0; n < 8; n++) s[n] = t[n];
+                    }
+                }
+                P.out[o] = pack8<BF16>(s);
+            }
+        }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, TMEM_COLS);
+}
+
+struct HeadParams
+{
+    float k[72];
+    float b[8];
+};
+
+// Head: conv3x3 1->8 (identity) in FP32 from the input plane, stored as a
+// 16-bit 8-channel map.  One thread per pixel, taps clamped to the plane.
+template <typename T, bool BF16>
+__global__ void __launch_bounds__(256) head_kernel(Plane in, uint4* __restrict__ feat, const __grid_constant__ HeadParams P)
+{
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= in.w || y >= in.h) return;
+    float t[9];
+#pragma unroll
+    for (int p = 0; p < 9; p++)
+    {
+        const int gy = clampi(y + p / 3 - 1, 0, in.h - 1), gx = clampi(x + p % 3 - 1, 0, in.w - 1);
+        t[p] = to_float<T>(row_ptr<T>(in.ptr, in.pitch, gy)[gx]);
+    }
+    float r[8];
+#pragma unroll
+    for (int n = 0; n < 8; n++)
+    {
+        float v = P.b[n];
+#pragma unroll
+        for (int p = 0; p < 9; p++) v = fmaf(t[p], P.k[n * 9 + p], v);
+        r[n] = v;
+    }
+    feat[static_cast<size_t>(y) * in.w + x] = pack8<BF16>(r);
+}
+
+struct UpParams
+{
+    float k[288];
+    float b[4];
+};
+
+// Upscale: conv3x3 8->4 (identity) in FP32 from the 16-bit map, pixel
+// shuffle 2x2, plus the nearest input pixel, fromFloat (Common.hpp:290-342).
+template <typename T, bool BF16>
+__global__ void __launch_bounds__(256) up_kernel(const uint4* __restrict__ map, Plane src, Plane dst,
+                                                 const __grid_constant__ UpParams U)
+{
+    const int w = src.w, h = src.h;
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= w || y >= h) return;
+    float acc[4];
+#pragma unroll
+    for (int n = 0; n < 4; n++) acc[n] = U.b[n];
+#pragma unroll
+    for (int p = 0; p < 9; p++)
+    {
+        const int gy = clampi(y + p / 3 - 1, 0, h - 1), gx = clampi(x + p % 3 - 1, 0, w - 1);
+        float xv[8];
+        unpack8<BF16>(map[static_cast<size_t>(gy) * w + gx], xv);
+#pragma unroll
+        for (int n = 0; n < 4; n++)
+#pragma unroll
+            for (int c = 0; c < 8; c++) acc[n] = fmaf(xv[c], U.k[n * 72 + p * 8 + c], acc[n]);
+    }
+    const float near = to_float<T>(row_ptr<T>(src.ptr, src.pitch, y)[x]);
+#pragma unroll
+    for (int n = 0; n < 4; n++) row_ptr_w<T>(dst.ptr, dst.pitch, 2 * y + (n >> 1))[2 * x + (n & 1)] = from_float<T>(acc[n] + near);
+}
+
+template <int MODE, bool BF16>
+cudaError_t launch_conv(const ConvParams& p, int tiles, cudaStream_t stream)
+{
+    static bool configured = false;
+    if (!configured)
+    {
+        cudaError_t err = cudaFuncSetAttribute(conv_kernel<MODE, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_REQ);
+        if (err != cudaSuccess) return err;
+        configured = true;
+    }
+    conv_kernel<MODE, BF16><<<tiles, THREADS, SMEM_REQ, stream>>>(p);
+    return cudaGetLastError();
+}
+
+uint16_t to_bits(float v, bool bf16)
+{
+    if (bf16)
+    {
+        uint32_t u;
+        std::memcpy(&u, &v, 4);
+        return static_cast<uint16_t>((u + 0x7FFFu + ((u >> 16) & 1u)) >> 16);
+    }
+    return __half_as_ushort(__float2half_rn(v));
+}
+
+}  // namespace arnettc
+
+// Packs the 3x3 8->8 kernel k[n*72 + tap*8 + c] of one layer for the pair
+// formulation: chunk j (0..11) of 256 bytes, output column n (0..15; n < 8 is
+// pixel 2r, n >= 8 pixel 2r+1, channel n % 8), input channel c.  MMA 2*dy
+// multiplies chunks 4dy (even pixel r+s) and 4dy+1 (odd pixel r-1+s), MMA
+// 2dy+1 chunks 4dy+2 (even r+1+s) and 4dy+3 (odd r+s); for pixel 2r the taps
+// dx = 0, 1, 2 sit at odd r-1, even r, odd r; for pixel 2r+1 at even r, odd r,
+// even r+1.
+void pack_pair_conv8(const float* k, bool bf16, uint16_t* out)
+{
+    using arnettc::to_bits;
+    std::memset(out, 0, 12 * 256);
+    auto put = [&](int chunk, int n, int dx, int dy) {
+        for (int c = 0; c < 8; c++) out[(chunk * 256 + (n / 8) * 128 + (n % 8) * 16) / 2 + c] = to_bits(k[(n % 8) * 72 + (dy * 3 + dx) * 8 + c], bf16);
+    };
+    for (int dy = 0; dy < 3; dy++)
+        for (int n = 0; n < 16; n++)
+        {
+            const bool odd = n >= 8;
+            put(4 * dy + 0, n, odd ? 0 : 1, dy);      // even pixel r
+            if (!odd) put(4 * dy + 1, n, 0, dy);      // odd pixel r-1
+            if (odd) put(4 * dy + 2, n, 2, dy);       // even pixel r+1
+            put(4 * dy + 3, n, odd ? 1 : 2, dy);      // odd pixel r
+        }
+}
+
+// Runs one ARNet x2 pass in the tensor-core form.  packed: 2*blocks layers of
+// pack_pair_conv8 output (device); maps: three [h][w] arrays of 16-byte pixels.
+cudaError_t launch_arnet_tc(const float* kernels, const float* biases, const float* alphas, int blocks, const void* packed,
+                            bool bf16, const Plane& in, const Plane& out, void* const maps[3], int* status,
+                            cudaStream_t stream)
+{
+    using namespace arnettc;
+    const int w = in.w, h = in.h;
+    if (w <= 0 || h <= 0) return cudaSuccess;
+    if (blocks < 2 || !packed || !status) return cudaErrorInvalidValue;
+    uint4* feat = static_cast<uint4*>(maps[0]);
+    uint4* x = static_cast<uint4*>(maps[1]);
+    uint4* t = static_cast<uint4*>(maps[2]);
+    const int tiles_x = (w + TW - 1) / TW, tiles = tiles_x * ((h + TH - 1) / TH);
+    const dim3 pgrid((w + 31) / 32, (h + 7) / 8);
+    cudaError_t err;
+    ConvParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.w = w;
+    p.h = h;
+    p.tiles_x = tiles_x;
+    p.status = status;
+    // head (FP32)
+    {
+        HeadParams hp;
+        for (int i = 0; i < 72; i++) hp.k[i] = kernels[i];
+        for (int i = 0; i < 8; i++) hp.b[i] = biases[i];
+        switch (in.type)
+        {
+        case kU8: bf16 ? head_kernel<uint8_t, true><<<pgrid, 256, 0, stream>>>(in, feat, hp) : head_kernel<uint8_t, false><<<pgrid, 256, 0, stream>>>(in, feat, hp); break;
+        case kU16: bf16 ? head_kernel<uint16_t, true><<<pgrid, 256, 0, stream>>>(in, feat, hp) : head_kernel<uint16_t, false><<<pgrid, 256, 0, stream>>>(in, feat, hp); break;
+        case kF32: bf16 ? head_kernel<float, true><<<pgrid, 256, 0, stream>>>(in, feat, hp) : head_kernel<float, false><<<pgrid, 256, 0, stream>>>(in, feat, hp); break;
+        default: return cudaErrorInvalidValue;
+        }
+        if ((err = cudaGetLastError()) != cudaSuccess) return err;
+        count_launch();
+    }
+    auto conv = [&](int l, int mode, const uint4* src, uint4* dst, const uint4* skip) -> cudaError_t {
+        ConvParams c = p;
+        c.in = src;
+        c.out = dst;
+        c.skip = skip;
+        c.feat = feat;
+        c.bw = static_cast<const uint4*>(packed) + static_cast<size_t>(l - 1) * (B_BYTES / 16);
+        for (int i = 0; i < 8; i++) c.b[i] = biases[8 * l + i];
+        for (int i = 0; i < 8; i++) c.a[i] = mode == kPReLU ? alphas[8 * ((l - 1) / 2) + i] : 0.0f;
+        if (mode == kTail)
+        {
+            for (int i = 0; i < 64; i++) c.k1[i] = kernels[72 + 576 * (2 * blocks) + i];
+            for (int i = 0; i < 8; i++) c.b1[i] = biases[8 * (l + 1) + i];
+            for (int i = 0; i < 8; i++) c.a1[i] = alphas[8 * blocks + i];
+        }
+        cudaError_t e;
+        if (mode == kPReLU) e = bf16 ? launch_conv<kPReLU, true>(c, tiles, stream) : launch_conv<kPReLU, false>(c, tiles, stream);
+        else if (mode == kResidual)
+            e = bf16 ? launch_conv<kResidual, true>(c, tiles, stream) : launch_conv<kResidual, false>(c, tiles, stream);
+        else e = bf16 ? launch_conv<kTail, true>(c, tiles, stream) : launch_conv<kTail, false>(c, tiles, stream);
+        if (e == cudaSuccess) count_launch();
+        return e;
+    };
+    // block 1: t = prelu(conv(feat)); x = 0.2 conv(t) + feat
+    int l = 1;
+    if ((err = conv(l++, kPReLU, feat, t, nullptr)) != cudaSuccess) return err;
+    if ((err = conv(l++, kResidual, t, x, feat)) != cudaSuccess) return err;
+    // blocks 2 .. B-1: t = prelu(conv(x)); x = 0.2 conv(t) + x (in place: each pixel reads its own skip)
+    for (int i = 0; i < blocks - 2; i++)
+    {
+        if ((err = conv(l++, kPReLU, x, t, nullptr)) != cudaSuccess) return err;
+        if ((err = conv(l++, kResidual, t, x, x)) != cudaSuccess) return err;
+    }
+    // block B with the 1x1 + PReLU + feat tail: result into t's partner (feat is still needed, so into x in place)
+    if ((err = conv(l++, kPReLU, x, t, nullptr)) != cudaSuccess) return err;
+    if ((err = conv(l++, kTail, t, x, x)) != cudaSuccess) return err;
+    l++;  // the 1x1 layer's bias index
+    // upscale (FP32)
+    UpParams u;
+    for (int i = 0; i < 288; i++) u.k[i] = kernels[72 + 576 * (2 * blocks) + 64 + i];
+    for (int i = 0; i < 4; i++) u.b[i] = biases[8 * l + i];
+    switch (in.type)
+    {
+    case kU8: bf16 ? up_kernel<uint8_t, true><<<pgrid, 256, 0, stream>>>(x, in, out, u) : up_kernel<uint8_t, false><<<pgrid, 256, 0, stream>>>(x, in, out, u); break;
+    case kU16: bf16 ? up_kernel<uint16_t, true><<<pgrid, 256, 0, stream>>>(x, in, out, u) : up_kernel<uint16_t, false><<<pgrid, 256, 0, stream>>>(x, in, out, u); break;
+    case kF32: bf16 ? up_kernel<float, true><<<pgrid, 256, 0, stream>>>(x, in, out, u) : up_kernel<float, false><<<pgrid, 256, 0, stream>>>(x, in, out, u); break;
+    default: return cudaErrorInvalidValue;
+    }
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    count_launch();
+    return cudaSuccess;
+}
+
+}  // namespace acgb

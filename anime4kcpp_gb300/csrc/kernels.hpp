@@ -110,6 +110,17 @@ cudaError_t launch_merge_resize(const Plane& y, const Plane& uv, ResizeAxis ax, 
 cudaError_t launch_arnet_fp32(const float* kernels, const float* biases, const float* alphas, int blocks, const Plane& in,
                               const Plane& out, float* const maps[4], cudaStream_t stream);
 
+// ARNet<8> x2 pass in the tensor-core form: the 2*blocks 3x3 8->8 layers on
+// tcgen05 (FP16 or BF16 operands, FP32 accumulation, 16-bit maps between
+// layers), the head and the upscale layer in FP32.  `packed`: device copy of
+// 2*blocks pack_pair_conv8 layers (3 KB each); maps: three [h][w] arrays of
+// 16-byte pixels; `status` as tc_status_buffer().
+void pack_pair_conv8(const float* k576, bool bf16, uint16_t* out /* 1536 values */);
+cudaError_t launch_arnet_tc(const float* kernels, const float* biases, const float* alphas, int blocks, const void* packed,
+                            bool bf16, const Plane& in, const Plane& out, void* const maps[3], int* status,
+                            cudaStream_t stream);
+int* tc_status_buffer();
+
 // Merge for chroma resampled by exactly `factor` (2 or 4) on both axes:
 // phase_weights[k*4 + t] is the Catmull-Rom weight of tap t of output phase k,
 // whose first tap is source index + merge_int_phase_offset(factor, k).

@@ -260,6 +260,7 @@ GB300Processor::GB300Processor(int device, const ModelSpec& spec) : spec_(spec)
     if (tc3Shape_ >= kTc3Shapes) tc3Shape_ = -1;
     if (const char* v = std::getenv("AC_GB300_TC3_PER_SM")) tc3PerSm_ = std::atoi(v);
     if (const char* v = std::getenv("AC_GB300_AUTOTUNE")) autotune_ = std::atoi(v) != 0;
+    if (const char* v = std::getenv("AC_GB300_ARNET_TC")) arnetTc_ = std::atoi(v) != 0;
     int n = 0;
     cudaError_t err = cudaGetDeviceCount(&n);
     if (err != cudaSuccess || n == 0)
@@ -338,6 +339,7 @@ GB300Processor::~GB300Processor()
     }
     states_.clear();
     for (auto& d : deviceWeights_) d.release();
+    for (auto& d : arnetPacked_) d.release();
 }
 
 Precision GB300Processor::default_precision()
@@ -446,9 +448,31 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
         cudaEventRecord(ev.first, stream);
     }
     cudaError_t err = cudaErrorNotSupported;
-    if (spec_.family == Family::ARNet)
+    if (spec_.family == Family::ARNet && precision_ != Precision::FP32 && arnetTc_)
     {
-        // ARNet runs the plain FP32 layer pipeline in every precision form.
+        // tensor-core form: 8->8 layers on tcgen05, 16-bit maps between layers
+        const bool bf16 = precision_ == Precision::BF16;
+        const void* w = arnetWeights(bf16);
+        const size_t bytes = static_cast<size_t>(in.w) * in.h * 16;
+        void* maps[3];
+        err = w ? cudaSuccess : cudaErrorMemoryAllocation;
+        for (int i = 0; i < 3 && err == cudaSuccess; i++)
+        {
+            err = ts.maps[i].ensure(bytes);
+            maps[i] = ts.maps[i].ptr;
+        }
+        int* status = tc_status_buffer();
+        if (err == cudaSuccess && !status) err = cudaErrorMemoryAllocation;
+        if (err == cudaSuccess)
+        {
+            const ModelParams& mp = model_params(spec_);
+            err = launch_arnet_tc(mp.kernels.data(), mp.biases.data(), mp.alphas.data(), spec_.blocks, w, bf16, in, out, maps,
+                                  status, stream);
+        }
+    }
+    else if (spec_.family == Family::ARNet)
+    {
+        // the plain FP32 layer pipeline
         const size_t bytes = static_cast<size_t>(in.w) * in.h * 8 * sizeof(float);
         float* maps[4];
         for (int i = 0; i < 4; i++)
@@ -526,6 +550,27 @@ int GB300Processor::collectProfile(double& ms, int& launches, double& outPixels)
     ts.events.clear();
     ts.eventPixels.clear();
     return 0;
+}
+
+const void* GB300Processor::arnetWeights(bool bf16)
+{
+    std::lock_guard<std::mutex> lock(mutex_);
+    DeviceBuffer& d = arnetPacked_[bf16 ? 1 : 0];
+    if (!d.ptr)
+    {
+        const ModelParams& mp = model_params(spec_);
+        const int layers = 2 * spec_.blocks;
+        std::vector<uint16_t> packed(static_cast<size_t>(layers) * 1536);
+        for (int l = 1; l <= layers; l++)
+            pack_pair_conv8(mp.kernels.data() + 72 + 576 * (l - 1), bf16, packed.data() + static_cast<size_t>(l - 1) * 1536);
+        if (d.ensure(packed.size() * sizeof(uint16_t)) != cudaSuccess) return nullptr;
+        if (cudaMemcpy(d.ptr, packed.data(), packed.size() * sizeof(uint16_t), cudaMemcpyHostToDevice) != cudaSuccess)
+        {
+            d.release();
+            return nullptr;
+        }
+    }
+    return d.ptr;
 }
 
 const void* GB300Processor::tcWeights(Precision p, bool pairForm)
