@@ -19,6 +19,8 @@ Voronoi-edge images (no public dataset is attached to this workload).
          persistent launch per step (autotuned tile shape, CUDA-graph replay)
          against FP32 per-image launches
 
+  video  the video workload: 8 frames of 1080p 10-bit YUV 4:2:0 u16 per step,
+         x4 with ARNet-B8 (two x2 luma passes), FP16 tensor-core form vs FP32
   serve  the serving workload: Poisson arrivals (200 jobs/s) of mixed sizes,
          factors, models and formats through the serving loop; p50/p99
          latency and output Mpx/s, FP16 against FP32
@@ -328,6 +330,46 @@ def time_batch(ac, torch, args):
     return res
 
 
+def time_video(ac, torch, args):
+    """The video workload: 8 frames of 1920x1080 10-bit YUV 4:2:0 in u16
+    (a seeded Voronoi-edge canvas translated 3 px per frame, noise 4 LSB) per
+    call, x4 with ARNet-B8 as two chained x2 luma passes (Y shifted by 6 around
+    the network, the reference CLI's recipe), chroma Catmull-Rom resized.
+    Output Mpx/s (luma frame pixels) with inputs resident in HBM."""
+    from anime4kcpp_gb300 import synthetic
+    canvas_y = synthetic.luma(1080, 1920 + 24, np.uint16, cells=256, seed=81, noise=4.0, bits=10)
+    canvas_c = [synthetic.luma(540, 960 + 12, np.uint16, cells=256, seed=82 + k, noise=4.0, bits=10) for k in range(2)]
+    frames, outs = [], []
+    for f in range(8):
+        dx = 3 * f
+        planes = (canvas_y[:, dx:dx + 1920], canvas_c[0][:, dx // 2:dx // 2 + 960], canvas_c[1][:, dx // 2:dx // 2 + 960])
+        frames.append(tuple(torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in planes))
+        outs.append((torch.empty((4320, 7680), dtype=torch.uint16, device="cuda"),
+                     torch.empty((2160, 3840), dtype=torch.uint16, device="cuda"),
+                     torch.empty((2160, 3840), dtype=torch.uint16, device="cuda")))
+    res = {"workload": "8 frames 1920x1080 10-bit YUV420 u16 per step, x4 ARNet-B8 (two x2 luma passes, shift 6), "
+                       "chroma Catmull-Rom"}
+    stream = torch.cuda.Stream()
+    for form in ("fp16", "fp32"):
+        proc = ac.Processor("cuda", 0, "arnet-b8", precision=form)
+        steps = max(2, args.video_steps if form == "fp16" else args.video_steps // 2)
+        with torch.cuda.stream(stream):
+            h = stream.cuda_stream
+            proc.process_yuv_device(frames, outs, 4.0, 6, stream=h, sync=True)
+            l0 = ac.launch_count()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                proc.process_yuv_device(frames, outs, 4.0, 6, stream=h, sync=False)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        res[form] = {"value": 8 * 7680 * 4320 / (ms / 1e3) / 1e6, "unit": "Mpx/s", "ms_per_8_frames": ms,
+                     "launches_per_step": (ac.launch_count() - l0) / steps}
+    res["fp16_over_fp32"] = res["fp16"]["value"] / res["fp32"]["value"]
+    return res
+
+
 SERVE_RES = [(480, 854), (720, 1280), (1080, 1920), (2160, 3840)]
 SERVE_RES_W = [1, 2, 2, 1]
 SERVE_MODELS = ["acnet-legacy-hdn0", "acnet-legacy-hdn1", "acnet-legacy-hdn2", "acnet-legacy-hdn3", "arnet-b8"]
@@ -598,6 +640,8 @@ def run_gb300(args, rank, world, local_rank):
     out["clocks"] = clocks
     if rank == 0 and world == 1 and not args.no_batch:
         out["batch"] = time_batch(ac, torch, args)
+    if rank == 0 and world == 1 and args.video_steps > 0:
+        out["video"] = time_video(ac, torch, args)
     if rank == 0 and world == 1 and args.serve_seconds > 0:
         out["serve"] = time_serve(ac, torch, args)
         out["serve"]["saturation"] = time_serve_saturation(ac, torch, args)
@@ -619,6 +663,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-image batching workload")
     ap.add_argument("--batch-steps", type=int, default=12)
+    ap.add_argument("--video-steps", type=int, default=4, help="8-frame steps of the video workload (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="serving workload length per form (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="serving workload arrival rate, jobs/s")
     ap.add_argument("--saturation-rate", type=float, default=4000.0, help="offered rate of the saturation run, jobs/s")
