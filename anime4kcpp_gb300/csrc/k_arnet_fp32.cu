@@ -46,6 +46,7 @@ struct HeadW
 {
     float k[72];
     float b[8];
+    float a[8];  // PReLU slopes (ACNet<8> head; unused for ARNet's identity head)
 };
 struct UpW
 {
@@ -157,8 +158,9 @@ __global__ void __launch_bounds__(THREADS) tail_kernel(const __grid_constant__ T
     reinterpret_cast<float4*>(out + o)[1] = make_float4(r[4], r[5], r[6], r[7]);
 }
 
-// Head: conv3x3 1->8 (identity) from the input plane.
-template <typename T>
+// Head: conv3x3 1->8 from the input plane, identity (ARNet) or PReLU
+// (ACNet<8>).
+template <typename T, int ACT>
 __global__ void __launch_bounds__(THREADS) head_kernel(const __grid_constant__ HeadW W, Plane in, float* __restrict__ feat)
 {
     __shared__ float s[SY][SX];
@@ -180,7 +182,7 @@ __global__ void __launch_bounds__(THREADS) head_kernel(const __grid_constant__ H
         float v = W.b[n];
 #pragma unroll
         for (int p = 0; p < 9; p++) v = fmaf(s[ty + p / 3][tx + p % 3], W.k[n * 9 + p], v);
-        r[n] = v;
+        r[n] = ACT == kPReLU ? prelu(v, W.a[n]) : v;
     }
     float* o = feat + (static_cast<size_t>(y) * in.w + x) * 8;
     reinterpret_cast<float4*>(o)[0] = make_float4(r[0], r[1], r[2], r[3]);
@@ -248,11 +250,12 @@ cudaError_t launch_arnet_fp32(const float* kernels, const float* biases, const f
         HeadW W;
         for (int i = 0; i < 72; i++) W.k[i] = kernels[i];
         for (int i = 0; i < 8; i++) W.b[i] = biases[i];
+        for (int i = 0; i < 8; i++) W.a[i] = 0.0f;
         switch (in.type)
         {
-        case kU8: head_kernel<uint8_t><<<grid, THREADS, 0, stream>>>(W, in, feat); break;
-        case kU16: head_kernel<uint16_t><<<grid, THREADS, 0, stream>>>(W, in, feat); break;
-        case kF32: head_kernel<float><<<grid, THREADS, 0, stream>>>(W, in, feat); break;
+        case kU8: head_kernel<uint8_t, kIdentity><<<grid, THREADS, 0, stream>>>(W, in, feat); break;
+        case kU16: head_kernel<uint16_t, kIdentity><<<grid, THREADS, 0, stream>>>(W, in, feat); break;
+        case kF32: head_kernel<float, kIdentity><<<grid, THREADS, 0, stream>>>(W, in, feat); break;
         default: return cudaErrorInvalidValue;
         }
         launches++;
@@ -301,6 +304,62 @@ cudaError_t launch_arnet_fp32(const float* kernels, const float* biases, const f
         launches++;
     }
     count_launch(launches);
+    return cudaGetLastError();
+}
+
+// Runs one ACNet<8> x2 pass (core/include/AC/Core/Model/ACNet.hpp:63-116, CPU
+// order core/src/processor/cpu/CPUProcessor.cpp:1417-1436): head conv3x3
+// 1->8 + PReLU, `blocks` x conv3x3 8->8 + PReLU, then the upscale layer of
+// ARNet (conv3x3 8->4, pixel shuffle, + nearest input).  Weight offsets
+// ACNet.hpp:93-114: layer l's kernels at 72 + 576 (l - 1), biases at 8 l,
+// slopes at 8 l.  maps: two [h][w][8] FP32 work maps.
+cudaError_t launch_acnet8_fp32(const float* kernels, const float* biases, const float* alphas, int blocks, const Plane& in,
+                               const Plane& out, float* const maps[2], cudaStream_t stream)
+{
+    using namespace arnet;
+    const int w = in.w, h = in.h;
+    if (w <= 0 || h <= 0) return cudaSuccess;
+    if (blocks < 1) return cudaErrorInvalidValue;
+    dim3 grid((w + BX - 1) / BX, (h + BY - 1) / BY);
+    float* a = maps[0];
+    float* b = maps[1];
+    {
+        HeadW W;
+        for (int i = 0; i < 72; i++) W.k[i] = kernels[i];
+        for (int i = 0; i < 8; i++) W.b[i] = biases[i];
+        for (int i = 0; i < 8; i++) W.a[i] = alphas[i];
+        switch (in.type)
+        {
+        case kU8: head_kernel<uint8_t, kPReLU><<<grid, THREADS, 0, stream>>>(W, in, a); break;
+        case kU16: head_kernel<uint16_t, kPReLU><<<grid, THREADS, 0, stream>>>(W, in, a); break;
+        case kF32: head_kernel<float, kPReLU><<<grid, THREADS, 0, stream>>>(W, in, a); break;
+        default: return cudaErrorInvalidValue;
+        }
+    }
+    for (int l = 1; l <= blocks; l++)
+    {
+        Conv8W W;
+        for (int i = 0; i < 576; i++) W.k[i] = kernels[72 + 576 * (l - 1) + i];
+        for (int i = 0; i < 8; i++) W.b[i] = biases[8 * l + i];
+        for (int i = 0; i < 8; i++) W.a[i] = alphas[8 * l + i];
+        conv8_kernel<kPReLU, false><<<grid, THREADS, 0, stream>>>(W, a, b, nullptr, 0.0f, w, h);
+        float* t = a;
+        a = b;
+        b = t;
+    }
+    {
+        UpW W;
+        for (int i = 0; i < 288; i++) W.k[i] = kernels[72 + 576 * blocks + i];
+        for (int i = 0; i < 4; i++) W.b[i] = biases[8 * (blocks + 1) + i];
+        switch (in.type)
+        {
+        case kU8: up_kernel<uint8_t><<<grid, THREADS, 0, stream>>>(W, a, in, out); break;
+        case kU16: up_kernel<uint16_t><<<grid, THREADS, 0, stream>>>(W, a, in, out); break;
+        case kF32: up_kernel<float><<<grid, THREADS, 0, stream>>>(W, a, in, out); break;
+        default: return cudaErrorInvalidValue;
+        }
+    }
+    count_launch(blocks + 2);
     return cudaGetLastError();
 }
 

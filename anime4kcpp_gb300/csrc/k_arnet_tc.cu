@@ -244,10 +244,13 @@ struct HeadParams
 {
     float k[72];
     float b[8];
+    float a[8];   // PReLU slopes when `prelu` is set (the ACNet<8> head)
+    int prelu;
 };
 
-// Head: conv3x3 1->8 (identity) in FP32 from the input plane, stored as a
-// 16-bit 8-channel map.  One thread per pixel, taps clamped to the plane.
+// Head: conv3x3 1->8 in FP32 from the input plane, identity (ARNet) or PReLU
+// (ACNet<8>), stored as a 16-bit 8-channel map.  One thread per pixel, taps
+// clamped to the plane.
 template <typename T, bool BF16>
 __global__ void __launch_bounds__(256) head_kernel(Plane in, uint4* __restrict__ feat, const __grid_constant__ HeadParams P)
 {
@@ -267,7 +270,7 @@ __global__ void __launch_bounds__(256) head_kernel(Plane in, uint4* __restrict__
         float v = P.b[n];
 #pragma unroll
         for (int p = 0; p < 9; p++) v = fmaf(t[p], P.k[n * 9 + p], v);
-        r[n] = v;
+        r[n] = P.prelu ? prelu(v, P.a[n]) : v;
     }
     feat[static_cast<size_t>(y) * in.w + x] = pack8<BF16>(r);
 }
@@ -358,6 +361,40 @@ void pack_pair_conv8(const float* k, bool bf16, uint16_t* out)
         }
 }
 
+namespace arnettc {
+
+cudaError_t launch_head(const HeadParams& hp, bool bf16, const Plane& in, uint4* feat, cudaStream_t stream)
+{
+    const dim3 pgrid((in.w + 31) / 32, (in.h + 7) / 8);
+    switch (in.type)
+    {
+    case kU8: bf16 ? head_kernel<uint8_t, true><<<pgrid, 256, 0, stream>>>(in, feat, hp) : head_kernel<uint8_t, false><<<pgrid, 256, 0, stream>>>(in, feat, hp); break;
+    case kU16: bf16 ? head_kernel<uint16_t, true><<<pgrid, 256, 0, stream>>>(in, feat, hp) : head_kernel<uint16_t, false><<<pgrid, 256, 0, stream>>>(in, feat, hp); break;
+    case kF32: bf16 ? head_kernel<float, true><<<pgrid, 256, 0, stream>>>(in, feat, hp) : head_kernel<float, false><<<pgrid, 256, 0, stream>>>(in, feat, hp); break;
+    default: return cudaErrorInvalidValue;
+    }
+    const cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess) count_launch();
+    return err;
+}
+
+cudaError_t launch_up(const UpParams& u, bool bf16, const uint4* map, const Plane& in, const Plane& out, cudaStream_t stream)
+{
+    const dim3 pgrid((in.w + 31) / 32, (in.h + 7) / 8);
+    switch (in.type)
+    {
+    case kU8: bf16 ? up_kernel<uint8_t, true><<<pgrid, 256, 0, stream>>>(map, in, out, u) : up_kernel<uint8_t, false><<<pgrid, 256, 0, stream>>>(map, in, out, u); break;
+    case kU16: bf16 ? up_kernel<uint16_t, true><<<pgrid, 256, 0, stream>>>(map, in, out, u) : up_kernel<uint16_t, false><<<pgrid, 256, 0, stream>>>(map, in, out, u); break;
+    case kF32: bf16 ? up_kernel<float, true><<<pgrid, 256, 0, stream>>>(map, in, out, u) : up_kernel<float, false><<<pgrid, 256, 0, stream>>>(map, in, out, u); break;
+    default: return cudaErrorInvalidValue;
+    }
+    const cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess) count_launch();
+    return err;
+}
+
+}  // namespace arnettc
+
 // Runs one ARNet x2 pass in the tensor-core form.  packed: 2*blocks layers of
 // pack_pair_conv8 output (device); maps: three [h][w] arrays of 16-byte pixels.
 cudaError_t launch_arnet_tc(const float* kernels, const float* biases, const float* alphas, int blocks, const void* packed,
@@ -385,6 +422,8 @@ cudaError_t launch_arnet_tc(const float* kernels, const float* biases, const flo
         HeadParams hp;
         for (int i = 0; i < 72; i++) hp.k[i] = kernels[i];
         for (int i = 0; i < 8; i++) hp.b[i] = biases[i];
+        for (int i = 0; i < 8; i++) hp.a[i] = 0.0f;
+        hp.prelu = 0;
         switch (in.type)
         {
         case kU8: bf16 ? head_kernel<uint8_t, true><<<pgrid, 256, 0, stream>>>(in, feat, hp) : head_kernel<uint8_t, false><<<pgrid, 256, 0, stream>>>(in, feat, hp); break;
@@ -446,6 +485,58 @@ cudaError_t launch_arnet_tc(const float* kernels, const float* biases, const flo
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     count_launch();
     return cudaSuccess;
+}
+
+// Runs one ACNet<8> x2 pass in the tensor-core form (network of
+// core/include/AC/Core/Model/ACNet.hpp:63-116, CPU order
+// core/src/processor/cpu/CPUProcessor.cpp:1417-1436): the PReLU head in FP32,
+// `blocks` 3x3 8->8 + PReLU layers on tcgen05 (packed: `blocks` layers of
+// pack_pair_conv8 output), the upscale layer in FP32.  maps: two [h][w]
+// arrays of 16-byte pixels used in turn.
+cudaError_t launch_acnet8_tc(const float* kernels, const float* biases, const float* alphas, int blocks, const void* packed,
+                             bool bf16, const Plane& in, const Plane& out, void* const maps[2], int* status,
+                             cudaStream_t stream)
+{
+    using namespace arnettc;
+    const int w = in.w, h = in.h;
+    if (w <= 0 || h <= 0) return cudaSuccess;
+    if (blocks < 1 || !packed || !status) return cudaErrorInvalidValue;
+    uint4* a = static_cast<uint4*>(maps[0]);
+    uint4* b = static_cast<uint4*>(maps[1]);
+    const int tiles_x = (w + TW - 1) / TW, tiles = tiles_x * ((h + TH - 1) / TH);
+    cudaError_t err;
+    {
+        HeadParams hp;
+        for (int i = 0; i < 72; i++) hp.k[i] = kernels[i];
+        for (int i = 0; i < 8; i++) hp.b[i] = biases[i];
+        for (int i = 0; i < 8; i++) hp.a[i] = alphas[i];
+        hp.prelu = 1;
+        if ((err = launch_head(hp, bf16, in, a, stream)) != cudaSuccess) return err;
+    }
+    ConvParams c;
+    std::memset(&c, 0, sizeof(c));
+    c.w = w;
+    c.h = h;
+    c.tiles_x = tiles_x;
+    c.status = status;
+    for (int l = 1; l <= blocks; l++)
+    {
+        c.in = a;
+        c.out = b;
+        c.bw = static_cast<const uint4*>(packed) + static_cast<size_t>(l - 1) * (B_BYTES / 16);
+        for (int i = 0; i < 8; i++) c.b[i] = biases[8 * l + i];
+        for (int i = 0; i < 8; i++) c.a[i] = alphas[8 * l + i];
+        err = bf16 ? launch_conv<kPReLU, true>(c, tiles, stream) : launch_conv<kPReLU, false>(c, tiles, stream);
+        if (err != cudaSuccess) return err;
+        count_launch();
+        uint4* t = a;
+        a = b;
+        b = t;
+    }
+    UpParams u;
+    for (int i = 0; i < 288; i++) u.k[i] = kernels[72 + 576 * blocks + i];
+    for (int i = 0; i < 4; i++) u.b[i] = biases[8 * (blocks + 1) + i];
+    return launch_up(u, bf16, a, in, out, stream);
 }
 
 }  // namespace acgb

@@ -121,6 +121,16 @@ cudaError_t launch_arnet_tc(const float* kernels, const float* biases, const flo
                             cudaStream_t stream);
 int* tc_status_buffer();
 
+// ACNet<8> x2 pass (head conv 1->8 + PReLU, `blocks` conv 8->8 + PReLU, conv
+// 8->4 + pixel shuffle + nearest input; ACNet.hpp:63-116).  Plain FP32 with
+// two [h][w][8] float maps, or the tensor-core form with `blocks` packed 8->8
+// layers and two [h][w] arrays of 16-byte pixels.
+cudaError_t launch_acnet8_fp32(const float* kernels, const float* biases, const float* alphas, int blocks, const Plane& in,
+                               const Plane& out, float* const maps[2], cudaStream_t stream);
+cudaError_t launch_acnet8_tc(const float* kernels, const float* biases, const float* alphas, int blocks, const void* packed,
+                             bool bf16, const Plane& in, const Plane& out, void* const maps[2], int* status,
+                             cudaStream_t stream);
+
 // Merge for chroma resampled by exactly `factor` (2 or 4) on both axes:
 // phase_weights[k*4 + t] is the Catmull-Rom weight of tap t of output phase k,
 // whose first tap is source index + merge_int_phase_offset(factor, k).

@@ -6,6 +6,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <tuple>
 
 namespace acgb {
 
@@ -15,6 +16,11 @@ extern const uint32_t kAcnetLegacyBlob[];
 extern const int kAcnetLegacyVariants;
 extern const int kAcnetLegacyKernels;
 extern const int kAcnetLegacyBiases;
+// Generated at build time from weights/acnet8.bin: word 0 the variant count
+// (12), then per variant a header {blocks, kernel floats, bias floats, alpha
+// floats} and the floats.
+extern const uint32_t kAcnet8Blob[];
+extern const int kAcnet8Words;
 
 bool parse_model(const char* model, ModelSpec& spec, std::string& error)
 {
@@ -59,8 +65,15 @@ bool parse_model(const char* model, ModelSpec& spec, std::string& error)
             }
             return true;
         }
-        error = "model family not provided by the GB300 backend (ACNet<8>): " + spec.name;
-        return false;
+        // ACNet<8> (Processor.cpp:146-184): every branch checks b4, then
+        // b8, then b18, with B8 the default; box and hdn pick the kind.
+        spec.family = Family::ACNet8;
+        spec.blocks = 8;
+        if (has("b4")) spec.blocks = 4;
+        else if (has("b8")) spec.blocks = 8;
+        else if (has("b18")) spec.blocks = 18;
+        spec.kind = (has("box") ? 2 : 0) + (has("hdn") ? 1 : 0);
+        return true;
     }
     // Processor.cpp:186: anything else is ACNetLegacy GAN.
     spec.family = Family::ACNetLegacy;
@@ -113,10 +126,11 @@ void arnet_synthetic_params(int blocks, uint64_t seed, ModelParams& out)
 const ModelParams& model_params(const ModelSpec& spec)
 {
     static std::mutex m;
-    static std::map<std::pair<int, int>, ModelParams> cache;
+    static std::map<std::tuple<int, int, int>, ModelParams> cache;
     std::lock_guard<std::mutex> lock(m);
-    std::pair<int, int> key = spec.family == Family::ACNetLegacy ? std::make_pair(0, spec.variant)
-                                                                  : std::make_pair(spec.blocks, spec.kind);
+    const auto key = spec.family == Family::ACNetLegacy
+                         ? std::make_tuple(static_cast<int>(spec.family), spec.variant, 0)
+                         : std::make_tuple(static_cast<int>(spec.family), spec.blocks, spec.kind);
     auto it = cache.find(key);
     if (it != cache.end()) return it->second;
     ModelParams p;
@@ -128,6 +142,27 @@ const ModelParams& model_params(const ModelSpec& spec)
         p.biases.resize(kAcnetLegacyBiases);
         std::memcpy(p.kernels.data(), base, sizeof(float) * kAcnetLegacyKernels);
         std::memcpy(p.biases.data(), base + kAcnetLegacyKernels, sizeof(float) * kAcnetLegacyBiases);
+    }
+    else if (spec.family == Family::ACNet8)
+    {
+        // variants in blob order: blocks 4, 8, 18, each as normal, HDN, Box, Box-HDN
+        const int want = (spec.blocks == 4 ? 0 : spec.blocks == 8 ? 1 : 2) * 4 + spec.kind;
+        size_t at = 1;
+        for (int v = 0; v <= want && v < static_cast<int>(kAcnet8Blob[0]); v++)
+        {
+            const uint32_t* h = kAcnet8Blob + at;
+            const size_t nk = h[1], nb = h[2], na = h[3];
+            if (v == want)
+            {
+                p.kernels.resize(nk);
+                p.biases.resize(nb);
+                p.alphas.resize(na);
+                std::memcpy(p.kernels.data(), h + 4, sizeof(float) * nk);
+                std::memcpy(p.biases.data(), h + 4 + nk, sizeof(float) * nb);
+                std::memcpy(p.alphas.data(), h + 4 + nk + nb, sizeof(float) * na);
+            }
+            at += 4 + nk + nb + na;
+        }
     }
     else
     {

@@ -1,9 +1,10 @@
 // Model selection and parameters for the GB300 backend.
 //
-// Families on the hot path: ACNetLegacy (trained parameters of the
-// reference, variants GAN and HDN0..3) and ARNet<8> (B8/16/32/64 x
-// {normal, HDN, Box, Box-HDN}; seeded synthetic parameters because the
-// reference's trained ARNet parameters are not distributed with its source).
+// Families: ACNetLegacy (trained parameters of the reference, variants GAN
+// and HDN0..3), ACNet<8> (trained parameters of the reference, B4/8/18 x
+// {normal, HDN, Box, Box-HDN}) and ARNet<8> (B8/16/32/64 x {normal, HDN,
+// Box, Box-HDN}; seeded synthetic parameters because the reference's trained
+// ARNet parameters are not distributed with its source).
 #pragma once
 
 #include <cstdint>
@@ -12,20 +13,20 @@
 
 namespace acgb {
 
-enum class Family { ACNetLegacy, ARNet };
+enum class Family { ACNetLegacy, ARNet, ACNet8 };
 
 struct ModelSpec
 {
     Family family = Family::ACNetLegacy;
     int variant = 0;  // ACNetLegacy: 0 GAN, 1..4 HDN0..3
-    int blocks = 0;   // ARNet: 8, 16, 32, 64
-    int kind = 0;     // ARNet: 0 normal, 1 HDN, 2 Box, 3 Box-HDN
+    int blocks = 0;   // ARNet: 8, 16, 32, 64; ACNet<8>: 4, 8, 18
+    int kind = 0;     // ARNet, ACNet<8>: 0 normal, 1 HDN, 2 Box, 3 Box-HDN
     std::string name;
 };
 
 // Parses a model string like core/src/processor/Processor.cpp:26-187 does
-// for the ACNetLegacy and ARNet families.  Returns false (with a message)
-// for the families this backend does not run (ACNet<8>, ArtCNN, FSRCNNX).
+// for the ACNetLegacy, ACNet<8> and ARNet families.  Returns false (with a
+// message) for the families this backend does not run (ArtCNN, FSRCNNX).
 bool parse_model(const char* model, ModelSpec& spec, std::string& error);
 
 struct ModelParams
@@ -33,8 +34,8 @@ struct ModelParams
     std::vector<float> kernels, biases, alphas;
 };
 
-// Parameters in the reference's NHWC blob layout (ACNet.hpp:34-60,
-// ARNet.hpp:26-70).
+// Parameters in the reference's NHWC blob layout (ACNet.hpp:34-60 and
+// :63-116, ARNet.hpp:26-70).
 const ModelParams& model_params(const ModelSpec& spec);
 
 // Seed of the synthetic ARNet parameters of a variant.

@@ -483,6 +483,41 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
         const ModelParams& mp = model_params(spec_);
         err = launch_arnet_fp32(mp.kernels.data(), mp.biases.data(), mp.alphas.data(), spec_.blocks, in, out, maps, stream);
     }
+    else if (spec_.family == Family::ACNet8)
+    {
+        const ModelParams& mp = model_params(spec_);
+        if (precision_ != Precision::FP32 && arnetTc_)
+        {
+            // tensor-core form: the 8->8 layers on tcgen05, 16-bit maps between layers
+            const bool bf16 = precision_ == Precision::BF16;
+            const void* w = arnetWeights(bf16);
+            const size_t bytes = static_cast<size_t>(in.w) * in.h * 16;
+            void* maps[2];
+            err = w ? cudaSuccess : cudaErrorMemoryAllocation;
+            for (int i = 0; i < 2 && err == cudaSuccess; i++)
+            {
+                err = ts.maps[i].ensure(bytes);
+                maps[i] = ts.maps[i].ptr;
+            }
+            int* status = tc_status_buffer();
+            if (err == cudaSuccess && !status) err = cudaErrorMemoryAllocation;
+            if (err == cudaSuccess)
+                err = launch_acnet8_tc(mp.kernels.data(), mp.biases.data(), mp.alphas.data(), spec_.blocks, w, bf16, in, out,
+                                       maps, status, stream);
+        }
+        else
+        {
+            const size_t bytes = static_cast<size_t>(in.w) * in.h * 8 * sizeof(float);
+            float* maps[2];
+            for (int i = 0; i < 2; i++)
+            {
+                if ((err = ts.maps[i].ensure(bytes)) != cudaSuccess) return err;
+                maps[i] = static_cast<float*>(ts.maps[i].ptr);
+            }
+            err = launch_acnet8_fp32(mp.kernels.data(), mp.biases.data(), mp.alphas.data(), spec_.blocks, in, out, maps,
+                                     stream);
+        }
+    }
     else if (spec_.family == Family::ACNetLegacy)
     {
         if (precision_ == Precision::FP32) err = launch_acnet_legacy_fp32(*acnet_, in, out, ph, stream);
@@ -559,7 +594,8 @@ const void* GB300Processor::arnetWeights(bool bf16)
     if (!d.ptr)
     {
         const ModelParams& mp = model_params(spec_);
-        const int layers = 2 * spec_.blocks;
+        // the 3x3 8->8 layers: two per ARNet block, one per ACNet<8> block
+        const int layers = spec_.family == Family::ARNet ? 2 * spec_.blocks : spec_.blocks;
         std::vector<uint16_t> packed(static_cast<size_t>(layers) * 1536);
         for (int l = 1; l <= layers; l++)
             pack_pair_conv8(mp.kernels.data() + 72 + 576 * (l - 1), bf16, packed.data() + static_cast<size_t>(l - 1) * 1536);

@@ -129,7 +129,7 @@ private:
     const ResizeAxis* axis(ThreadState& ts, int n_in, int n_out, int mode, cudaStream_t stream, cudaError_t& err);
     cudaError_t luma_pass(ThreadState& ts, const Plane& in, const Plane& out, const Phase2* ph, cudaStream_t stream);
     const void* tcWeights(Precision p, bool pairForm);
-    const void* arnetWeights(bool bf16);  // packed 8->8 layers of the ARNet tensor-core form
+    const void* arnetWeights(bool bf16);  // packed 8->8 layers of the ARNet / ACNet<8> tensor-core forms
     // Tile shape and CTAs per SM for a persistent launch over these images:
     // forced by AC_GB300_TC3_SHAPE / AC_GB300_TC3_PER_SM, else measured once
     // per batch class (element type, channels, form, log2 of the total and
@@ -148,8 +148,8 @@ private:
     bool profiling_ = false;
     std::unique_ptr<AcnetLegacyWeights> acnet_;
     DeviceBuffer deviceWeights_[4];  // TC weights: {one-pixel, pair} x {FP16, BF16}
-    DeviceBuffer arnetPacked_[2];    // ARNet 8->8 layers, pair form: FP16, BF16
-    bool arnetTc_ = true;            // ARNet tensor-core form in FP16/BF16 (AC_GB300_ARNET_TC=0: FP32 pipeline)
+    DeviceBuffer arnetPacked_[2];    // ARNet / ACNet<8> 8->8 layers, pair form: FP16, BF16
+    bool arnetTc_ = true;            // ARNet / ACNet<8> tensor-core form in FP16/BF16 (AC_GB300_ARNET_TC=0: FP32 pipeline)
     int tc3Ctas_ = 0;                // CTAs of the persistent kernel (0: one per SM; AC_GB300_TC3_CTAS)
     bool fused_ = true;              // RGB(A) x2 in one fused kernel (AC_GB300_FUSED=0 disables)
     int tcKernel_ = 3;               // tensor-core kernel: 3 persistent (default), 2 pair-interleaved, 1 one-pixel-per-row (AC_GB300_TC_KERNEL)

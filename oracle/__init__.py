@@ -26,6 +26,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 WEIGHTS_BLOB = os.path.join(ROOT, "anime4kcpp_gb300", "weights", "acnet_legacy.bin")
+ACNET8_BLOB = os.path.join(ROOT, "anime4kcpp_gb300", "weights", "acnet8.bin")
 
 U8, U16, F32 = 0x001, 0x002, 0x204
 _TYPE_OF = {np.dtype(np.uint8): U8, np.dtype(np.uint16): U16, np.dtype(np.float32): F32}
@@ -58,6 +59,8 @@ def lib():
             L.orc_acnet_legacy_x2_f64.argtypes = [vp, i, i, i, i, dp, fp, fp, i]
             L.orc_arnet_x2.argtypes = [vp, i, i, i, i, vp, i, fp, fp, fp, i, i]
             L.orc_arnet_x2_f64.argtypes = [vp, i, i, i, i, dp, fp, fp, fp, i, i]
+            L.orc_acnet8_x2.argtypes = [vp, i, i, i, i, vp, i, fp, fp, fp, i, i]
+            L.orc_acnet8_x2_f64.argtypes = [vp, i, i, i, i, dp, fp, fp, fp, i, i]
             L.orc_rgb2yuv.argtypes = [vp, i, i, i, i, i, vp, i, vp, i]
             L.orc_yuv2rgb.argtypes = [vp, i, vp, i, i, i, i, i, vp, i]
             L.orc_resize.argtypes = [vp, i, i, i, i, i, vp, i, i, i, i]
@@ -65,6 +68,7 @@ def lib():
             L.orc_resize_coeffs.argtypes = [i, i, i, vp, vp, i]
             L.orc_arnet_synth.argtypes = [i, ctypes.c_uint64, fp, fp, fp]
             for fn in ("orc_acnet_legacy_x2", "orc_acnet_legacy_x2_f64", "orc_arnet_x2", "orc_arnet_x2_f64",
+                       "orc_acnet8_x2", "orc_acnet8_x2_f64",
                        "orc_rgb2yuv", "orc_yuv2rgb", "orc_resize", "orc_resize_mt", "orc_resize_coeffs", "orc_arnet_synth"):
                 getattr(L, fn).restype = ctypes.c_int
             _lib = L
@@ -107,8 +111,9 @@ def _plane(a):
 
 def parse_model(name):
     """Model string -> (family, variant) following Processor.cpp:26-187 for the
-    ACNetLegacy and ARNet families.  Returns ("acnet_legacy", idx 0..4) with
-    0=GAN, 1..4=HDN0..3, or ("arnet", (blocks, kind))."""
+    ACNetLegacy, ACNet<8> and ARNet families.  Returns ("acnet_legacy", idx
+    0..4) with 0=GAN, 1..4=HDN0..3, ("acnet8", (blocks, kind)) or ("arnet",
+    (blocks, kind)); kind 0 normal, 1 HDN, 2 Box, 3 Box-HDN."""
     s = (name or "").lower()
     if "arnet" in s:
         box = "box" in s
@@ -129,8 +134,16 @@ def parse_model(name):
                     idx = 1 + int(ch)
                     break
         return "acnet_legacy", idx
-    if "acnet" in s or "artcnn" in s or "fsrcnnx" in s:
+    if "fsrcnnx" in s or "artcnn" in s:
         raise ValueError("model family outside this backend's scope: %r" % name)
+    if "acnet" in s:
+        # Processor.cpp:146-184: b4, then b8, then b18; B8 by default.
+        blocks = 8
+        for tag, b in (("b4", 4), ("b8", 8), ("b18", 18)):
+            if tag in s:
+                blocks = b
+                break
+        return "acnet8", (blocks, (2 if "box" in s else 0) + (1 if "hdn" in s else 0))
     return "acnet_legacy", 0
 
 
@@ -162,6 +175,25 @@ def arnet_weights(blocks, kind):
     return _weights_cache[key]
 
 
+def acnet8_weights(blocks, kind):
+    """(kernels, biases, alphas) float32 of the trained ACNet<8> variant
+    (blocks 4/8/18; kind 0 normal, 1 HDN, 2 Box, 3 Box-HDN), read from the
+    blob extracted from the reference's ACNet.p."""
+    if "acnet8" not in _weights_cache:
+        raw = open(ACNET8_BLOB, "rb").read()
+        assert raw[:8] == b"ACGBW8F1"
+        n = int(np.frombuffer(raw[8:12], dtype="<u4")[0])
+        at, table = 12, {}
+        for v in range(n):
+            b, nk, nb, na = (int(x) for x in np.frombuffer(raw[at:at + 16], dtype="<u4"))
+            f = np.frombuffer(raw[at + 16:at + 16 + 4 * (nk + nb + na)], dtype="<f4")
+            table[(b, v % 4)] = (np.ascontiguousarray(f[:nk]), np.ascontiguousarray(f[nk:nk + nb]),
+                                 np.ascontiguousarray(f[nk + nb:]))
+            at += 16 + 4 * (nk + nb + na)
+        _weights_cache["acnet8"] = table
+    return _weights_cache["acnet8"][(blocks, kind)]
+
+
 # --------------------------------------------------------------- primitives
 
 def luma_x2(y, model, threads=0, f64=False):
@@ -176,6 +208,9 @@ def luma_x2(y, model, threads=0, f64=False):
         if fam == "acnet_legacy":
             k, b = acnet_legacy_weights(var)
             rc = lib().orc_acnet_legacy_x2_f64(_p(y), w, h, y.strides[0], t, _p(out), _p(k), _p(b), threads)
+        elif fam == "acnet8":
+            k, b, a = acnet8_weights(*var)
+            rc = lib().orc_acnet8_x2_f64(_p(y), w, h, y.strides[0], t, _p(out), _p(k), _p(b), _p(a), var[0], threads)
         else:
             k, b, a = arnet_weights(*var)
             rc = lib().orc_arnet_x2_f64(_p(y), w, h, y.strides[0], t, _p(out), _p(k), _p(b), _p(a), var[0], threads)
@@ -184,6 +219,10 @@ def luma_x2(y, model, threads=0, f64=False):
         if fam == "acnet_legacy":
             k, b = acnet_legacy_weights(var)
             rc = lib().orc_acnet_legacy_x2(_p(y), w, h, y.strides[0], t, _p(out), out.strides[0], _p(k), _p(b), threads)
+        elif fam == "acnet8":
+            k, b, a = acnet8_weights(*var)
+            rc = lib().orc_acnet8_x2(_p(y), w, h, y.strides[0], t, _p(out), out.strides[0], _p(k), _p(b), _p(a), var[0],
+                                     threads)
         else:
             k, b, a = arnet_weights(*var)
             rc = lib().orc_arnet_x2(_p(y), w, h, y.strides[0], t, _p(out), out.strides[0], _p(k), _p(b), _p(a), var[0], threads)

@@ -20,7 +20,8 @@
  *       :116-164 conv3x3_float, :166-197 conv3x3_cin1, :223-288 conv3x3_conv1x1,
  *       :290-342 conv3x3_pixelshuffle, :344-393 conv3x3_deconv2x2
  *   core/internal/AC/Core/Internal/Processor/CPU/Generic.hpp:19-81  summation order
- *   core/src/processor/cpu/CPUProcessor.cpp:1371-1390 (ACNetLegacy), :1464-1491 (ARNet)
+ *   core/src/processor/cpu/CPUProcessor.cpp:1371-1390 (ACNetLegacy), :1417-1436 (ACNet<8>),
+ *       :1464-1491 (ARNet)
  *   core/src/ImageProcess.cpp:39-61 rgb2yuv, :114-138 rgba2yuva,
  *       :192-215 yuv2rgb, :276-308 yuva2rgba
  *   core/src/ImageResize.cpp:62-83,127-134,136-273  resize filters (the
@@ -410,6 +411,34 @@ int orc_arnet_x2(const void* src, int w, int h, int sstride, int type,
     return 0;
 }
 
+/* ACNet<8> x2 pass, CPUProcessor.cpp:1417-1436: conv3x3_1to8_prelu, `blocks` x
+ * conv3x3_8to8_prelu, conv3x3_8to4_identity_pixelshuffle_4to1_add.  Weight
+ * offsets ACNet.hpp:93-114: layer l's kernels at 72 + 576 (l - 1), biases and
+ * PReLU slopes at 8 l. */
+int orc_acnet8_x2(const void* src, int w, int h, int sstride, int type,
+                  void* dst, int dstride, const float* kernels, const float* biases, const float* alphas,
+                  int blocks, int threads)
+{
+    if (!src || !dst || w <= 0 || h <= 0 || blocks < 1) return -22;
+    size_t n = (size_t)w * h * 8;
+    float* a = (float*)malloc(n * sizeof(float));
+    float* b = (float*)malloc(n * sizeof(float));
+    if (!a || !b) { free(a); free(b); return -12; }
+    l0_ctx c0 = { src, w, h, sstride, type, a, kernels, biases, ACT_PRELU, alphas };
+    parallel_rows(l0_rows, &c0, h, threads);
+    for (int l = 1; l <= blocks; l++)
+    {
+        l8_ctx c = { a, b, w, h, kernels + 72 + 576 * (l - 1), biases + 8 * l, ACT_PRELU, alphas + 8 * l, NULL, 0.0f };
+        parallel_rows(l8_rows, &c, h, threads);
+        float* t = a; a = b; b = t;
+    }
+    lp_ctx cp = { a, w, h, src, sstride, dst, dstride, type, kernels + 72 + 576 * blocks, biases + 8 * (blocks + 1) };
+    parallel_rows(lp_rows, &cp, h, threads);
+    free(a);
+    free(b);
+    return 0;
+}
+
 /* ------------------------------------------------------- FP64 networks */
 
 static inline void taps_d(const double* src, int w, int x, int y, int h, const double** rp)
@@ -619,6 +648,36 @@ int orc_arnet_x2_f64(const void* src, int w, int h, int sstride, int type,
 #undef KOFF
 #undef AOFF
     free(feat); free(t1); free(t2); free(t3);
+    return 0;
+}
+
+/* ACNet<8> x2 in FP64. */
+int orc_acnet8_x2_f64(const void* src, int w, int h, int sstride, int type,
+                      double* dst, const float* kernels, const float* biases, const float* alphas,
+                      int blocks, int threads)
+{
+    if (!src || !dst || w <= 0 || h <= 0 || blocks < 1) return -22;
+    size_t n = (size_t)w * h * 8;
+    double* a = (double*)malloc(n * sizeof(double));
+    double* b = (double*)malloc(n * sizeof(double));
+    if (!a || !b) { free(a); free(b); return -12; }
+    d_ctx c;
+    memset(&c, 0, sizeof(c));
+    c.src = src; c.w = w; c.h = h; c.sstride = sstride; c.type = type; c.dst = dst;
+    c.k = kernels; c.bi = biases; c.al = alphas; c.blocks = blocks;
+    c.out = a; c.act = ACT_PRELU; c.alpha_l = alphas; c.kl = kernels; c.bl = biases;
+    parallel_rows(d_l0_rows, &c, h, threads);
+    for (int l = 1; l <= blocks; l++)
+    {
+        c.in = a; c.out = b; c.act = ACT_PRELU; c.alpha_l = alphas + 8 * l;
+        c.kl = kernels + 72 + 576 * (l - 1); c.bl = biases + 8 * l; c.id = NULL;
+        parallel_rows(d_l8_rows, &c, h, threads);
+        double* t = a; a = b; b = t;
+    }
+    c.in = a; c.kl = kernels + 72 + 576 * blocks; c.bl = biases + 8 * (blocks + 1);
+    parallel_rows(d_shuffle_rows, &c, h, threads);
+    free(a);
+    free(b);
     return 0;
 }
 

@@ -4,7 +4,8 @@ Runs where the Anime4KCPP sources were compiled into ``oracle/_ref`` (``make -C
 oracle ref``).  Every case feeds a seeded synthetic input to the reference's
 ``ac::core::Processor`` (CPU, Generic backend = arch 1, and its automatic ISA
 choice = arch 0) and stores input and outputs in ``golden.npz`` with the case
-list in ``golden.json``.  The reference's ARNet parameters are absent, so the
+list in ``golden.json``.  ACNetLegacy and ACNet<8> cases use the reference's
+trained parameters.  The reference's ARNet parameters are absent, so the
 ARNet cases use the seeded synthetic ARNet parameters of ``oracle``; the chroma
 resize inside the reference build is this project's restatement (the
 reference's stb_image_resize2 is not vendored), so RGB cases pin the
@@ -47,6 +48,13 @@ CASES = [
     ("gray_u16_arnet_b8_x4", "luma10", (11, 13), "uint16", "arnet-b8", 4.0, 28),
     ("gray_u8_arnet_hdn_b16_x2", "luma", (15, 18), "uint8", "arnet-hdn-b16", 2.0, 29),
     ("rgb_u8_arnet_b8_x2", "rgb", (12, 14), "uint8", "arnet-b8", 2.0, 30),
+    ("gray_u8_acnet_f8b4_x2", "luma", (21, 29), "uint8", "acnet-f8b4", 2.0, 31),
+    ("gray_u8_acnet_f8b8_hdn_x2", "luma", (18, 23), "uint8", "acnet-f8b8-hdn", 2.0, 32),
+    ("gray_u16_acnet_f8b18_box_x2", "luma10", (13, 17), "uint16", "acnet-f8b18-box", 2.0, 33),
+    ("gray_f32_acnet_box_hdn_x2", "luma", (11, 19), "float32", "acnet-box-hdn", 2.0, 34),
+    ("gray_u8_acnet_f8b8_x4", "luma", (9, 14), "uint8", "acnet-f8b8", 4.0, 35),
+    ("rgb_u8_acnet_f8b8_hdn_x2", "rgb", (14, 18), "uint8", "acnet-f8b8-hdn", 2.0, 36),
+    ("gray_u8_acnet_1x3_x2", "luma", (1, 3), "uint8", "acnet-f8b4-hdn", 2.0, 37),
 ]
 
 

@@ -81,8 +81,26 @@ def test_cpu_and_opencl_types_are_refused(lib):
 
 
 def test_unsupported_family_is_refused(lib):
-    p = ac.Processor("cuda", 0, "acnet-f8b8-hdn")
-    assert not p.ok() and "ACNet<8>" in p.error()
+    for m in ("artcnn-c4f16", "fsrcnnx-f8b4"):
+        p = ac.Processor("cuda", 0, m)
+        assert not p.ok() and "not provided" in p.error()
+
+
+def test_acnet8_parameters_match_the_reference_blob(lib):
+    """Every ACNet<8> variant (B4/8/18 x normal/HDN/Box/Box-HDN) resolves as the
+    reference's model strings do and carries the reference's trained
+    parameters, in the NHWC sizes of ACNet.hpp:79-84."""
+    for blocks in (4, 8, 18):
+        for kind, tag in enumerate(("", "-hdn", "-box", "-box-hdn")):
+            name = "acnet-f8b%d%s" % (blocks, tag)
+            assert oracle.parse_model(name) == ("acnet8", (blocks, kind))
+            k, b, a = ac.model_params(name)
+            assert (k.size, b.size, a.size) == (72 + 576 * blocks + 288, 8 + 8 * blocks + 4, 8 * (blocks + 1))
+            rk, rb, ra = oracle.acnet8_weights(blocks, kind)
+            assert np.array_equal(k, rk) and np.array_equal(b, rb) and np.array_equal(a, ra)
+    # defaults: B8, and "acnet" alone is ACNet<8> B8 normal (Processor.cpp:175-184)
+    assert np.array_equal(ac.model_params("acnet-hdn")[0], oracle.acnet8_weights(8, 1)[0])
+    assert np.array_equal(ac.model_params("ACNet")[0], oracle.acnet8_weights(8, 0)[0])
 
 
 def test_output_shape_matches_oracle_pipeline(lib):
