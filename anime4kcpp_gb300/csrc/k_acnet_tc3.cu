@@ -12,6 +12,31 @@ int* tc_status_buffer();
 
 int acnet_tc3_max_images() { return tcv3::kMaxImages; }
 
+// B matrices of the persistent kernel: layer 0 as an 8-channel layer over
+// the input slots (y_hi, y_lo, y_hi) with weights (w_hi, w_hi, w_lo), then
+// the eight 3x3 8->8 layers, each in the pair layout of pack_pair_conv8.
+void pack_acnet_tc3_weights(const AcnetLegacyWeights& w, bool bf16, std::vector<uint16_t>& packed)
+{
+    using namespace tcv3;
+    packed.assign(static_cast<size_t>(B_BYTES) / 2, 0);
+    auto round16 = [bf16](float v) {
+        return bf16 ? __bfloat162float(__float2bfloat16_rn(v)) : __half2float(__float2half_rn(v));
+    };
+    std::vector<float> k0(576, 0.0f);
+    for (int n = 0; n < 8; n++)
+        for (int t = 0; t < 9; t++)
+        {
+            const float v = w.k[n * 9 + t];  // layer 0: k[n * 9 + tap] (ACNet.hpp:48-60)
+            const float hi = round16(v);
+            k0[n * 72 + t * 8 + 0] = hi;
+            k0[n * 72 + t * 8 + 1] = hi;
+            k0[n * 72 + t * 8 + 2] = v - hi;
+        }
+    pack_pair_conv8(k0.data(), bf16, packed.data());
+    for (int l = 1; l < NL; l++)
+        pack_pair_conv8(w.k + 72 + 576 * (l - 1), bf16, packed.data() + static_cast<size_t>(l) * BL_BYTES / 2);
+}
+
 void acnet_tc3_shape(int shape, int* tw, int* th)
 {
     using namespace tcv3;
@@ -42,11 +67,9 @@ cudaError_t launch_tc3(const AcnetLegacyWeights& wts, const void* packed2, bool 
     Params p;
     std::memset(&p, 0, sizeof(p));
     p.bw = static_cast<const uint4*>(packed2);
-    for (int i = 0; i < 72; i++) p.k0[i] = wts.k[i];
-    for (int i = 0; i < 8; i++) p.b0[i] = wts.b[i];
     for (int i = 0; i < 32; i++) p.k2[i] = wts.k[72 + 576 * 8 + i];
     for (int l = 0; l < NL; l++)
-        for (int k = 0; k < 8; k++) p.bias[l][k] = wts.b[8 * (l + 1) + k];
+        for (int k = 0; k < 8; k++) p.bias[l][k] = wts.b[8 * l + k];
     if (phase2) p.ph = *phase2;
     int tiles = 0;
     for (int i = 0; i < n; i++)

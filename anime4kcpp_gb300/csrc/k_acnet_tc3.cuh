@@ -33,6 +33,13 @@
 //    after it have completed (they read the rows it overwrites; they may come
 //    from the other issuer), and a block's accumulator
 //    is overwritten by the next layer only after the round barrier above.
+//  * Layer 0 (3x3, 1 -> 8) runs on the tensor core too, as a ninth layer of
+//    the same shape: the prologue stores each window pixel's luma in the
+//    activation slot as three 16-bit channels (y_hi, y_lo, y_hi, where y_lo =
+//    y - y_hi) and the layer's B matrix holds (w_hi, w_hi, w_lo) for them, so
+//    the FP32 accumulation of y_hi w_hi + y_lo w_hi + y_hi w_lo carries the
+//    layer at close to FP32 accuracy (the dropped y_lo w_lo term is ~2^-22
+//    relative for FP16 operands).
 //  * Every wait is bounded by %globaltimer; a timeout raises a CTA-wide abort
 //    flag and the status word, all roles fall through their loops without
 //    touching tensor memory, and the CTA frees its tensor memory and exits.
@@ -54,8 +61,9 @@ namespace tcv3 {
 constexpr int HALO = 9;
 constexpr int NBLK = 16;  // 16 x 128 pairs per window
 constexpr int NROUND = NBLK / 4;
-constexpr int BL_BYTES = 14 * 256;
-constexpr int NL = 8;
+constexpr int BL_BYTES = 12 * 256;       // one layer's packed B (pack_pair_conv8)
+constexpr int NL = 9;                    // MMA layers: layer 0 and the eight 3x3 8->8 layers
+constexpr int LAST = NL - 1;             // the layer followed by the deconvolution
 constexpr int B_BYTES = NL * BL_BYTES;
 constexpr int NEPI = 8;                   // epilogue warps: two groups of four
 constexpr int NISS = 2;                   // MMA issuing warps
@@ -89,10 +97,8 @@ struct Layout
 {
     static constexpr int ACT_OFF = 0;
     static constexpr int B_OFF = G::ACT_BYTES;
-    static constexpr int RAW_OFF = B_OFF + B_BYTES;
     static constexpr int WW = G::WW, WH = G::WH, UVW = G::UVW, UVH = G::UVH;
-    static constexpr int raw_bytes = (WW * WH * static_cast<int>(sizeof(T)) + 15) / 16 * 16;
-    static constexpr int uv_off = RAW_OFF + raw_bytes;
+    static constexpr int uv_off = B_OFF + B_BYTES;
     static constexpr int uv_bytes = C == 1 ? 0 : (UVW * UVH * (C - 1) * static_cast<int>(sizeof(T)) + 15) / 16 * 16;
     static constexpr int lut_off = uv_off + uv_bytes;
     static constexpr int lut_bytes = sizeof(T) == 1 ? 1024 : 0;
@@ -109,11 +115,9 @@ struct Image3
 
 struct Params
 {
-    const uint4* bw;
-    float k0[72];
-    float b0[8];
+    const uint4* bw;    // NL packed B matrices (pack_acnet_tc3_weights)
     float k2[32];
-    float bias[NL][8];  // layers 1..8, added in the epilogue
+    float bias[NL][8];  // layers 0..8, added in the epilogue
     Phase2 ph;
     int nimg;
     int ntiles;
@@ -131,6 +135,23 @@ __device__ __forceinline__ uint4 pack8(const float* v)
     else
         return make_uint4(tc::pack_relu_f16x2(v[0], v[1]), tc::pack_relu_f16x2(v[2], v[3]), tc::pack_relu_f16x2(v[4], v[5]),
                           tc::pack_relu_f16x2(v[6], v[7]));
+}
+
+// Layer-0 input slot of a luma value: channels (y_hi, y_lo, y_hi, 0, ...),
+// y_hi = y rounded to the operand type and y_lo = y - y_hi rounded again.
+template <bool BF16>
+__device__ __forceinline__ uint4 luma_slot(float y)
+{
+    if constexpr (BF16)
+    {
+        const float hi = __bfloat162float(__float2bfloat16_rn(y));
+        return make_uint4(tc::pack_bf16x2(y, y - hi), tc::pack_bf16x2(y, 0.0f), 0u, 0u);
+    }
+    else
+    {
+        const float hi = __half2float(__float2half_rn(y));
+        return make_uint4(tc::pack_f16x2(y, y - hi), tc::pack_f16x2(y, 0.0f), 0u, 0u);
+    }
 }
 
 // Activation slot of window pixel p in the buffer at `base`.
@@ -198,8 +219,7 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
     constexpr int TW = G::TW, TH = G::TH, WW = G::WW, WH = G::WH, PPR = G::PPR, PADP = G::PADP;
     constexpr int PLANE_BYTES = G::PLANE_BYTES, ACT_BYTES = G::ACT_BYTES;
     constexpr int UVW = G::UVW, UVH = G::UVH, UVX0 = G::UVX0;
-    constexpr int ACT_OFF = L::ACT_OFF, B_OFF = L::B_OFF, RAW_OFF = L::RAW_OFF;
-    T* raw = reinterpret_cast<T*>(smem + RAW_OFF);
+    constexpr int ACT_OFF = L::ACT_OFF, B_OFF = L::B_OFF;
     T* uvs = reinterpret_cast<T*>(smem + L::uv_off);
     float* lut = reinterpret_cast<float*>(smem + L::lut_off);
     uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + L::misc_off);         // [NBLK]
@@ -269,7 +289,7 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
         const int iy0 = max(0, -gy0), iy1 = min(WH - 1, H - 1 - gy0);
         const bool edges = ix0 > 0 || ix1 < WW - 1 || iy0 > 0 || iy1 < WH - 1;  // an image edge inside the window
 
-        // ---- prologue (all warps): window luma (+ chroma region), layer 0 ----
+        // ---- prologue (all warps): window luma as layer-0 input slots (+ chroma region) ----
         // Loads are issued in batches of four pixels per thread before any
         // of them is converted, so their latencies overlap.
         constexpr int PER = (WW * WH + THREADS - 1) / THREADS;
@@ -294,13 +314,13 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
             {
                 const int i = tid + (k0 + k) * THREADS;
                 if (i >= WW * WH) continue;
-                if constexpr (C == 1) raw[i] = px[k][0];
+                T yq;
+                if constexpr (C == 1) yq = px[k][0];
                 else
                 {
                     const int wy = i / WW, wx = i - wy * WW;
-                    T yq, uvq[C - 1];
+                    T uvq[C - 1];
                     rgb_to_yuv_q_lut<T, C>(px[k], yq, uvq, lut);
-                    raw[i] = yq;
                     const int ux = wx - UVX0, uy = wy - UVX0;
                     if (ux >= 0 && ux < UVW && uy >= 0 && uy < UVH)
                     {
@@ -308,31 +328,23 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
                         for (int c = 0; c < C - 1; c++) uvs[(uy * UVW + ux) * (C - 1) + c] = uvq[c];
                     }
                 }
+                // the window is loaded with clamped coordinates, so taps
+                // that leave the image read the edge pixel (clamp-to-edge)
+                *slot<G>(act, i) = luma_slot<BF16>(to_float_lut<T>(yq, lut));
             }
         }
-        __syncthreads();
-        // With chroma the previous tile's horizontal pass left float data in
-        // the buffer, so layer 0 then covers the whole window (border too).
-        constexpr int L0B = C > 1 ? 0 : 1;
-        for (int i = tid; i < (WW - 2 * L0B) * (WH - 2 * L0B); i += THREADS)
+        // The slots around the window (the planes' pads and the unused tail)
+        // are read with zero weights by the window's first and last rows;
+        // the previous tile's chroma pass may have left non-finite bit
+        // patterns there, so they are cleared.
         {
-            const int y = L0B + i / (WW - 2 * L0B), x = L0B + i % (WW - 2 * L0B);
-            const int cy = clampi(y, iy0, iy1), cx = clampi(x, ix0, ix1);
-            const int ty[3] = {max(cy - 1, iy0), cy, min(cy + 1, iy1)};
-            const int tx[3] = {max(cx - 1, ix0), cx, min(cx + 1, ix1)};
-            float r[9];
-#pragma unroll
-            for (int t = 0; t < 9; t++) r[t] = to_float_lut<T>(raw[ty[t / 3] * WW + tx[t % 3]], lut);
-            float a[8];
-#pragma unroll
-            for (int n = 0; n < 8; n++)
+            constexpr int TAIL = G::PADP + NBLK * 128 - WW * WH / 2;  // slots after the window in a plane
+            constexpr int NZ = G::PADP + TAIL;                        // per plane
+            for (int i = tid; i < 2 * NZ; i += THREADS)
             {
-                float s = r[0] * P.k0[n * 9];
-#pragma unroll
-                for (int t = 1; t < 9; t++) s = fmaf(r[t], P.k0[n * 9 + t], s);
-                a[n] = s + P.b0[n];
+                const int pl = i / NZ, k = i - pl * NZ;
+                reinterpret_cast<uint4*>(act + pl * PLANE_BYTES)[k < G::PADP ? k : WW * WH / 2 + k] = make_uint4(0, 0, 0, 0);
             }
-            *slot<G>(act, y * WW + x) = pack8<BF16>(a);
         }
         tc::fence_proxy_async_smem();
         tc::fence_before_sync();
@@ -345,19 +357,19 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
             {
                 // descriptors: A for (block b, tap row dy, half h) = a_desc0 +
                 // 128 b + PPR dy + h; B for (layer l, dy, h) = b_desc0 +
-                // (BL_BYTES (l-1) + 512 (2 dy + h)) / 16
+                // (BL_BYTES l + 512 (2 dy + h)) / 16
                 const uint64_t a_desc0 = tc::smem_desc(tc::smem_u32(act) + (PADP - PPR) * 16, PLANE_BYTES - 16, 128);
                 const uint64_t b_desc0 = tc::smem_desc(tc::smem_u32(smem + B_OFF), 256, 128);
-                for (int l = 1; l <= NL; l++)
+                for (int l = 0; l < NL; l++)
                 {
                     const LayerRange<G> R(l, ix0, ix1, iy0, iy1);
-                    const uint64_t b_desc = b_desc0 + static_cast<uint64_t>(((l - 1) * BL_BYTES) >> 4);
+                    const uint64_t b_desc = b_desc0 + static_cast<uint64_t>((l * BL_BYTES) >> 4);
                     // round barriers: phase of layer l-1 of this tile
-                    const uint32_t rpar = (layers_done + static_cast<uint32_t>(l) - 2u) & 1u;
+                    const uint32_t rpar = (layers_done + static_cast<uint32_t>(l) - 1u) & 1u;
                     for (int r = 0; r < NROUND; r++)
                     {
                         bool ok = true;
-                        if (l >= 2) ok = wait_bar(&round_bar[min(r + 1, NROUND - 1)], rpar, abort_flag);
+                        if (l >= 1) ok = wait_bar(&round_bar[min(r + 1, NROUND - 1)], rpar, abort_flag);
                         tc::fence_after_sync();
                         const int mine = 4 * r + 2 * (warp - NEPI);  // this issuer's two blocks
                         const int lo = max(mine, R.b0), hi = min(mine + 1, R.b1);
@@ -384,14 +396,14 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
         else
         {
             const int q = warp & 3, g = warp >> 2;
-            for (int l = 1; l <= NL; l++)
+            for (int l = 0; l < NL; l++)
             {
-                const uint32_t parity = (layers_done + static_cast<uint32_t>(l) - 1u) & 1u;
+                const uint32_t parity = (layers_done + static_cast<uint32_t>(l)) & 1u;
                 const LayerRange<G> R(l, ix0, ix1, iy0, iy1);
                 float* Hs = reinterpret_cast<float*>(act);  // last layer: the activations are dead once its MMAs completed
                 if constexpr (C > 1)
                 {
-                    if (l == NL)
+                    if (l == LAST)
                     {
                         // the horizontal chroma pass once every layer-8 MMA completed
                         // (the last commit of each issuer)
@@ -412,7 +424,7 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
                         __syncwarp();
                     }
                 }
-                const float* bias = P.bias[l - 1];
+                const float* bias = P.bias[l];
                 for (int rr = 0; rr < NROUND; rr++)
 #pragma unroll
                     for (int k2 = 0; k2 < 2; k2++)
@@ -438,7 +450,7 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
                                 const int p = 2 * r + k;
                                 const int y = p / WW, x = p - y * WW;
                                 if (y < R.ry0 || y > R.ry1 || x < R.rx0 || x > R.rx1) continue;
-                                if (l < NL)
+                                if (l < LAST)
                                 {
                                     const uint4 val = pack8<BF16>(v + 8 * k);
                                     *slot<G>(act, p) = val;

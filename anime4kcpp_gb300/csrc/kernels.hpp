@@ -73,12 +73,13 @@ cudaError_t launch_acnet_legacy_tc2(const AcnetLegacyWeights& wts, const void* p
 void pack_acnet_tc2_weights(const AcnetLegacyWeights& wts, bool bf16, std::vector<uint16_t>& packed);
 
 // Persistent warp-specialised tensor-core form over a tile queue of n images
-// (same type and channel count, every output 2x its input); packed2 as for
-// the pair-interleaved form.  `counter` is a device int (zeroed by the call
+// (same type and channel count, every output 2x its input); packed2 is the
+// device copy of pack_acnet_tc3_weights() (nine layers, layer 0 included).  `counter` is a device int (zeroed by the call
 // on `stream`); `ctas` = SMs' worth of CTAs to launch.
 // `shape` picks the tile geometry (0: 48x44, 1: 64x31, 2: 32x63; the same
 // bytes come out of each) and `per_sm_cap` caps the CTAs per SM (1 or 2).
 constexpr int kTc3Shapes = 3;
+void pack_acnet_tc3_weights(const AcnetLegacyWeights& wts, bool bf16, std::vector<uint16_t>& packed);
 int acnet_tc3_max_images();
 void acnet_tc3_shape(int shape, int* tw, int* th);
 cudaError_t launch_acnet_legacy_tc3(const AcnetLegacyWeights& wts, const void* packed2, bool bf16, int n, const Plane* in,

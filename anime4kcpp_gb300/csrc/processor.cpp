@@ -527,7 +527,7 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
             if (tcKernel_ == 3)
             {
                 // persistent warp-specialised form (default)
-                const void* w = tcWeights(precision_, true);
+                const void* w = tcWeights(precision_, 2);
                 if (!w) err = cudaErrorMemoryAllocation;
                 else if ((err = ts.counter.ensure(256)) == cudaSuccess)
                 {
@@ -547,7 +547,7 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
                 // (16-byte aligned plane) and runs the fused RGB(A) path; other
                 // 1-channel planes take the one-pixel-per-row form.
                 const bool v2 = (tcKernel_ != 1 || in.channels > 1) && acnet_tc2_supported(in);
-                const void* w = tcWeights(precision_, v2);
+                const void* w = tcWeights(precision_, v2 ? 1 : 0);
                 if (!w) err = cudaErrorMemoryAllocation;
                 else if (v2) err = launch_acnet_legacy_tc2(*acnet_, w, bf16, in, out, ph, stream);
                 else if (in.channels == 1) err = launch_acnet_legacy_tc(*acnet_, w, bf16, in, out, stream);
@@ -609,15 +609,16 @@ const void* GB300Processor::arnetWeights(bool bf16)
     return d.ptr;
 }
 
-const void* GB300Processor::tcWeights(Precision p, bool pairForm)
+const void* GB300Processor::tcWeights(Precision p, int form)
 {
     const bool bf16 = p == Precision::BF16;
-    const int idx = (pairForm ? 2 : 0) + (bf16 ? 1 : 0);
+    const int idx = 2 * form + (bf16 ? 1 : 0);
     std::lock_guard<std::mutex> lock(mutex_);
     if (!deviceWeights_[idx].ptr)
     {
         std::vector<uint16_t> packed;
-        if (pairForm) pack_acnet_tc2_weights(*acnet_, bf16, packed);
+        if (form == 2) pack_acnet_tc3_weights(*acnet_, bf16, packed);
+        else if (form == 1) pack_acnet_tc2_weights(*acnet_, bf16, packed);
         else pack_acnet_tc_weights(*acnet_, bf16, packed);
         if (deviceWeights_[idx].ensure(packed.size() * sizeof(uint16_t)) != cudaSuccess) return nullptr;
         if (cudaMemcpy(deviceWeights_[idx].ptr, packed.data(), packed.size() * sizeof(uint16_t), cudaMemcpyHostToDevice) !=
@@ -954,7 +955,7 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
     else
     {
         const bool bf16 = precision_ == Precision::BF16;
-        const void* w = tcWeights(precision_, true);
+        const void* w = tcWeights(precision_, 2);
         if (!w) return fail(ts, "tensor-core weights", cudaErrorMemoryAllocation), false;
         cudaError_t err = ts.counter.ensure(256);
         if (err != cudaSuccess) return fail(ts, "device allocation", err), false;
@@ -1211,7 +1212,7 @@ int GB300Processor::processDeviceNoAlloc(int n, const DeviceImage* src, const De
     const void* w = nullptr;
     {
         std::lock_guard<std::mutex> lock(mutex_);
-        w = deviceWeights_[2 + (bf16 ? 1 : 0)].ptr;
+        w = deviceWeights_[4 + (bf16 ? 1 : 0)].ptr;
     }
     if (!w)
         return rejected("allocation-free call: the tensor-core weights of this precision are not on the device yet; make one "

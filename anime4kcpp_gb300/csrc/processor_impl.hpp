@@ -128,7 +128,9 @@ private:
     bool run(ThreadState& ts, const DeviceImage& src, const DeviceImage& dst, double factor, cudaStream_t stream);
     const ResizeAxis* axis(ThreadState& ts, int n_in, int n_out, int mode, cudaStream_t stream, cudaError_t& err);
     cudaError_t luma_pass(ThreadState& ts, const Plane& in, const Plane& out, const Phase2* ph, cudaStream_t stream);
-    const void* tcWeights(Precision p, bool pairForm);
+    // Packed tensor-core weights on the device: form 0 one pixel per row, 1
+    // pair-interleaved (per-tile kernel), 2 persistent kernel.
+    const void* tcWeights(Precision p, int form);
     const void* arnetWeights(bool bf16);  // packed 8->8 layers of the ARNet / ACNet<8> tensor-core forms
     // Tile shape and CTAs per SM for a persistent launch over these images:
     // forced by AC_GB300_TC3_SHAPE / AC_GB300_TC3_PER_SM, else measured once
@@ -147,7 +149,7 @@ private:
     Precision precision_ = Precision::FP32;
     bool profiling_ = false;
     std::unique_ptr<AcnetLegacyWeights> acnet_;
-    DeviceBuffer deviceWeights_[4];  // TC weights: {one-pixel, pair} x {FP16, BF16}
+    DeviceBuffer deviceWeights_[6];  // TC weights: {one-pixel, pair, persistent} x {FP16, BF16}
     DeviceBuffer arnetPacked_[2];    // ARNet / ACNet<8> 8->8 layers, pair form: FP16, BF16
     bool arnetTc_ = true;            // ARNet / ACNet<8> tensor-core form in FP16/BF16 (AC_GB300_ARNET_TC=0: FP32 pipeline)
     int tc3Ctas_ = 0;                // CTAs of the persistent kernel (0: one per SM; AC_GB300_TC3_CTAS)
