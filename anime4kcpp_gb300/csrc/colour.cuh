@@ -43,6 +43,14 @@ __device__ __forceinline__ void yuv_to_rgb_store(float yy, float u, float v, flo
 {
     u = __fsub_rn(u, 0.5f);
     v = __fsub_rn(v, 0.5f);
+    if constexpr (C == 3 && sizeof(T) < 4)
+    {
+        // integer RGB: the saturation folded into the last rounded operation
+        out[0] = from_unit<T>(add_sat(yy, __fmul_rn(1.403f, v)));
+        out[1] = from_unit<T>(sub_sat(__fsub_rn(yy, __fmul_rn(0.344f, u)), __fmul_rn(0.714f, v)));
+        out[2] = from_unit<T>(add_sat(yy, __fmul_rn(1.773f, u)));
+        return;
+    }
     float r = __fadd_rn(yy, __fmul_rn(1.403f, v));
     float g = __fsub_rn(__fsub_rn(yy, __fmul_rn(0.344f, u)), __fmul_rn(0.714f, v));
     float b = __fadd_rn(yy, __fmul_rn(1.773f, u));
@@ -85,13 +93,26 @@ __device__ __forceinline__ void rgb_to_yuv_q_lut(const T* in, T& yq, T* uvq, con
         g = __fmul_rn(g, a);
         b = __fmul_rn(b, a);
     }
-    const float yy = __fadd_rn(__fadd_rn(__fmul_rn(0.299f, r), __fmul_rn(0.587f, g)), __fmul_rn(0.114f, b));
-    const float u = __fadd_rn(__fmul_rn(0.564f, __fsub_rn(b, yy)), 0.5f);
-    const float v = __fadd_rn(__fmul_rn(0.713f, __fsub_rn(r, yy)), 0.5f);
-    yq = from_float<T>(yy);
-    uvq[0] = from_float<T>(u);
-    uvq[1] = from_float<T>(v);
-    if constexpr (C == 4) uvq[2] = from_float<T>(a);
+    const float ry = __fadd_rn(__fmul_rn(0.299f, r), __fmul_rn(0.587f, g));
+    const float yy = __fadd_rn(ry, __fmul_rn(0.114f, b));
+    if constexpr (sizeof(T) < 4)
+    {
+        // integer outputs: the saturation folded into the last rounded add
+        // (an input alpha is already in [0, 1])
+        yq = from_unit<T>(add_sat(ry, __fmul_rn(0.114f, b)));
+        uvq[0] = from_unit<T>(add_sat(__fmul_rn(0.564f, __fsub_rn(b, yy)), 0.5f));
+        uvq[1] = from_unit<T>(add_sat(__fmul_rn(0.713f, __fsub_rn(r, yy)), 0.5f));
+        if constexpr (C == 4) uvq[2] = from_unit<T>(a);
+    }
+    else
+    {
+        const float u = __fadd_rn(__fmul_rn(0.564f, __fsub_rn(b, yy)), 0.5f);
+        const float v = __fadd_rn(__fmul_rn(0.713f, __fsub_rn(r, yy)), 0.5f);
+        yq = from_float<T>(yy);
+        uvq[0] = from_float<T>(u);
+        uvq[1] = from_float<T>(v);
+        if constexpr (C == 4) uvq[2] = from_float<T>(a);
+    }
 }
 
 // Horizontal pass of the x2 chroma resample for one region row: for output
@@ -132,9 +153,11 @@ __device__ __forceinline__ void merge_block2_h(const float* H, int hpitch, int i
             {
                 float s = 0.0f;
 #pragma unroll
-                for (int t = 0; t < 4; t++)
+                for (int t = 0; t < 3; t++)
                     s = __fadd_rn(s, __fmul_rn(ph.w[dy][t], H[((j + dy + t) * hpitch + 2 * i + k) * UC + c]));
-                q[c] = to_float_lut<T>(encode_resampled<T>(s), lut);
+                const float m = __fmul_rn(ph.w[dy][3], H[((j + dy + 3) * hpitch + 2 * i + k) * UC + c]);
+                if constexpr (sizeof(T) < 4) q[c] = to_float_lut<T>(from_unit<T>(add_sat(s, m)), lut);
+                else q[c] = to_float_lut<T>(encode_resampled<T>(__fadd_rn(s, m)), lut);
             }
             yuv_to_rgb_store<T, C>(to_float_lut<T>(yq[dy][k], lut), q[0], q[1], C == 4 ? q[2] : 1.0f, out + k * C);
         }

@@ -39,6 +39,38 @@ __device__ __forceinline__ T from_float(float v)
     else return static_cast<T>(__float2uint_rz(__fadd_rn(__fmul_rn(s, TypeMax<T>::value), 0.5f)));
 }
 
+// Rounded add / subtract / fused multiply-add whose result is clamped to
+// [0, 1] (PTX .sat).  For non-NaN values this equals rounding and then
+// applying fromFloat's saturation, so fromFloat of such a result needs only
+// the scaling (from_unit).
+__device__ __forceinline__ float add_sat(float a, float b)
+{
+    float r;
+    asm("add.rn.sat.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float sub_sat(float a, float b)
+{
+    float r;
+    asm("sub.rn.sat.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float fma_sat(float a, float b, float c)
+{
+    float r;
+    asm("fma.rn.sat.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// fromFloat of a value already in [0, 1]: (T)(s * max + 0.5f) for unsigned
+// types, s for float.
+template <typename T>
+__device__ __forceinline__ T from_unit(float s)
+{
+    if constexpr (sizeof(T) == 4) return s;
+    else return static_cast<T>(__float2uint_rz(__fadd_rn(__fmul_rn(s, TypeMax<T>::value), 0.5f)));
+}
+
 // The resampler's decode (multiplication by the reciprocal of the maximum).
 template <typename T>
 __device__ __forceinline__ float decode_float(T v)

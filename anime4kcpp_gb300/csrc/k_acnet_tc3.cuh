@@ -40,6 +40,10 @@
 //    the FP32 accumulation of y_hi w_hi + y_lo w_hi + y_hi w_lo carries the
 //    layer at close to FP32 accuracy (the dropped y_lo w_lo term is ~2^-22
 //    relative for FP16 operands).
+//  * The bias rides in the accumulator: before a layer's MMAs the block's
+//    tensor-memory columns hold that layer's bias (written with tcgen05.st
+//    by the epilogue warp that drained the previous layer's accumulator, or
+//    by the prologue for layer 0), and every MMA accumulates onto it.
 //  * Every wait is bounded by %globaltimer; a timeout raises a CTA-wide abort
 //    flag and the status word, all roles fall through their loops without
 //    touching tensor memory, and the CTA frees its tensor memory and exits.
@@ -117,7 +121,7 @@ struct Params
 {
     const uint4* bw;    // NL packed B matrices (pack_acnet_tc3_weights)
     float k2[32];
-    float bias[NL][8];  // layers 0..8, added in the epilogue
+    float bias[NL][8];  // layers 0..8, preloaded into the accumulators
     Phase2 ph;
     int nimg;
     int ntiles;
@@ -333,6 +337,19 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
                 *slot<G>(act, i) = luma_slot<BF16>(to_float_lut<T>(yq, lut));
             }
         }
+        // Layer 0's bias into the accumulators of the blocks this warp drains.
+        if (!mma_warp)
+        {
+            float bv[8];
+#pragma unroll
+            for (int c = 0; c < 8; c++) bv[c] = P.bias[0][c];
+#pragma unroll 1
+            for (int k = 0; k < NBLK / 2; k++)
+                tc::tmem_st16_dup8(tmem + (static_cast<uint32_t>((warp & 3) * 32) << 16) +
+                                       static_cast<uint32_t>((4 * (k >> 1) + (warp >> 2) + 2 * (k & 1)) * 16),
+                                   bv);
+            tc::tmem_wait_st();
+        }
         // The slots around the window (the planes' pads and the unused tail)
         // are read with zero weights by the window's first and last rows;
         // the previous tile's chroma pass may have left non-finite bit
@@ -383,8 +400,7 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
 #pragma unroll
                                     for (int h = 0; h < 2; h++)
                                         tc::mma_f16(d, a_desc + static_cast<uint64_t>(dy * PPR + h),
-                                                    b_desc + static_cast<uint64_t>((2 * dy + h) * 32), IDESC,
-                                                    (dy | h) ? 1u : 0u);
+                                                    b_desc + static_cast<uint64_t>((2 * dy + h) * 32), IDESC, 1u);
                             }
                         tc::mma_commit(&mma_bar[mine]);
                         tc::mma_commit(&mma_bar[mine + 1]);
@@ -424,7 +440,6 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
                         __syncwarp();
                     }
                 }
-                const float* bias = P.bias[l];
                 for (int rr = 0; rr < NROUND; rr++)
 #pragma unroll
                     for (int k2 = 0; k2 < 2; k2++)
@@ -439,10 +454,18 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
                         if (done && b >= R.b0 && b <= R.b1)
                         {
                             float v[16];
-                            tc::tmem_ld16(tmem + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(b * 16), v);
+                            const uint32_t ta = tmem + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(b * 16);
+                            tc::tmem_ld16(ta, v);
                             tc::tmem_wait_ld();
+                            if (l < LAST)
+                            {
+                                // the next layer's bias into the drained accumulator
+                                float nb[8];
 #pragma unroll
-                            for (int c = 0; c < 16; c++) v[c] += bias[c & 7];
+                                for (int c = 0; c < 8; c++) nb[c] = P.bias[l + 1][c];
+                                tc::tmem_st16_dup8(ta, nb);
+                                tc::tmem_wait_st();
+                            }
                             const int r = b * 128 + q * 32 + lane;
 #pragma unroll
                             for (int k = 0; k < 2; k++)
@@ -487,8 +510,9 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
                                             const int ko = 8 * (dy * 2 + dx);
                                             float d = s[0] * P.k2[ko];
 #pragma unroll
-                                            for (int c = 1; c < 8; c++) d = fmaf(s[c], P.k2[ko + c], d);
-                                            o[dy][dx] = from_float<T>(d);
+                                            for (int c = 1; c < 7; c++) d = fmaf(s[c], P.k2[ko + c], d);
+                                            if constexpr (sizeof(T) < 4) o[dy][dx] = from_unit<T>(fma_sat(s[7], P.k2[ko + 7], d));
+                                            else o[dy][dx] = from_float<T>(fmaf(s[7], P.k2[ko + 7], d));
                                         }
                                     const int ox = 2 * (gx0 + x), oy = 2 * (gy0 + y);
                                     T* row0 = row_ptr_w<T>(I.out.ptr, I.out.pitch, oy) + ox * C;
