@@ -164,6 +164,169 @@ __device__ __forceinline__ void merge_block2_h(const float* H, int hpitch, int i
     }
 }
 
+// Both phases of the horizontal pass for source column i of one region row
+// (outputs 2i and 2i + 1): taps i .. i + 4 decoded once, each sum ascending as
+// in chroma_hpass.  h_out receives 2 x UC floats (phase 0, then phase 1).
+template <typename T, int UC>
+__device__ __forceinline__ void chroma_hpass2(const T* uv_row, int i, const Phase2& ph, float* h_out)
+{
+    float d[5][UC];
+    if constexpr (sizeof(T) == 1 && UC == 2)
+    {
+        // the row's UV pairs are 2-byte aligned: one 16-bit load per tap
+        const uint16_t* p = reinterpret_cast<const uint16_t*>(uv_row) + i;
+#pragma unroll
+        for (int t = 0; t < 5; t++)
+        {
+            const uint32_t v = p[t];
+            d[t][0] = decode_float<T>(static_cast<T>(v & 0xFFu));
+            d[t][1] = decode_float<T>(static_cast<T>(v >> 8));
+        }
+    }
+    else
+    {
+#pragma unroll
+        for (int t = 0; t < 5; t++)
+#pragma unroll
+            for (int c = 0; c < UC; c++) d[t][c] = decode_float<T>(uv_row[(i + t) * UC + c]);
+    }
+    float o[2 * UC];
+#pragma unroll
+    for (int k = 0; k < 2; k++)
+#pragma unroll
+        for (int c = 0; c < UC; c++)
+        {
+            float s = 0.0f;
+#pragma unroll
+            for (int t = 0; t < 4; t++) s = __fadd_rn(s, __fmul_rn(ph.w[k][t], d[k + t][c]));
+            o[k * UC + c] = s;
+        }
+    if constexpr (UC == 2)
+        *reinterpret_cast<float4*>(h_out) = make_float4(o[0], o[1], o[2], o[3]);  // 16-byte aligned (2i even)
+    else
+    {
+#pragma unroll
+        for (int c = 0; c < 2 * UC; c++) h_out[c] = o[c];
+    }
+}
+
+// Bytes of one output row's two pixels (2 x C elements of T) written at `dst`:
+// with `wide` (the row start is aligned to the widest store used) in 2-3
+// aligned stores, else element by element.
+template <typename T, int C>
+__device__ __forceinline__ void store_px2(T* dst, const T (&v)[2 * C], bool wide)
+{
+    if (wide)
+    {
+        if constexpr (sizeof(T) == 1 && C == 3)
+        {
+            // 6 bytes at a 2-byte aligned address (6 x is even)
+            const uint32_t b01 = v[0] | (v[1] << 8), b23 = v[2] | (v[3] << 8), b45 = v[4] | (v[5] << 8);
+            if ((reinterpret_cast<uintptr_t>(dst) & 3u) == 0)
+            {
+                *reinterpret_cast<uint32_t*>(dst) = b01 | (b23 << 16);
+                *reinterpret_cast<uint16_t*>(dst + 4) = static_cast<uint16_t>(b45);
+            }
+            else
+            {
+                *reinterpret_cast<uint16_t*>(dst) = static_cast<uint16_t>(b01);
+                *reinterpret_cast<uint32_t*>(dst + 2) = b23 | (b45 << 16);
+            }
+            return;
+        }
+        else if constexpr (sizeof(T) == 1 && C == 4)
+        {
+            *reinterpret_cast<uint2*>(dst) = make_uint2(v[0] | (v[1] << 8) | (v[2] << 16) | (static_cast<uint32_t>(v[3]) << 24),
+                                                        v[4] | (v[5] << 8) | (v[6] << 16) | (static_cast<uint32_t>(v[7]) << 24));
+            return;
+        }
+        else if constexpr (sizeof(T) == 2 && C == 3)
+        {
+            uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+            d[0] = v[0] | (static_cast<uint32_t>(v[1]) << 16);
+            d[1] = v[2] | (static_cast<uint32_t>(v[3]) << 16);
+            d[2] = v[4] | (static_cast<uint32_t>(v[5]) << 16);
+            return;
+        }
+        else if constexpr (sizeof(T) == 2 && C == 4)
+        {
+            uint2* d = reinterpret_cast<uint2*>(dst);
+            d[0] = make_uint2(v[0] | (static_cast<uint32_t>(v[1]) << 16), v[2] | (static_cast<uint32_t>(v[3]) << 16));
+            d[1] = make_uint2(v[4] | (static_cast<uint32_t>(v[5]) << 16), v[6] | (static_cast<uint32_t>(v[7]) << 16));
+            return;
+        }
+        else if constexpr (sizeof(T) == 4)
+        {
+            float2* d = reinterpret_cast<float2*>(dst);
+#pragma unroll
+            for (int k = 0; k < C; k++) d[k] = make_float2(v[2 * k], v[2 * k + 1]);
+            return;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 2 * C; k++) dst[k] = v[k];
+}
+
+// Alignment of a row start that store_px2 needs for its wide stores.
+template <typename T, int C>
+__host__ __device__ constexpr unsigned store_px2_align()
+{
+    return sizeof(T) == 1 ? (C == 3 ? 4u : 8u) : (sizeof(T) == 2 ? (C == 3 ? 4u : 8u) : 8u);
+}
+
+// merge_block2_h with the same arithmetic, loading each of the five H rows
+// the 2x2 block needs once (both columns and all channels together) and
+// storing each output row's two pixels with store_px2.
+template <typename T, int C>
+__device__ __forceinline__ void merge_block2_hv(const float* H, int hpitch, int i, int j, const Phase2& ph,
+                                                const T (&yq)[2][2], T* out0, T* out1, bool wide, const float* lut)
+{
+    constexpr int UC = C - 1;
+    float h[5][2][UC];
+#pragma unroll
+    for (int t = 0; t < 5; t++)
+    {
+        const float* row = H + ((j + t) * hpitch + 2 * i) * UC;
+        if constexpr (UC == 2)
+        {
+            const float4 q = *reinterpret_cast<const float4*>(row);  // 16-byte aligned (2i even)
+            h[t][0][0] = q.x;
+            h[t][0][1] = q.y;
+            h[t][1][0] = q.z;
+            h[t][1][1] = q.w;
+        }
+        else
+        {
+#pragma unroll
+            for (int k = 0; k < 2; k++)
+#pragma unroll
+                for (int c = 0; c < UC; c++) h[t][k][c] = row[k * UC + c];
+        }
+    }
+#pragma unroll
+    for (int dy = 0; dy < 2; dy++)
+    {
+        T px[2 * C];
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+        {
+            float q[UC];
+#pragma unroll
+            for (int c = 0; c < UC; c++)
+            {
+                float s = 0.0f;
+#pragma unroll
+                for (int t = 0; t < 3; t++) s = __fadd_rn(s, __fmul_rn(ph.w[dy][t], h[dy + t][k][c]));
+                const float m = __fmul_rn(ph.w[dy][3], h[dy + 3][k][c]);
+                if constexpr (sizeof(T) < 4) q[c] = to_float_lut<T>(from_unit<T>(add_sat(s, m)), lut);
+                else q[c] = to_float_lut<T>(encode_resampled<T>(__fadd_rn(s, m)), lut);
+            }
+            yuv_to_rgb_store<T, C>(to_float_lut<T>(yq[dy][k], lut), q[0], q[1], C == 4 ? q[2] : 1.0f, px + k * C);
+        }
+        store_px2<T, C>(dy ? out1 : out0, px, wide);
+    }
+}
+
 // The 2x2 output block of source pixel (cx, cy): luma yq[dy][dx] (already
 // quantised) merged with the chroma of a UV(A) region `uv` (UC channels of
 // type T per pixel, `pitch` pixels per row; (cx, cy) in region coordinates

@@ -292,6 +292,9 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
         const int ix0 = max(0, -gx0), ix1 = min(WW - 1, W - 1 - gx0);
         const int iy0 = max(0, -gy0), iy1 = min(WH - 1, H - 1 - gy0);
         const bool edges = ix0 > 0 || ix1 < WW - 1 || iy0 > 0 || iy1 < WH - 1;  // an image edge inside the window
+        // output rows aligned for the colour epilogue's wide stores
+        const bool wide = ((reinterpret_cast<uintptr_t>(I.out.ptr) | static_cast<uintptr_t>(I.out.pitch)) &
+                           (store_px2_align<T, C>() - 1)) == 0;
 
         // ---- prologue (all warps): window luma as layer-0 input slots (+ chroma region) ----
         // Loads are issued in batches of four pixels per thread before any
@@ -427,10 +430,11 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
                         for (int i = 0; i < NISS; i++) last = wait_bar(&mma_bar[NBLK - 3 + 2 * i], parity, abort_flag) && last;
                         const bool ok = __all_sync(0xffffffffu, last ? 1 : 0);
                         if (ok)
-                            for (int e = tid; e < UVH * 2 * TW; e += NEPI * 32)
+                            for (int e = tid; e < UVH * TW; e += NEPI * 32)
                             {
-                                const int r = e / (2 * TW), ox = e - r * (2 * TW);
-                                chroma_hpass<T, C - 1>(uvs + r * UVW * (C - 1), ox >> 1, ox & 1, P.ph, Hs + e * (C - 1));
+                                // both phases of source column i of region row r
+                                const int r = e / TW, i = e - r * TW;
+                                chroma_hpass2<T, C - 1>(uvs + r * UVW * (C - 1), i, P.ph, Hs + (r * 2 * TW + 2 * i) * (C - 1));
                             }
                         // bounded barrier of the epilogue warps
                         __syncwarp();
@@ -524,7 +528,7 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
                                         row1[0] = o[1][0];
                                         row1[1] = o[1][1];
                                     }
-                                    else merge_block2_h<T, C>(Hs, 2 * TW, x - HALO, y - HALO, P.ph, o, row0, row1, lut);
+                                    else merge_block2_hv<T, C>(Hs, 2 * TW, x - HALO, y - HALO, P.ph, o, row0, row1, wide, lut);
                                 }
                             }
                         }

@@ -128,6 +128,10 @@ private:
     bool run(ThreadState& ts, const DeviceImage& src, const DeviceImage& dst, double factor, cudaStream_t stream);
     const ResizeAxis* axis(ThreadState& ts, int n_in, int n_out, int mode, cudaStream_t stream, cudaError_t& err);
     cudaError_t luma_pass(ThreadState& ts, const Plane& in, const Plane& out, const Phase2* ph, cudaStream_t stream);
+    // Kernel timing (setProfiling): an event pair recorded around one launch
+    // on its stream, with the output pixels it produced.
+    std::pair<cudaEvent_t, cudaEvent_t> profileBegin(ThreadState& ts, cudaStream_t stream);
+    void profileEnd(ThreadState& ts, std::pair<cudaEvent_t, cudaEvent_t> ev, cudaStream_t stream, double outPixels);
     // Packed tensor-core weights on the device: form 0 one pixel per row, 1
     // pair-interleaved (per-tile kernel), 2 persistent kernel.
     const void* tcWeights(Precision p, int form);

@@ -1,7 +1,10 @@
 """Run one upscale of a seeded synthetic frame through the device-pointer
-entry point, a fixed number of times (used for kernel profiling).
+entry point, a fixed number of times (used for kernel profiling); with
+--batch N, N such frames per call through the batch entry point (one
+persistent launch per call in the tensor-core forms).
 
     python -m anime4kcpp_gb300.run_once --form fp16 --size 1920x1080 --channels 3 --repeat 2
+    python -m anime4kcpp_gb300.run_once --form fp16 --size 1920x1080 --channels 3 --batch 8 --repeat 2
 """
 import argparse
 
@@ -16,6 +19,7 @@ def main():
     ap.add_argument("--channels", type=int, default=3, choices=[1, 3, 4])
     ap.add_argument("--factor", type=float, default=2.0)
     ap.add_argument("--repeat", type=int, default=2)
+    ap.add_argument("--batch", type=int, default=0, help="frames per call through the batch entry point (0: single)")
     a = ap.parse_args()
     import torch
 
@@ -28,11 +32,16 @@ def main():
     else:
         x = synthetic.rgb_u8(h, w, seed=1, alpha=a.channels == 4)
     ow, oh = ac.output_shape(w, h, a.channels, a.factor)
-    src = torch.from_numpy(x).cuda()
-    dst = torch.empty((oh, ow) + ((a.channels,) if a.channels > 1 else ()), dtype=torch.uint8, device="cuda")
+    n = max(1, a.batch)
+    srcs = [torch.from_numpy(np.roll(x, 7 * i, axis=1).copy()).cuda() for i in range(n)]
+    dsts = [torch.empty((oh, ow) + ((a.channels,) if a.channels > 1 else ()), dtype=torch.uint8, device="cuda")
+            for _ in range(n)]
     p = ac.Processor("cuda", 0, a.model, precision=a.form)
     for _ in range(a.repeat):
-        p.process_device(src, dst, a.factor)
+        if a.batch:
+            p.process_batch_device(srcs, dsts, a.factor)
+        else:
+            p.process_device(srcs[0], dsts[0], a.factor)
     torch.cuda.synchronize()
     print("ok", a.form, a.size, a.channels, "launches", ac.launch_count())
 

@@ -8,8 +8,11 @@ frames per step, two alternating batches of 8 so each step's 50 MB of input
 and 200 MB of output exceed the 129 MB L2.  Inputs are seeded synthetic
 Voronoi-edge images (no public dataset is attached to this workload).
 
-  value  output Mpx/s with inputs resident in HBM (device-pointer entry point,
-         CUDA events on the launching stream)
+  value  output Mpx/s with inputs resident in HBM, CUDA events on the
+         launching stream: the 8 frames of a step as one persistent launch
+         (batch entry point) in the tensor-core forms; each frame's own
+         launch (device-pointer entry point) is reported beside it
+         ("per_frame_launch"), and the FP32 form runs frame by frame
   e2e    the same metric through the C ABI with pinned host buffers, H2D and
          D2H copies inside the timed region (several host threads share one
          processor, as the reference CLI does)
@@ -194,7 +197,7 @@ def run_reference(args, rank):
     }
 
 
-def time_device(ac, torch, proc, srcs, dsts, frames, steps, warmup, profile=False, clocks=None):
+def time_device(ac, torch, proc, srcs, dsts, frames, steps, warmup, profile=False, clocks=None, batched=False):
     # A dedicated stream: the kernels and the timing events share it.
     stream = torch.cuda.Stream()
     handle = stream.cuda_stream
@@ -202,6 +205,10 @@ def time_device(ac, torch, proc, srcs, dsts, frames, steps, warmup, profile=Fals
 
     def step(i):
         b = i % nb
+        if batched:
+            proc.process_batch_device(srcs[b * frames:(b + 1) * frames], dsts[b * frames:(b + 1) * frames], FACTOR,
+                                      stream=handle, sync=False)
+            return
         for j in range(frames):
             proc.process_device(srcs[b * frames + j], dsts[b * frames + j], FACTOR, stream=handle, sync=False)
 
@@ -561,12 +568,20 @@ def run_gb300(args, rank, world, local_rank):
         is_head = headline is None
         sampler = ClockSampler(local_rank) if is_head else None
         steps = args.steps if is_head else max(3, args.steps // 2)
+        batched = form != "fp32" and not args.per_frame
         ms, launches, prof = time_device(ac, torch, proc, srcs, dsts, frames, steps, args.warmup, profile=True,
-                                         clocks=sampler)
+                                         clocks=sampler, batched=batched)
         out_px = OW * OH * frames * steps
         rec = {"value": out_px / (ms / 1e3) / 1e6, "ms_per_step": ms / steps, "launches": launches,
                "kernel_ms_per_launch": prof[0] / max(prof[1], 1), "kernel_launches": prof[1],
-               "kernel_out_px": prof[2], "steps": steps}
+               "kernel_out_px": prof[2], "steps": steps, "launch": "one per step (8 frames)" if batched else "one per frame"}
+        if batched:
+            # the same frames, each in its own launch
+            pms, plaunches, pprof = time_device(ac, torch, proc, srcs, dsts, frames, max(3, steps // 2), args.warmup,
+                                                profile=True)
+            psteps = max(3, steps // 2)
+            rec["per_frame_launch"] = {"value": OW * OH * frames * psteps / (pms / 1e3) / 1e6, "ms_per_step": pms / psteps,
+                                       "launches": plaunches, "kernel_ms_per_launch": pprof[0] / max(pprof[1], 1)}
         forms[form] = rec
         if is_head:
             headline = (form, proc, rec, sampler)
@@ -623,7 +638,7 @@ def run_gb300(args, rank, world, local_rank):
         "warmup": args.warmup, "ms_per_step": rec["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32" if form == "fp32" else ("f16" if form == "fp16" else "bf16"),
         "data": DATA,
-        "config": {"workload": WORKLOAD, "frames_per_step": frames, "form": form,
+        "config": {"workload": WORKLOAD, "frames_per_step": frames, "form": form, "launch": rec["launch"],
                    "l2": "inputs larger than L2: 2 alternating batches of 8 distinct frames (50 MB in, 200 MB out per step)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_value, "unit": "Mpx/s", "h2d_bytes_per_step": H * W * 3 * frames,
@@ -658,7 +673,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--frames", type=int, default=8)
     ap.add_argument("--forms", default="fp16,fp32,bf16")
-    ap.add_argument("--e2e-threads", type=int, default=4)
+    ap.add_argument("--e2e-threads", type=int, default=8)
+    ap.add_argument("--per-frame", action="store_true", help="time the tensor-core forms one launch per frame")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-image batching workload")
