@@ -877,7 +877,11 @@ void GB300Processor::processHost(const Image& src, Image& dst, double factor)
     cudaStream_t stream = ts.stream;
     cudaError_t err;
     const int es = src.elementSize();
-    DeviceImage dsrc{nullptr, src.width(), src.height(), src.channels(), align_pitch(src.width() * src.pixelSize()), src.type()};
+    // The device copy of the source keeps the caller's row stride when it is
+    // 16-byte aligned, so the upload is one contiguous copy.
+    const int srcRow = src.width() * src.pixelSize();
+    const int devPitch = (src.stride() % 16 == 0 && src.stride() >= srcRow) ? src.stride() : align_pitch(srcRow);
+    DeviceImage dsrc{nullptr, src.width(), src.height(), src.channels(), devPitch, src.type()};
     DeviceImage ddst{nullptr, ow, oh, src.channels(), align_pitch(ow * src.channels() * es), src.type()};
     if ((err = ts.src.ensure(static_cast<size_t>(dsrc.stride) * dsrc.h)) != cudaSuccess) { fail(ts, "device allocation", err); return; }
     if ((err = ts.out.ensure(static_cast<size_t>(ddst.stride) * ddst.h)) != cudaSuccess) { fail(ts, "device allocation", err); return; }

@@ -249,30 +249,43 @@ class _Null:
 
 
 def time_e2e(ac, torch, proc, frames_host, outs_host, frames, steps, warmup, threads):
-    """Host API: every call copies its frame in, runs, copies the result out."""
-    per = frames // threads
+    """Host API: every call copies its frame in, runs, copies the result out.
+    `threads` host threads (started before the clock) take the frames of all
+    steps in order from a shared counter, as the reference CLI's thread pool
+    takes images, so one step's copies overlap the next step's kernels; the
+    timed region ends when every frame's result is in its host buffer."""
+    import itertools
 
-    def step_worker(t, i, errs):
-        for j in range(per):
-            k = (i % 2) * frames + t * per + j
-            proc.process(frames_host[k], FACTOR, dst=outs_host[k])
-            if not proc.ok():
-                errs.append(proc.error())
-
-    def step(i):
+    def run(nsteps):
+        total = nsteps * frames
+        counter = itertools.count()
         errs = []
-        ts = [threading.Thread(target=step_worker, args=(t, i, errs)) for t in range(threads)]
+        go = threading.Event()
+
+        def worker():
+            go.wait()
+            while True:
+                k = next(counter)
+                if k >= total:
+                    return
+                i, j = divmod(k, frames)
+                idx = (i % 2) * frames + j
+                proc.process(frames_host[idx], FACTOR, dst=outs_host[idx])
+                if not proc.ok():
+                    errs.append(proc.error())
+
+        ts = [threading.Thread(target=worker) for _ in range(threads)]
         [t.start() for t in ts]
+        t0 = time.perf_counter()
+        go.set()
         [t.join() for t in ts]
+        el = time.perf_counter() - t0
         if errs:
             raise RuntimeError(errs[0])
+        return el
 
-    for i in range(warmup):
-        step(i)
-    t0 = time.perf_counter()
-    for i in range(steps):
-        step(i)
-    return time.perf_counter() - t0
+    run(warmup)
+    return run(steps)
 
 
 BATCH_MODEL = "acnet-legacy-hdn1"
