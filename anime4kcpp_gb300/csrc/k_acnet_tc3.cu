@@ -156,6 +156,18 @@ cudaError_t launch_acnet_legacy_tc3_noalloc(const AcnetLegacyWeights& wts, const
     return launch_tc3(wts, packed2, bf16, n, in, out, phase2, s, s + 1, ctas, stream, 0, 2);
 }
 
+// The quad kernel's launch over the same scratch (counter and status word).
+cudaError_t launch_acnet_legacy_tc4_noalloc(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n,
+                                            const Plane* in, const Plane* out, const Phase2* phase2, int ctas,
+                                            cudaStream_t stream)
+{
+    int* s = nullptr;
+    cudaError_t err = noalloc_scratch(&s);
+    if (err != cudaSuccess) return err;
+    if ((err = cudaMemsetAsync(s, 0, 2 * sizeof(int), stream)) != cudaSuccess) return err;
+    return launch_acnet_legacy_tc4_core(wts, packed4, bf16, n, in, out, phase2, s, s + 1, ctas, stream, 2);
+}
+
 // Status word of the allocation-free launches on the current device: 0, or
 // 1 when a bounded wait gave up.  Read it after the stream synchronised.
 cudaError_t acnet_tc3_noalloc_status(int* value)

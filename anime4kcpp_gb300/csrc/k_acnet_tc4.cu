@@ -1,0 +1,139 @@
+// Host side of the quad tensor-core ACNetLegacy kernel (k_acnet_tc4.cuh):
+// the B-matrix packing and the launcher.
+#include <cstring>
+#include <vector>
+
+#include "k_acnet_tc4.cuh"
+
+namespace acgb {
+
+int* tc_status_buffer();
+
+namespace {
+
+uint16_t bits16(float v, bool bf16)
+{
+    if (bf16)
+    {
+        uint32_t u;
+        std::memcpy(&u, &v, 4);
+        return static_cast<uint16_t>((u + 0x7FFFu + ((u >> 16) & 1u)) >> 16);
+    }
+    return __half_as_ushort(__float2half_rn(v));
+}
+
+// One layer of 3x3 8->8 weights k[n * 72 + tap * 8 + c] (reference NHWC
+// order) as the nine N32 x K16 B chunks of the quad GEMM.  Chunk 3 dy + j
+// multiplies tap row dy; its K halves hold the 8 channels of the input
+// pixels at offsets (0, -1), (+1, +2), (+4, +3) from the row's first pixel
+// 4r for j = 0, 1, 2.  Output column n is pixel 4r + n / 8, channel n % 8;
+// input offset o feeds output pixel k through tap dx = o - k + 1 (zero
+// weight outside 0..2).  Bytes of element (n, kk) in a chunk: (kk / 8) 512 +
+// (n / 8) 128 + (n % 8) 16 + (kk % 8) 2 (K-major, no swizzle, leading byte
+// offset 512, stride byte offset 128).
+void pack_quad_conv8(const float* k, bool bf16, uint16_t* out)
+{
+    static const int off[3][2] = {{0, -1}, {1, 2}, {4, 3}};
+    std::memset(out, 0, tcv4::BL_BYTES);
+    for (int dy = 0; dy < 3; dy++)
+        for (int j = 0; j < 3; j++)
+        {
+            uint16_t* ch = out + (3 * dy + j) * (tcv4::CHUNK_BYTES / 2);
+            for (int n = 0; n < 32; n++)
+                for (int kk = 0; kk < 16; kk++)
+                {
+                    const int dx = off[j][kk >> 3] - (n >> 3) + 1;
+                    if (dx < 0 || dx > 2) continue;
+                    const float w = k[(n & 7) * 72 + (dy * 3 + dx) * 8 + (kk & 7)];
+                    ch[((kk >> 3) * 512 + (n >> 3) * 128 + (n & 7) * 16 + (kk & 7) * 2) / 2] = bits16(w, bf16);
+                }
+        }
+}
+
+}  // namespace
+
+int acnet_tc4_max_images() { return tcv4::kMaxImages; }
+
+void acnet_tc4_shape(int* tw, int* th)
+{
+    *tw = tcv4::Geo0::TW;
+    *th = tcv4::Geo0::TH;
+}
+
+// Layer 0 as an 8-channel layer over the input slots (y_hi, y_lo, y_hi) with
+// weights (w_hi, w_hi, w_lo), then the eight 3x3 8->8 layers.
+void pack_acnet_tc4_weights(const AcnetLegacyWeights& w, bool bf16, std::vector<uint16_t>& packed)
+{
+    using namespace tcv4;
+    packed.assign(static_cast<size_t>(NL) * BL_BYTES / 2, 0);
+    auto round16 = [bf16](float v) {
+        return bf16 ? __bfloat162float(__float2bfloat16_rn(v)) : __half2float(__float2half_rn(v));
+    };
+    std::vector<float> k0(576, 0.0f);
+    for (int n = 0; n < 8; n++)
+        for (int t = 0; t < 9; t++)
+        {
+            const float v = w.k[n * 9 + t];
+            const float hi = round16(v);
+            k0[n * 72 + t * 8 + 0] = hi;
+            k0[n * 72 + t * 8 + 1] = hi;
+            k0[n * 72 + t * 8 + 2] = v - hi;
+        }
+    pack_quad_conv8(k0.data(), bf16, packed.data());
+    for (int l = 1; l < NL; l++)
+        pack_quad_conv8(w.k + 72 + 576 * (l - 1), bf16, packed.data() + static_cast<size_t>(l) * BL_BYTES / 2);
+}
+
+// One persistent launch over all tiles of n images (same element type and
+// channel count; each output exactly 2x its input).  `counter` is a device
+// int the call zeroes on `stream`, `status` the word a timed-out wait sets;
+// `ctas` SMs' worth of CTAs drain the queue.
+cudaError_t launch_acnet_legacy_tc4_core(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n, const Plane* in,
+                                         const Plane* out, const Phase2* phase2, int* counter, int* status, int ctas,
+                                         cudaStream_t stream, int per_sm_cap)
+{
+    using namespace tcv4;
+    if (n <= 0) return cudaSuccess;
+    if (n > kMaxImages || !packed4 || !counter || !status || ctas <= 0) return cudaErrorInvalidValue;
+    const int c = in[0].channels, type = in[0].type;
+    if (c > 1 && !phase2) return cudaErrorInvalidValue;
+    Params p;
+    std::memset(&p, 0, sizeof(p));
+    p.bw = static_cast<const uint4*>(packed4);
+    for (int i = 0; i < 32; i++) p.k2[i] = wts.k[72 + 576 * 8 + i];
+    for (int l = 0; l < NL; l++)
+        for (int k = 0; k < 8; k++) p.bias[l][k] = wts.b[8 * l + k];
+    if (phase2) p.ph = *phase2;
+    constexpr int TW = Geo0::TW, TH = Geo0::TH;
+    int tiles = 0;
+    for (int i = 0; i < n; i++)
+    {
+        if (in[i].channels != c || in[i].type != type || in[i].w <= 0 || in[i].h <= 0) return cudaErrorInvalidValue;
+        p.img[i].in = in[i];
+        p.img[i].out = out[i];
+        p.img[i].tiles_x = (in[i].w + TW - 1) / TW;
+        p.img[i].tile0 = tiles;
+        tiles += p.img[i].tiles_x * ((in[i].h + TH - 1) / TH);
+    }
+    p.nimg = n;
+    p.ntiles = tiles;
+    p.tile_counter = counter;
+    p.status = status;
+    cudaError_t err = cudaMemsetAsync(counter, 0, sizeof(int), stream);
+    if (err != cudaSuccess) return err;
+    const int grid = tiles < ctas ? tiles : ctas;
+    err = launch_shape<Geo0>(type, c, bf16, p, grid, per_sm_cap, stream);
+    if (err == cudaSuccess) count_launch();
+    return err;
+}
+
+cudaError_t launch_acnet_legacy_tc4(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n, const Plane* in,
+                                    const Plane* out, const Phase2* phase2, int* counter, int ctas, cudaStream_t stream,
+                                    int per_sm_cap)
+{
+    int* status = tc_status_buffer();
+    if (!status) return cudaErrorMemoryAllocation;
+    return launch_acnet_legacy_tc4_core(wts, packed4, bf16, n, in, out, phase2, counter, status, ctas, stream, per_sm_cap);
+}
+
+}  // namespace acgb

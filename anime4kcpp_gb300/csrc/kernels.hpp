@@ -94,6 +94,27 @@ cudaError_t launch_acnet_legacy_tc3_noalloc(const AcnetLegacyWeights& wts, const
                                             cudaStream_t stream);
 cudaError_t acnet_tc3_noalloc_status(int* value);
 
+// Quad form of the persistent kernel: four pixels per GEMM row (N = 32), one
+// 46x46 tile shape, B matrices streamed per layer; `packed4` is the device
+// copy of pack_acnet_tc4_weights().  Same arguments and output bytes
+// contract as launch_acnet_legacy_tc3 (results agree within the FP16/BF16
+// tolerance; the MMA accumulation order differs).
+int acnet_tc4_max_images();
+void acnet_tc4_shape(int* tw, int* th);
+void pack_acnet_tc4_weights(const AcnetLegacyWeights& wts, bool bf16, std::vector<uint16_t>& packed);
+cudaError_t launch_acnet_legacy_tc4(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n, const Plane* in,
+                                    const Plane* out, const Phase2* phase2, int* counter, int ctas, cudaStream_t stream,
+                                    int per_sm_cap = 2);
+// The same with the caller's status word (`status`, 0 or 1 after a timed-out wait).
+cudaError_t launch_acnet_legacy_tc4_core(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n, const Plane* in,
+                                         const Plane* out, const Phase2* phase2, int* counter, int* status, int ctas,
+                                         cudaStream_t stream, int per_sm_cap);
+// The quad launch with its tile counter and status word in the static
+// scratch of the allocation-free entry (see launch_acnet_legacy_tc3_noalloc).
+cudaError_t launch_acnet_legacy_tc4_noalloc(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n,
+                                            const Plane* in, const Plane* out, const Phase2* phase2, int ctas,
+                                            cudaStream_t stream);
+
 // RGB(A) -> Y + UV(A) (rgb2yuv / rgba2yuva of core/src/ImageProcess.cpp).
 cudaError_t launch_rgb2yuv_split(const Plane& rgb, const Plane& y, const Plane& uv, cudaStream_t stream);
 // Interleaved 3/4-channel RGB(A) -> interleaved YUV(A) in place or not.

@@ -252,7 +252,7 @@ GB300Processor::GB300Processor(int device, const ModelSpec& spec) : spec_(spec)
     if (const char* k = std::getenv("AC_GB300_TC_KERNEL"))
     {
         const int v = std::atoi(k);
-        tcKernel_ = (v == 1 || v == 2) ? v : 3;
+        tcKernel_ = (v >= 1 && v <= 3) ? v : 4;
     }
     if (const char* f = std::getenv("AC_GB300_FUSED")) fused_ = std::atoi(f) != 0;
     if (const char* n = std::getenv("AC_GB300_TC3_CTAS")) tc3Ctas_ = std::atoi(n);
@@ -536,7 +536,20 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
         else
         {
             const bool bf16 = precision_ == Precision::BF16;
-            if (tcKernel_ == 3)
+            if (tcKernel_ == 4)
+            {
+                // persistent quad form (one tile shape, no autotune)
+                const void* w = tcWeights(precision_, 3);
+                if (!w) err = cudaErrorMemoryAllocation;
+                else if ((err = ts.counter.ensure(256)) == cudaSuccess)
+                {
+                    int* counter = static_cast<int*>(ts.counter.ptr) + (ts.counterSlot++ & 63);
+                    err = launch_acnet_legacy_tc4(*acnet_, w, bf16, 1, &in, &out, ph, counter,
+                                                  tc3Ctas_ > 0 ? tc3Ctas_ : smCount_, stream,
+                                                  tc3PerSm_ > 0 ? tc3PerSm_ : 2);
+                }
+            }
+            else if (tcKernel_ == 3)
             {
                 // persistent warp-specialised form (default)
                 const void* w = tcWeights(precision_, 2);
@@ -624,7 +637,8 @@ const void* GB300Processor::tcWeights(Precision p, int form)
     if (!deviceWeights_[idx].ptr)
     {
         std::vector<uint16_t> packed;
-        if (form == 2) pack_acnet_tc3_weights(*acnet_, bf16, packed);
+        if (form == 3) pack_acnet_tc4_weights(*acnet_, bf16, packed);
+        else if (form == 2) pack_acnet_tc3_weights(*acnet_, bf16, packed);
         else if (form == 1) pack_acnet_tc2_weights(*acnet_, bf16, packed);
         else pack_acnet_tc_weights(*acnet_, bf16, packed);
         if (deviceWeights_[idx].ensure(packed.size() * sizeof(uint16_t)) != cudaSuccess) return nullptr;
@@ -934,7 +948,7 @@ int GB300Processor::processDevice(const DeviceImage& src, const DeviceImage& dst
 bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, const DeviceImage* dst, double factor,
                               cudaStream_t s)
 {
-    const bool tcBatch = spec_.family == Family::ACNetLegacy && precision_ != Precision::FP32 && tcKernel_ == 3 && fused_;
+    const bool tcBatch = spec_.family == Family::ACNetLegacy && precision_ != Precision::FP32 && tcKernel_ >= 3 && fused_;
     bool gray4 = tcBatch && factor == 4.0 && n > 0;
     for (int i = 0; i < n && gray4; i++)
         gray4 = src[i].c == 1 && dst[i].w == 4 * src[i].w && dst[i].h == 4 * src[i].h;
@@ -966,14 +980,15 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
     else
     {
         const bool bf16 = precision_ == Precision::BF16;
-        const void* w = tcWeights(precision_, 2);
+        const bool quad = tcKernel_ == 4;
+        const void* w = tcWeights(precision_, quad ? 3 : 2);
         if (!w) return fail(ts, "tensor-core weights", cudaErrorMemoryAllocation), false;
         cudaError_t err = ts.counter.ensure(256);
         if (err != cudaSuccess) return fail(ts, "device allocation", err), false;
         int* counter = static_cast<int*>(ts.counter.ptr) + (ts.counterSlot++ & 63);
         Phase2 ph;
         if (!phase_weights(2, &ph.w[0][0])) return fail(ts, "chroma resample weights"), false;
-        const int maxImages = std::min(acnet_tc3_max_images(), 64);
+        const int maxImages = std::min(quad ? acnet_tc4_max_images() : acnet_tc3_max_images(), 64);
         std::vector<int> order(n);
         for (int i = 0; i < n; i++) order[i] = i;
         // groups of one channel count and element type, in chunks of at most 64 images
@@ -1009,10 +1024,18 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
             }
             const Phase2* php = in[0].channels > 1 ? &ph : nullptr;
             bool ran = false;
-            const Tc3Plan plan = tc3Plan(m, in, out, php, w, bf16, counter, s, ran, err);
+            Tc3Plan plan;
+            if (quad) plan.perSm = tc3PerSm_ > 0 ? tc3PerSm_ : 2;
+            else plan = tc3Plan(m, in, out, php, w, bf16, counter, s, ran, err);
             if (err != cudaSuccess) return fail(ts, "batched upscale", err), false;
             mix(static_cast<uint64_t>(plan.shape * 4 + plan.perSm));
+            mix(static_cast<uint64_t>(quad));
             const int ctas = tc3Ctas_ > 0 ? tc3Ctas_ : smCount_;
+            auto launchGroup = [&]() {
+                return quad ? launch_acnet_legacy_tc4(*acnet_, w, bf16, m, in, out, php, counter, ctas, s, plan.perSm)
+                            : launch_acnet_legacy_tc3(*acnet_, w, bf16, m, in, out, php, counter, ctas, s, plan.shape,
+                                                      plan.perSm);
+            };
             cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
             if ((err = cudaStreamIsCapturing(s, &cap)) != cudaSuccess) return fail(ts, "stream state", err), false;
             auto git = ts.graphs.find(sig);
@@ -1038,8 +1061,7 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
                 GraphEntry ge;
                 if ((err = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
                     return fail(ts, "stream capture", err), false;
-                const cudaError_t lerr = launch_acnet_legacy_tc3(*acnet_, w, bf16, m, in, out, php, counter, ctas, s,
-                                                                 plan.shape, plan.perSm);
+                const cudaError_t lerr = launchGroup();
                 err = cudaStreamEndCapture(s, &ge.graph);
                 if (lerr != cudaSuccess || err != cudaSuccess)
                 {
@@ -1059,9 +1081,7 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
             {
                 if (ts.seen.size() >= 4096) ts.seen.clear();
                 ts.seen[sig] = 1;
-                if ((err = launch_acnet_legacy_tc3(*acnet_, w, bf16, m, in, out, php, counter, ctas, s, plan.shape,
-                                                   plan.perSm)) != cudaSuccess)
-                    return fail(ts, "batched upscale", err), false;
+                if ((err = launchGroup()) != cudaSuccess) return fail(ts, "batched upscale", err), false;
             }
             profileEnd(ts, ev, s, groupPixels);
             g0 = g1;
@@ -1230,15 +1250,18 @@ int GB300Processor::processDeviceNoAlloc(int n, const DeviceImage* src, const De
     const void* w = nullptr;
     {
         std::lock_guard<std::mutex> lock(mutex_);
-        w = deviceWeights_[4 + (bf16 ? 1 : 0)].ptr;
+        w = deviceWeights_[(tcKernel_ == 4 ? 6 : 4) + (bf16 ? 1 : 0)].ptr;
     }
     if (!w)
         return rejected("allocation-free call: the tensor-core weights of this precision are not on the device yet; make one "
                       "ordinary process call in this precision first");
     cudaError_t err = cudaSetDevice(device_);
     if (err != cudaSuccess) return failed("cudaSetDevice", err);
-    err = launch_acnet_legacy_tc3_noalloc(*acnet_, w, bf16, n, in, out, c > 1 ? &ph : nullptr,
-                                          tc3Ctas_ > 0 ? tc3Ctas_ : smCount_, stream);
+    // the persistent kernel the ordinary entry runs (quad or pair form)
+    err = tcKernel_ == 4 ? launch_acnet_legacy_tc4_noalloc(*acnet_, w, bf16, n, in, out, c > 1 ? &ph : nullptr,
+                                                           tc3Ctas_ > 0 ? tc3Ctas_ : smCount_, stream)
+                         : launch_acnet_legacy_tc3_noalloc(*acnet_, w, bf16, n, in, out, c > 1 ? &ph : nullptr,
+                                                           tc3Ctas_ > 0 ? tc3Ctas_ : smCount_, stream);
     if (err != cudaSuccess) return failed("allocation-free upscale", err);
     if (sync)
     {

@@ -133,7 +133,8 @@ private:
     std::pair<cudaEvent_t, cudaEvent_t> profileBegin(ThreadState& ts, cudaStream_t stream);
     void profileEnd(ThreadState& ts, std::pair<cudaEvent_t, cudaEvent_t> ev, cudaStream_t stream, double outPixels);
     // Packed tensor-core weights on the device: form 0 one pixel per row, 1
-    // pair-interleaved (per-tile kernel), 2 persistent kernel.
+    // pair-interleaved (per-tile kernel), 2 persistent kernel, 3 persistent
+    // quad kernel.
     const void* tcWeights(Precision p, int form);
     const void* arnetWeights(bool bf16);  // packed 8->8 layers of the ARNet / ACNet<8> tensor-core forms
     // Tile shape and CTAs per SM for a persistent launch over these images:
@@ -153,12 +154,12 @@ private:
     Precision precision_ = Precision::FP32;
     bool profiling_ = false;
     std::unique_ptr<AcnetLegacyWeights> acnet_;
-    DeviceBuffer deviceWeights_[6];  // TC weights: {one-pixel, pair, persistent} x {FP16, BF16}
+    DeviceBuffer deviceWeights_[8];  // TC weights: {one-pixel, pair, persistent, quad} x {FP16, BF16}
     DeviceBuffer arnetPacked_[2];    // ARNet / ACNet<8> 8->8 layers, pair form: FP16, BF16
     bool arnetTc_ = true;            // ARNet / ACNet<8> tensor-core form in FP16/BF16 (AC_GB300_ARNET_TC=0: FP32 pipeline)
     int tc3Ctas_ = 0;                // CTAs of the persistent kernel (0: one per SM; AC_GB300_TC3_CTAS)
     bool fused_ = true;              // RGB(A) x2 in one fused kernel (AC_GB300_FUSED=0 disables)
-    int tcKernel_ = 3;               // tensor-core kernel: 3 persistent (default), 2 pair-interleaved, 1 one-pixel-per-row (AC_GB300_TC_KERNEL)
+    int tcKernel_ = 4;               // tensor-core kernel: 4 persistent quad (default), 3 persistent pair, 2 pair-interleaved per tile, 1 one-pixel-per-row (AC_GB300_TC_KERNEL)
     int tc3Shape_ = -1;              // forced tile shape (AC_GB300_TC3_SHAPE), -1: autotuned
     int tc3PerSm_ = 0;               // forced CTAs per SM (AC_GB300_TC3_PER_SM), 0: autotuned
     bool autotune_ = true;           // AC_GB300_AUTOTUNE=0: default shape, two CTAs per SM

@@ -123,6 +123,17 @@ __device__ __forceinline__ void tmem_st16_dup8(uint32_t taddr, const float (&v)[
           "r"(__float_as_uint(v[7]))
         : "memory");
 }
+// 32 consecutive columns, four copies of the same 8 source registers.
+__device__ __forceinline__ void tmem_st32_dup8(uint32_t taddr, const float (&v)[8])
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %1, %2, %3, %4, %5, %6, %7, %8, "
+        "%1, %2, %3, %4, %5, %6, %7, %8, %1, %2, %3, %4, %5, %6, %7, %8};"
+        ::"r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+          "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])),
+          "r"(__float_as_uint(v[7]))
+        : "memory");
+}
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // ---- mbarriers ----

@@ -68,12 +68,13 @@ def psnr(got_u8, ref_f64):
     return 99.0 if mse == 0 else 10 * np.log10(1.0 / mse)
 
 
-@pytest.mark.parametrize("kernel", ["1", "2", "3"])
+@pytest.mark.parametrize("kernel", ["1", "2", "3", "4"])
 @pytest.mark.parametrize("form", ["fp16", "bf16"])
 @pytest.mark.parametrize("shape", [(67, 95), (46, 46), (47, 93), (1, 30), (30, 1), (140, 200), (45, 49), (89, 97)])
 def test_tc_luma_vs_fp64_oracle(form, shape, kernel, monkeypatch):
     """kernel "1": one pixel per GEMM row; "2": pixel pairs with TMA staging;
-    "3": persistent warp-specialised pipeline."""
+    "3": persistent warp-specialised pipeline; "4": its quad form (four pixels
+    per GEMM row, B matrices streamed per layer)."""
     monkeypatch.setenv("AC_GB300_TC_KERNEL", kernel)
     h, w = shape
     x = synthetic.luma(h, w, np.uint8, seed=h * 131 + w)
@@ -92,7 +93,7 @@ def test_tc_luma_vs_fp64_oracle(form, shape, kernel, monkeypatch):
         assert d.max() <= 16
 
 
-@pytest.mark.parametrize("kernel", ["1", "2", "3"])
+@pytest.mark.parametrize("kernel", ["1", "2", "3", "4"])
 @pytest.mark.parametrize("form", ["fp16", "bf16"])
 def test_tc_rgb_full_hd(form, kernel, monkeypatch):
     monkeypatch.setenv("AC_GB300_TC_KERNEL", kernel)
@@ -109,7 +110,7 @@ def test_tc_rgb_full_hd(form, kernel, monkeypatch):
         assert (d <= 2).mean() >= 0.95
 
 
-@pytest.mark.parametrize("kernel", ["1", "2", "3"])
+@pytest.mark.parametrize("kernel", ["1", "2", "3", "4"])
 @pytest.mark.parametrize("case", [c for c in META if "arnet" not in c["model"]], ids=lambda c: c["name"])
 def test_tc_golden_fp16(case, kernel, monkeypatch):
     monkeypatch.setenv("AC_GB300_TC_KERNEL", kernel)
@@ -127,12 +128,16 @@ def test_tc_golden_fp16(case, kernel, monkeypatch):
         assert d.max() <= 6
 
 
+@pytest.mark.parametrize("kernel", ["3", "4"])
 @pytest.mark.parametrize("form", ["fp32", "fp16", "bf16"])
 @pytest.mark.parametrize("c", [3, 4])
 @pytest.mark.parametrize("dtype", ["uint8", "uint16", "float32"])
-def test_fused_colour_path_matches_unfused(form, c, dtype, monkeypatch):
+def test_fused_colour_path_matches_unfused(form, c, dtype, kernel, monkeypatch):
     """RGB(A) x2 runs split + CNN + chroma resample + merge in one kernel; the
     result must equal the separate split / CNN / merge kernels bit for bit."""
+    if form == "fp32" and kernel == "4":
+        pytest.skip("the FP32 form has one kernel")
+    monkeypatch.setenv("AC_GB300_TC_KERNEL", kernel)
     x = synthetic.rgb_u8(61, 83, seed=5, alpha=(c == 4))
     if dtype == "uint16":
         x = (x.astype(np.uint16) * 257).astype(np.uint16)
@@ -147,11 +152,12 @@ def test_fused_colour_path_matches_unfused(form, c, dtype, monkeypatch):
     assert np.array_equal(outs[0], outs[1])
 
 
+@pytest.mark.parametrize("kernel", ["3", "4"])
 @pytest.mark.parametrize("c", [1, 3])
-def test_persistent_kernel_independent_of_cta_count(c, monkeypatch):
+def test_persistent_kernel_independent_of_cta_count(c, kernel, monkeypatch):
     """The persistent kernel's tile queue: any number of CTAs, each taking a
     varying number of tiles (3 x 4 tiles here), gives the same bytes."""
-    monkeypatch.setenv("AC_GB300_TC_KERNEL", "3")
+    monkeypatch.setenv("AC_GB300_TC_KERNEL", kernel)
     if c == 1:
         x = synthetic.luma(131, 150, np.uint8, seed=17)
     else:
@@ -167,3 +173,25 @@ def test_persistent_kernel_independent_of_cta_count(c, monkeypatch):
     ref32 = oracle.process(x, 2.0, "acnet-legacy-hdn1")
     d = np.abs(outs[0].astype(int) - ref32.astype(int))
     assert (d <= 1).mean() >= 0.99 and d.max() <= 6
+
+
+@pytest.mark.parametrize("form", ["fp16", "bf16"])
+@pytest.mark.parametrize("c", [1, 3, 4])
+def test_quad_kernel_batch_equals_single(form, c, monkeypatch):
+    """The quad persistent kernel over a batch of uneven images (one launch)
+    gives each image the bytes of its own launch."""
+    import torch
+    monkeypatch.setenv("AC_GB300_TC_KERNEL", "4")
+    sizes = [(37, 53), (64, 64), (95, 140), (1, 7), (46, 46), (47, 93)]
+    imgs = [synthetic.luma(h, w, np.uint8, seed=h + w) if c == 1 else synthetic.rgb_u8(h, w, seed=h + w, alpha=(c == 4))
+            for h, w in sizes]
+    p = ac.Processor("cuda", 0, "acnet-legacy-hdn2", precision=form)
+    singles = [p.process(x, 2.0) for x in imgs]
+    assert p.ok(), p.error()
+    srcs = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in imgs]
+    dsts = [torch.empty((2 * x.shape[0], 2 * x.shape[1]) + x.shape[2:], dtype=torch.uint8, device="cuda") for x in imgs]
+    for _ in range(3):  # direct launch, graph capture, graph replay
+        p.process_batch_device(srcs, dsts, 2.0)
+        assert p.ok(), p.error()
+        for d, want in zip(dsts, singles):
+            assert np.array_equal(d.cpu().numpy(), want)
