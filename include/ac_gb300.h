@@ -53,10 +53,11 @@ AC_C_API int ac_gb300_process_device(ACProcessor* processor, const ACGB300Device
  * as for ac_gb300_process_device.  An ACNetLegacy model at factor 2 in the
  * FP16 or BF16 form runs every group of images with one channel count and
  * element type (up to 64 per launch, any mix of sizes) as ONE persistent
- * tensor-core launch over a shared tile queue.  The tile shape and CTAs per
- * SM come from a measured autotune the first time a batch class (element
- * type, channels, form, total and mean image size) is seen; a repeated
- * identical batch (same buffers and shapes) replays a captured CUDA graph.
+ * tensor-core launch over a shared tile queue (the quad kernel, one 46x46
+ * tile shape; with AC_GB300_TC_KERNEL=3 the pair kernel, whose tile shape and
+ * CTAs per SM come from a measured autotune the first time a batch class is
+ * seen); a repeated identical batch (same buffers and shapes) replays a
+ * captured CUDA graph.
  * Other models, factors and forms process the images one after another.
  * Returns AC_SUCCESS or AC_ERROR(AC_EPROCESSOR) / AC_ERROR(AC_EINVAL). */
 AC_C_API int ac_gb300_process_batch_device(ACProcessor* processor, int count, const ACGB300DeviceImage* src,
