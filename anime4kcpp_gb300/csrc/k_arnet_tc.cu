@@ -58,17 +58,27 @@ enum Mode
     kTail = 2,      // prelu(1x1(0.2 * (conv + b) + skip) + b1) + feat
 };
 
-struct ConvParams
+constexpr int kMaxImg = 16;  // images per launch (the frames of a batch)
+
+// One image of a launch: its maps ([h][w] pixels of 8 16-bit channels) and
+// its tiles' place in the launch's tile sequence.
+struct ConvImg
 {
-    const uint4* in;  // [h][w] pixels of 8 16-bit channels
+    const uint4* in;
     uint4* out;
     const uint4* skip;
     const uint4* feat;
+    int w, h, tiles_x, tile0;
+};
+
+struct ConvParams
+{
     const uint4* bw;  // packed B (12 chunks of 256 bytes)
-    int w, h, tiles_x;
     float b[8], a[8];
     float k1[64], b1[8], a1[8];
     int* status;
+    int nimg;
+    ConvImg img[kMaxImg];
 };
 
 template <bool BF16>
@@ -115,7 +125,11 @@ __global__ void __launch_bounds__(THREADS, 4) conv_kernel(const __grid_constant_
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + 2 * PLANE_BYTES + B_BYTES);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 2 * PLANE_BYTES + B_BYTES + 8);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int x0 = (blockIdx.x % P.tiles_x) * TW - 1, y0 = (blockIdx.x / P.tiles_x) * TH - 1;
+    int im = 0;
+    while (im + 1 < P.nimg && P.img[im + 1].tile0 <= static_cast<int>(blockIdx.x)) im++;
+    const ConvImg& I = P.img[im];
+    const int local = static_cast<int>(blockIdx.x) - I.tile0;
+    const int x0 = (local % I.tiles_x) * TW - 1, y0 = (local / I.tiles_x) * TH - 1;
 
     if (tid == 0)
     {
@@ -147,8 +161,8 @@ __global__ void __launch_bounds__(THREADS, 4) conv_kernel(const __grid_constant_
         {
             const int p = tid + (k0 + k) * THREADS;
             const int wy = p / WW, wx = p - wy * WW;
-            const int gx = clampi(x0 + wx, 0, P.w - 1), gy = clampi(y0 + wy, 0, P.h - 1);
-            px[k] = P.in[static_cast<size_t>(gy) * P.w + gx];
+            const int gx = clampi(x0 + wx, 0, I.w - 1), gy = clampi(y0 + wy, 0, I.h - 1);
+            px[k] = I.in[static_cast<size_t>(gy) * I.w + gx];
         }
 #pragma unroll
         for (int k = 0; k < 8; k++)
@@ -200,8 +214,8 @@ __global__ void __launch_bounds__(THREADS, 4) conv_kernel(const __grid_constant_
                 const int p = 2 * r + k;
                 const int y = p / WW, x = p - y * WW;
                 const int gx = x0 + x, gy = y0 + y;
-                if (y < 1 || y > TH || x < 1 || x > TW || gx >= P.w || gy >= P.h) continue;
-                const size_t o = static_cast<size_t>(gy) * P.w + gx;
+                if (y < 1 || y > TH || x < 1 || x > TW || gx >= I.w || gy >= I.h) continue;
+                const size_t o = static_cast<size_t>(gy) * I.w + gx;
                 float s[8];
 #pragma unroll
                 for (int c = 0; c < 8; c++) s[c] = v[8 * k + c] + P.b[c];
@@ -213,13 +227,13 @@ __global__ void __launch_bounds__(THREADS, 4) conv_kernel(const __grid_constant_
                 else
                 {
                     float sk[8];
-                    unpack8<BF16>(P.skip[o], sk);
+                    unpack8<BF16>(I.skip[o], sk);
 #pragma unroll
                     for (int c = 0; c < 8; c++) s[c] = fmaf(s[c], 0.2f, sk[c]);
                     if constexpr (MODE == kTail)
                     {
                         float f[8], t[8];
-                        unpack8<BF16>(P.feat[o], f);
+                        unpack8<BF16>(I.feat[o], f);
 #pragma unroll
                         for (int n = 0; n < 8; n++)
                         {
@@ -232,7 +246,7 @@ __global__ void __launch_bounds__(THREADS, 4) conv_kernel(const __grid_constant_
                         for (int n = 0; n < 8; n++) s[n] = t[n];
                     }
                 }
-                P.out[o] = pack8<BF16>(s);
+                I.out[o] = pack8<BF16>(s);
             }
         }
     tc::fence_before_sync();
@@ -246,14 +260,18 @@ struct HeadParams
     float b[8];
     float a[8];   // PReLU slopes when `prelu` is set (the ACNet<8> head)
     int prelu;
+    Plane in[kMaxImg];     // image blockIdx.z
+    uint4* feat[kMaxImg];
 };
 
 // Head: conv3x3 1->8 in FP32 from the input plane, identity (ARNet) or PReLU
 // (ACNet<8>), stored as a 16-bit 8-channel map.  One thread per pixel, taps
 // clamped to the plane.
 template <typename T, bool BF16>
-__global__ void __launch_bounds__(256) head_kernel(Plane in, uint4* __restrict__ feat, const __grid_constant__ HeadParams P)
+__global__ void __launch_bounds__(256) head_kernel(const __grid_constant__ HeadParams P)
 {
+    const Plane& in = P.in[blockIdx.z];
+    uint4* __restrict__ feat = P.feat[blockIdx.z];
     const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
     if (x >= in.w || y >= in.h) return;
     float t[9];
@@ -279,14 +297,18 @@ struct UpParams
 {
     float k[288];
     float b[4];
+    const uint4* map[kMaxImg];  // image blockIdx.z
+    Plane src[kMaxImg], dst[kMaxImg];
 };
 
 // Upscale: conv3x3 8->4 (identity) in FP32 from the 16-bit map, pixel
 // shuffle 2x2, plus the nearest input pixel, fromFloat (Common.hpp:290-342).
 template <typename T, bool BF16>
-__global__ void __launch_bounds__(256) up_kernel(const uint4* __restrict__ map, Plane src, Plane dst,
-                                                 const __grid_constant__ UpParams U)
+__global__ void __launch_bounds__(256) up_kernel(const __grid_constant__ UpParams U)
 {
+    const uint4* __restrict__ map = U.map[blockIdx.z];
+    const Plane& src = U.src[blockIdx.z];
+    const Plane& dst = U.dst[blockIdx.z];
     const int w = src.w, h = src.h;
     const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
     if (x >= w || y >= h) return;
@@ -363,14 +385,21 @@ void pack_pair_conv8(const float* k, bool bf16, uint16_t* out)
 
 namespace arnettc {
 
-cudaError_t launch_head(const HeadParams& hp, bool bf16, const Plane& in, uint4* feat, cudaStream_t stream)
+// The head over n images (grid z = image); hp.in / hp.feat filled in.
+cudaError_t launch_head(const HeadParams& hp, bool bf16, int n, cudaStream_t stream)
 {
-    const dim3 pgrid((in.w + 31) / 32, (in.h + 7) / 8);
-    switch (in.type)
+    int mw = 0, mh = 0;
+    for (int i = 0; i < n; i++)
     {
-    case kU8: bf16 ? head_kernel<uint8_t, true><<<pgrid, 256, 0, stream>>>(in, feat, hp) : head_kernel<uint8_t, false><<<pgrid, 256, 0, stream>>>(in, feat, hp); break;
-    case kU16: bf16 ? head_kernel<uint16_t, true><<<pgrid, 256, 0, stream>>>(in, feat, hp) : head_kernel<uint16_t, false><<<pgrid, 256, 0, stream>>>(in, feat, hp); break;
-    case kF32: bf16 ? head_kernel<float, true><<<pgrid, 256, 0, stream>>>(in, feat, hp) : head_kernel<float, false><<<pgrid, 256, 0, stream>>>(in, feat, hp); break;
+        mw = hp.in[i].w > mw ? hp.in[i].w : mw;
+        mh = hp.in[i].h > mh ? hp.in[i].h : mh;
+    }
+    const dim3 pgrid((mw + 31) / 32, (mh + 7) / 8, n);
+    switch (hp.in[0].type)
+    {
+    case kU8: bf16 ? head_kernel<uint8_t, true><<<pgrid, 256, 0, stream>>>(hp) : head_kernel<uint8_t, false><<<pgrid, 256, 0, stream>>>(hp); break;
+    case kU16: bf16 ? head_kernel<uint16_t, true><<<pgrid, 256, 0, stream>>>(hp) : head_kernel<uint16_t, false><<<pgrid, 256, 0, stream>>>(hp); break;
+    case kF32: bf16 ? head_kernel<float, true><<<pgrid, 256, 0, stream>>>(hp) : head_kernel<float, false><<<pgrid, 256, 0, stream>>>(hp); break;
     default: return cudaErrorInvalidValue;
     }
     const cudaError_t err = cudaGetLastError();
@@ -378,68 +407,93 @@ cudaError_t launch_head(const HeadParams& hp, bool bf16, const Plane& in, uint4*
     return err;
 }
 
-cudaError_t launch_up(const UpParams& u, bool bf16, const uint4* map, const Plane& in, const Plane& out, cudaStream_t stream)
+// The upscale layer over n images (grid z = image); u.map / src / dst filled in.
+cudaError_t launch_up(const UpParams& u, bool bf16, int n, cudaStream_t stream)
 {
-    const dim3 pgrid((in.w + 31) / 32, (in.h + 7) / 8);
-    switch (in.type)
+    int mw = 0, mh = 0;
+    for (int i = 0; i < n; i++)
     {
-    case kU8: bf16 ? up_kernel<uint8_t, true><<<pgrid, 256, 0, stream>>>(map, in, out, u) : up_kernel<uint8_t, false><<<pgrid, 256, 0, stream>>>(map, in, out, u); break;
-    case kU16: bf16 ? up_kernel<uint16_t, true><<<pgrid, 256, 0, stream>>>(map, in, out, u) : up_kernel<uint16_t, false><<<pgrid, 256, 0, stream>>>(map, in, out, u); break;
-    case kF32: bf16 ? up_kernel<float, true><<<pgrid, 256, 0, stream>>>(map, in, out, u) : up_kernel<float, false><<<pgrid, 256, 0, stream>>>(map, in, out, u); break;
+        mw = u.src[i].w > mw ? u.src[i].w : mw;
+        mh = u.src[i].h > mh ? u.src[i].h : mh;
+    }
+    const dim3 pgrid((mw + 31) / 32, (mh + 7) / 8, n);
+    switch (u.src[0].type)
+    {
+    case kU8: bf16 ? up_kernel<uint8_t, true><<<pgrid, 256, 0, stream>>>(u) : up_kernel<uint8_t, false><<<pgrid, 256, 0, stream>>>(u); break;
+    case kU16: bf16 ? up_kernel<uint16_t, true><<<pgrid, 256, 0, stream>>>(u) : up_kernel<uint16_t, false><<<pgrid, 256, 0, stream>>>(u); break;
+    case kF32: bf16 ? up_kernel<float, true><<<pgrid, 256, 0, stream>>>(u) : up_kernel<float, false><<<pgrid, 256, 0, stream>>>(u); break;
     default: return cudaErrorInvalidValue;
     }
     const cudaError_t err = cudaGetLastError();
     if (err == cudaSuccess) count_launch();
     return err;
+}
+
+// Checks a batch (1 to kMaxImg single-channel images of one element type,
+// each output 2x its input) and fills the per-image parts of the launch
+// parameters: tile sequence of the conv launches, head and upscale planes.
+cudaError_t prepare_batch(int n, const Plane* in, const Plane* out, ConvParams& c, HeadParams& hp, UpParams& u, int& tiles)
+{
+    if (n < 1 || n > kMaxImg) return cudaErrorInvalidValue;
+    tiles = 0;
+    for (int i = 0; i < n; i++)
+    {
+        if (in[i].w <= 0 || in[i].h <= 0 || in[i].channels != 1 || out[i].channels != 1 || in[i].type != in[0].type ||
+            out[i].w != 2 * in[i].w || out[i].h != 2 * in[i].h)
+            return cudaErrorInvalidValue;
+        ConvImg& I = c.img[i];
+        I.w = in[i].w;
+        I.h = in[i].h;
+        I.tiles_x = (in[i].w + TW - 1) / TW;
+        I.tile0 = tiles;
+        tiles += I.tiles_x * ((in[i].h + TH - 1) / TH);
+        hp.in[i] = in[i];
+        u.src[i] = in[i];
+        u.dst[i] = out[i];
+    }
+    c.nimg = n;
+    return cudaSuccess;
 }
 
 }  // namespace arnettc
 
-// Runs one ARNet x2 pass in the tensor-core form.  packed: 2*blocks layers of
-// pack_pair_conv8 output (device); maps: three [h][w] arrays of 16-byte pixels.
-cudaError_t launch_arnet_tc(const float* kernels, const float* biases, const float* alphas, int blocks, const void* packed,
-                            bool bf16, const Plane& in, const Plane& out, void* const maps[3], int* status,
-                            cudaStream_t stream)
+// Runs one ARNet x2 pass over n images in the tensor-core form, every layer
+// as one launch over all images.  packed: 2*blocks layers of pack_pair_conv8
+// output (device); maps[3 i + j]: image i's three [h][w] arrays of 16-byte
+// pixels.
+cudaError_t launch_arnet_tc_batch(const float* kernels, const float* biases, const float* alphas, int blocks, const void* packed,
+                                  bool bf16, int n, const Plane* in, const Plane* out, void* const* maps, int* status,
+                                  cudaStream_t stream)
 {
     using namespace arnettc;
-    const int w = in.w, h = in.h;
-    if (w <= 0 || h <= 0) return cudaSuccess;
-    if (blocks < 2 || !packed || !status) return cudaErrorInvalidValue;
-    uint4* feat = static_cast<uint4*>(maps[0]);
-    uint4* x = static_cast<uint4*>(maps[1]);
-    uint4* t = static_cast<uint4*>(maps[2]);
-    const int tiles_x = (w + TW - 1) / TW, tiles = tiles_x * ((h + TH - 1) / TH);
-    const dim3 pgrid((w + 31) / 32, (h + 7) / 8);
-    cudaError_t err;
+    if (n <= 0) return cudaSuccess;
+    if (blocks < 2 || !packed || !status || !maps) return cudaErrorInvalidValue;
     ConvParams p;
+    HeadParams hp;
+    UpParams u;
     std::memset(&p, 0, sizeof(p));
-    p.w = w;
-    p.h = h;
-    p.tiles_x = tiles_x;
+    std::memset(&hp, 0, sizeof(hp));
+    std::memset(&u, 0, sizeof(u));
+    int tiles = 0;
+    cudaError_t err = prepare_batch(n, in, out, p, hp, u, tiles);
+    if (err != cudaSuccess) return err;
     p.status = status;
     // head (FP32)
-    {
-        HeadParams hp;
-        for (int i = 0; i < 72; i++) hp.k[i] = kernels[i];
-        for (int i = 0; i < 8; i++) hp.b[i] = biases[i];
-        for (int i = 0; i < 8; i++) hp.a[i] = 0.0f;
-        hp.prelu = 0;
-        switch (in.type)
-        {
-        case kU8: bf16 ? head_kernel<uint8_t, true><<<pgrid, 256, 0, stream>>>(in, feat, hp) : head_kernel<uint8_t, false><<<pgrid, 256, 0, stream>>>(in, feat, hp); break;
-        case kU16: bf16 ? head_kernel<uint16_t, true><<<pgrid, 256, 0, stream>>>(in, feat, hp) : head_kernel<uint16_t, false><<<pgrid, 256, 0, stream>>>(in, feat, hp); break;
-        case kF32: bf16 ? head_kernel<float, true><<<pgrid, 256, 0, stream>>>(in, feat, hp) : head_kernel<float, false><<<pgrid, 256, 0, stream>>>(in, feat, hp); break;
-        default: return cudaErrorInvalidValue;
-        }
-        if ((err = cudaGetLastError()) != cudaSuccess) return err;
-        count_launch();
-    }
-    auto conv = [&](int l, int mode, const uint4* src, uint4* dst, const uint4* skip) -> cudaError_t {
+    for (int i = 0; i < 72; i++) hp.k[i] = kernels[i];
+    for (int i = 0; i < 8; i++) hp.b[i] = biases[i];
+    hp.prelu = 0;
+    for (int i = 0; i < n; i++) hp.feat[i] = static_cast<uint4*>(maps[3 * i]);
+    if ((err = launch_head(hp, bf16, n, stream)) != cudaSuccess) return err;
+    // maps of image i: feat, x, t
+    auto conv = [&](int l, int mode, int src, int dst, int skip) -> cudaError_t {
         ConvParams c = p;
-        c.in = src;
-        c.out = dst;
-        c.skip = skip;
-        c.feat = feat;
+        for (int i = 0; i < n; i++)
+        {
+            c.img[i].in = static_cast<const uint4*>(maps[3 * i + src]);
+            c.img[i].out = static_cast<uint4*>(maps[3 * i + dst]);
+            c.img[i].skip = skip < 0 ? nullptr : static_cast<const uint4*>(maps[3 * i + skip]);
+            c.img[i].feat = static_cast<const uint4*>(maps[3 * i]);
+        }
         c.bw = static_cast<const uint4*>(packed) + static_cast<size_t>(l - 1) * (B_BYTES / 16);
         for (int i = 0; i < 8; i++) c.b[i] = biases[8 * l + i];
         for (int i = 0; i < 8; i++) c.a[i] = mode == kPReLU ? alphas[8 * ((l - 1) / 2) + i] : 0.0f;
@@ -457,86 +511,93 @@ cudaError_t launch_arnet_tc(const float* kernels, const float* biases, const flo
         if (e == cudaSuccess) count_launch();
         return e;
     };
+    constexpr int FEAT = 0, X = 1, T = 2;
     // block 1: t = prelu(conv(feat)); x = 0.2 conv(t) + feat
     int l = 1;
-    if ((err = conv(l++, kPReLU, feat, t, nullptr)) != cudaSuccess) return err;
-    if ((err = conv(l++, kResidual, t, x, feat)) != cudaSuccess) return err;
+    if ((err = conv(l++, kPReLU, FEAT, T, -1)) != cudaSuccess) return err;
+    if ((err = conv(l++, kResidual, T, X, FEAT)) != cudaSuccess) return err;
     // blocks 2 .. B-1: t = prelu(conv(x)); x = 0.2 conv(t) + x (in place: each pixel reads its own skip)
     for (int i = 0; i < blocks - 2; i++)
     {
-        if ((err = conv(l++, kPReLU, x, t, nullptr)) != cudaSuccess) return err;
-        if ((err = conv(l++, kResidual, t, x, x)) != cudaSuccess) return err;
+        if ((err = conv(l++, kPReLU, X, T, -1)) != cudaSuccess) return err;
+        if ((err = conv(l++, kResidual, T, X, X)) != cudaSuccess) return err;
     }
-    // block B with the 1x1 + PReLU + feat tail: result into t's partner (feat is still needed, so into x in place)
-    if ((err = conv(l++, kPReLU, x, t, nullptr)) != cudaSuccess) return err;
-    if ((err = conv(l++, kTail, t, x, x)) != cudaSuccess) return err;
+    // block B with the 1x1 + PReLU + feat tail, into x in place
+    if ((err = conv(l++, kPReLU, X, T, -1)) != cudaSuccess) return err;
+    if ((err = conv(l++, kTail, T, X, X)) != cudaSuccess) return err;
     l++;  // the 1x1 layer's bias index
     // upscale (FP32)
-    UpParams u;
     for (int i = 0; i < 288; i++) u.k[i] = kernels[72 + 576 * (2 * blocks) + 64 + i];
     for (int i = 0; i < 4; i++) u.b[i] = biases[8 * l + i];
-    switch (in.type)
-    {
-    case kU8: bf16 ? up_kernel<uint8_t, true><<<pgrid, 256, 0, stream>>>(x, in, out, u) : up_kernel<uint8_t, false><<<pgrid, 256, 0, stream>>>(x, in, out, u); break;
-    case kU16: bf16 ? up_kernel<uint16_t, true><<<pgrid, 256, 0, stream>>>(x, in, out, u) : up_kernel<uint16_t, false><<<pgrid, 256, 0, stream>>>(x, in, out, u); break;
-    case kF32: bf16 ? up_kernel<float, true><<<pgrid, 256, 0, stream>>>(x, in, out, u) : up_kernel<float, false><<<pgrid, 256, 0, stream>>>(x, in, out, u); break;
-    default: return cudaErrorInvalidValue;
-    }
-    if ((err = cudaGetLastError()) != cudaSuccess) return err;
-    count_launch();
-    return cudaSuccess;
+    for (int i = 0; i < n; i++) u.map[i] = static_cast<const uint4*>(maps[3 * i + X]);
+    return launch_up(u, bf16, n, stream);
 }
 
-// Runs one ACNet<8> x2 pass in the tensor-core form (network of
+cudaError_t launch_arnet_tc(const float* kernels, const float* biases, const float* alphas, int blocks, const void* packed,
+                            bool bf16, const Plane& in, const Plane& out, void* const maps[3], int* status,
+                            cudaStream_t stream)
+{
+    if (in.w <= 0 || in.h <= 0) return cudaSuccess;
+    return launch_arnet_tc_batch(kernels, biases, alphas, blocks, packed, bf16, 1, &in, &out, maps, status, stream);
+}
+
+// Runs one ACNet<8> x2 pass over n images in the tensor-core form (network of
 // core/include/AC/Core/Model/ACNet.hpp:63-116, CPU order
 // core/src/processor/cpu/CPUProcessor.cpp:1417-1436): the PReLU head in FP32,
 // `blocks` 3x3 8->8 + PReLU layers on tcgen05 (packed: `blocks` layers of
-// pack_pair_conv8 output), the upscale layer in FP32.  maps: two [h][w]
-// arrays of 16-byte pixels used in turn.
-cudaError_t launch_acnet8_tc(const float* kernels, const float* biases, const float* alphas, int blocks, const void* packed,
-                             bool bf16, const Plane& in, const Plane& out, void* const maps[2], int* status,
-                             cudaStream_t stream)
+// pack_pair_conv8 output), the upscale layer in FP32.  maps[2 i + j]: image
+// i's two [h][w] arrays of 16-byte pixels, used in turn.
+cudaError_t launch_acnet8_tc_batch(const float* kernels, const float* biases, const float* alphas, int blocks,
+                                   const void* packed, bool bf16, int n, const Plane* in, const Plane* out,
+                                   void* const* maps, int* status, cudaStream_t stream)
 {
     using namespace arnettc;
-    const int w = in.w, h = in.h;
-    if (w <= 0 || h <= 0) return cudaSuccess;
-    if (blocks < 1 || !packed || !status) return cudaErrorInvalidValue;
-    uint4* a = static_cast<uint4*>(maps[0]);
-    uint4* b = static_cast<uint4*>(maps[1]);
-    const int tiles_x = (w + TW - 1) / TW, tiles = tiles_x * ((h + TH - 1) / TH);
-    cudaError_t err;
-    {
-        HeadParams hp;
-        for (int i = 0; i < 72; i++) hp.k[i] = kernels[i];
-        for (int i = 0; i < 8; i++) hp.b[i] = biases[i];
-        for (int i = 0; i < 8; i++) hp.a[i] = alphas[i];
-        hp.prelu = 1;
-        if ((err = launch_head(hp, bf16, in, a, stream)) != cudaSuccess) return err;
-    }
+    if (n <= 0) return cudaSuccess;
+    if (blocks < 1 || !packed || !status || !maps) return cudaErrorInvalidValue;
     ConvParams c;
+    HeadParams hp;
+    UpParams u;
     std::memset(&c, 0, sizeof(c));
-    c.w = w;
-    c.h = h;
-    c.tiles_x = tiles_x;
+    std::memset(&hp, 0, sizeof(hp));
+    std::memset(&u, 0, sizeof(u));
+    int tiles = 0;
+    cudaError_t err = prepare_batch(n, in, out, c, hp, u, tiles);
+    if (err != cudaSuccess) return err;
     c.status = status;
+    for (int i = 0; i < 72; i++) hp.k[i] = kernels[i];
+    for (int i = 0; i < 8; i++) hp.b[i] = biases[i];
+    for (int i = 0; i < 8; i++) hp.a[i] = alphas[i];
+    hp.prelu = 1;
+    for (int i = 0; i < n; i++) hp.feat[i] = static_cast<uint4*>(maps[2 * i]);
+    if ((err = launch_head(hp, bf16, n, stream)) != cudaSuccess) return err;
+    int a = 0;  // the map holding the current layer's input
     for (int l = 1; l <= blocks; l++)
     {
-        c.in = a;
-        c.out = b;
+        for (int i = 0; i < n; i++)
+        {
+            c.img[i].in = static_cast<const uint4*>(maps[2 * i + a]);
+            c.img[i].out = static_cast<uint4*>(maps[2 * i + 1 - a]);
+        }
         c.bw = static_cast<const uint4*>(packed) + static_cast<size_t>(l - 1) * (B_BYTES / 16);
         for (int i = 0; i < 8; i++) c.b[i] = biases[8 * l + i];
         for (int i = 0; i < 8; i++) c.a[i] = alphas[8 * l + i];
         err = bf16 ? launch_conv<kPReLU, true>(c, tiles, stream) : launch_conv<kPReLU, false>(c, tiles, stream);
         if (err != cudaSuccess) return err;
         count_launch();
-        uint4* t = a;
-        a = b;
-        b = t;
+        a = 1 - a;
     }
-    UpParams u;
     for (int i = 0; i < 288; i++) u.k[i] = kernels[72 + 576 * blocks + i];
     for (int i = 0; i < 4; i++) u.b[i] = biases[8 * (blocks + 1) + i];
-    return launch_up(u, bf16, a, in, out, stream);
+    for (int i = 0; i < n; i++) u.map[i] = static_cast<const uint4*>(maps[2 * i + a]);
+    return launch_up(u, bf16, n, stream);
+}
+
+cudaError_t launch_acnet8_tc(const float* kernels, const float* biases, const float* alphas, int blocks, const void* packed,
+                             bool bf16, const Plane& in, const Plane& out, void* const maps[2], int* status,
+                             cudaStream_t stream)
+{
+    if (in.w <= 0 || in.h <= 0) return cudaSuccess;
+    return launch_acnet8_tc_batch(kernels, biases, alphas, blocks, packed, bf16, 1, &in, &out, maps, status, stream);
 }
 
 }  // namespace acgb

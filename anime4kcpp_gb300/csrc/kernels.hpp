@@ -142,6 +142,13 @@ cudaError_t launch_arnet_tc(const float* kernels, const float* biases, const flo
                             bool bf16, const Plane& in, const Plane& out, void* const maps[3], int* status,
                             cudaStream_t stream);
 int* tc_status_buffer();
+// The same for n single-channel images at once (1 to kArnetTcMaxImages, one
+// element type, each output 2x its input): every layer is one launch over all
+// images' tiles; maps[3 i + j] are image i's three work maps.
+constexpr int kArnetTcMaxImages = 16;
+cudaError_t launch_arnet_tc_batch(const float* kernels, const float* biases, const float* alphas, int blocks, const void* packed,
+                                  bool bf16, int n, const Plane* in, const Plane* out, void* const* maps, int* status,
+                                  cudaStream_t stream);
 
 // ACNet<8> x2 pass (head conv 1->8 + PReLU, `blocks` conv 8->8 + PReLU, conv
 // 8->4 + pixel shuffle + nearest input; ACNet.hpp:63-116).  Plain FP32 with
@@ -152,6 +159,10 @@ cudaError_t launch_acnet8_fp32(const float* kernels, const float* biases, const 
 cudaError_t launch_acnet8_tc(const float* kernels, const float* biases, const float* alphas, int blocks, const void* packed,
                              bool bf16, const Plane& in, const Plane& out, void* const maps[2], int* status,
                              cudaStream_t stream);
+// n images at once (as launch_arnet_tc_batch); maps[2 i + j].
+cudaError_t launch_acnet8_tc_batch(const float* kernels, const float* biases, const float* alphas, int blocks,
+                                   const void* packed, bool bf16, int n, const Plane* in, const Plane* out,
+                                   void* const* maps, int* status, cudaStream_t stream);
 
 // Merge for chroma resampled by exactly `factor` (2 or 4) on both axes:
 // phase_weights[k*4 + t] is the Catmull-Rom weight of tap t of output phase k,

@@ -949,6 +949,14 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
                               cudaStream_t s)
 {
     const bool tcBatch = spec_.family == Family::ACNetLegacy && precision_ != Precision::FP32 && tcKernel_ >= 3 && fused_;
+    // ARNet / ACNet<8> in a tensor-core form: single-channel images of one
+    // element type run every layer as one launch over all images
+    bool layered = spec_.family != Family::ACNetLegacy && precision_ != Precision::FP32 && arnetTc_ && n > 1 &&
+                   (factor == 2.0 || factor == 4.0);
+    for (int i = 0; i < n && layered; i++)
+        layered = src[i].c == 1 && src[i].type == src[0].type && dst[i].w == static_cast<int>(factor) * src[i].w &&
+                  dst[i].h == static_cast<int>(factor) * src[i].h;
+    if (layered) return layeredBatch(ts, n, src, dst, factor, s);
     bool gray4 = tcBatch && factor == 4.0 && n > 0;
     for (int i = 0; i < n && gray4; i++)
         gray4 = src[i].c == 1 && dst[i].w == 4 * src[i].w && dst[i].h == 4 * src[i].h;
@@ -1085,6 +1093,73 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
             }
             profileEnd(ts, ev, s, groupPixels);
             g0 = g1;
+        }
+    }
+    return true;
+}
+
+bool GB300Processor::layeredBatch(ThreadState& ts, int n, const DeviceImage* src, const DeviceImage* dst, double factor,
+                                  cudaStream_t s)
+{
+    const int per = spec_.family == Family::ARNet ? 3 : 2;  // work maps per image
+    const bool bf16 = precision_ == Precision::BF16;
+    const void* w = arnetWeights(bf16);
+    int* status = tc_status_buffer();
+    if (!w || !status) return fail(ts, "tensor-core weights", cudaErrorMemoryAllocation), false;
+    const ModelParams& mp = model_params(spec_);
+    // x4: x2 into temporaries, then x2 into dst (the reference's power-of-two pass loop)
+    std::vector<DeviceImage> mid;
+    if (factor == 4.0)
+    {
+        mid.resize(n);
+        std::vector<size_t> off(n);
+        size_t total = 0;
+        for (int i = 0; i < n; i++)
+        {
+            const int es = src[i].type & 0xff, pitch = align_pitch(2 * src[i].w * es);
+            off[i] = total;
+            total += (static_cast<size_t>(pitch) * 2 * src[i].h + 255) & ~static_cast<size_t>(255);
+            mid[i] = DeviceImage{nullptr, 2 * src[i].w, 2 * src[i].h, 1, pitch, src[i].type};
+        }
+        cudaError_t err = ts.batchTmp.ensure(total);
+        if (err != cudaSuccess) return fail(ts, "device allocation", err), false;
+        for (int i = 0; i < n; i++) mid[i].ptr = static_cast<char*>(ts.batchTmp.ptr) + off[i];
+    }
+    for (int pass = 0; pass < (factor == 4.0 ? 2 : 1); pass++)
+    {
+        const DeviceImage* a = pass == 0 ? src : mid.data();
+        const DeviceImage* b = (factor == 4.0 && pass == 0) ? mid.data() : dst;
+        for (int g0 = 0; g0 < n; g0 += kArnetTcMaxImages)
+        {
+            const int m = std::min(n - g0, kArnetTcMaxImages);
+            std::vector<Plane> in(m), out(m);
+            std::vector<size_t> moff(m);
+            size_t mapBytes = 0;
+            for (int j = 0; j < m; j++)
+            {
+                in[j] = plane_of(a[g0 + j]);
+                out[j] = plane_of(b[g0 + j]);
+                moff[j] = mapBytes;
+                mapBytes += (static_cast<size_t>(in[j].w) * in[j].h * 16 + 255) & ~static_cast<size_t>(255);
+            }
+            std::vector<void*> maps(static_cast<size_t>(per) * m);
+            for (int k = 0; k < per; k++)
+            {
+                cudaError_t err = ts.maps[k].ensure(mapBytes);
+                if (err != cudaSuccess) return fail(ts, "device allocation", err), false;
+                for (int j = 0; j < m; j++) maps[static_cast<size_t>(per) * j + k] = static_cast<char*>(ts.maps[k].ptr) + moff[j];
+            }
+            double px = 0.0;
+            for (int j = 0; j < m; j++) px += static_cast<double>(out[j].w) * out[j].h;
+            const std::pair<cudaEvent_t, cudaEvent_t> ev = profileBegin(ts, s);
+            const cudaError_t err =
+                spec_.family == Family::ARNet
+                    ? launch_arnet_tc_batch(mp.kernels.data(), mp.biases.data(), mp.alphas.data(), spec_.blocks, w, bf16, m,
+                                            in.data(), out.data(), maps.data(), status, s)
+                    : launch_acnet8_tc_batch(mp.kernels.data(), mp.biases.data(), mp.alphas.data(), spec_.blocks, w, bf16, m,
+                                             in.data(), out.data(), maps.data(), status, s);
+            profileEnd(ts, ev, s, px);
+            if (err != cudaSuccess) return fail(ts, "batched upscale", err), false;
         }
     }
     return true;

@@ -143,6 +143,9 @@ private:
     // mean image sizes) over every shape x {2, 1} CTAs per SM.  When it
     // measured, the launches already produced the output (`ran`).
     bool batchRun(ThreadState& ts, int n, const DeviceImage* src, const DeviceImage* dst, double factor, cudaStream_t s);
+    // ARNet / ACNet<8> tensor-core forms over n single-channel images, x2 or
+    // x4: each layer one launch over every image (up to kArnetTcMaxImages).
+    bool layeredBatch(ThreadState& ts, int n, const DeviceImage* src, const DeviceImage* dst, double factor, cudaStream_t s);
     Tc3Plan tc3Plan(int n, const Plane* in, const Plane* out, const Phase2* ph, const void* w, bool bf16, int* counter,
                     cudaStream_t stream, bool& ran, cudaError_t& err);
 

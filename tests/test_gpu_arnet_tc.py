@@ -83,3 +83,29 @@ def test_arnet_tc_matches_fp32_pipeline_closely(monkeypatch):
     q = ac.Processor("cuda", 0, "arnet-b8", precision="fp16")
     fp32 = q.process(x, 2.0)
     assert np.abs(tc.astype(int) - fp32.astype(int)).max() <= 2
+
+
+@pytest.mark.parametrize("factor", [2.0, 4.0])
+@pytest.mark.parametrize("model", ["arnet-b8", "acnet-f8b8-hdn"])
+def test_layered_tc_batch_equals_single(model, factor):
+    """ARNet / ACNet<8> tensor-core forms over a batch of uneven single-channel
+    images: every layer is one launch over all images, and each image gets the
+    bytes of its own per-image run (x4: two chained batched x2 passes)."""
+    import torch
+    sizes = [(67, 131), (30, 62), (1, 40), (45, 1), (90, 33)]
+    imgs = [synthetic.luma(h, w, np.uint16, seed=h * 7 + w, noise=4.0, bits=10) << 6 for h, w in sizes]
+    imgs = [x.astype(np.uint16) for x in imgs]
+    p = ac.Processor("cuda", 0, model, precision="fp16")
+    singles = [p.process(x, factor) for x in imgs]
+    assert p.ok(), p.error()
+    f = int(factor)
+    srcs = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in imgs]
+    dsts = [torch.empty((f * x.shape[0], f * x.shape[1]), dtype=torch.uint16, device="cuda") for x in imgs]
+    l0 = ac.launch_count()
+    p.process_batch_device(srcs, dsts, factor)
+    assert p.ok(), p.error()
+    launches = ac.launch_count() - l0
+    layers = 2 * 8 + 2 if model.startswith("arnet") else 8 + 2  # head, 8->8 layers, upscale
+    assert launches == layers * (2 if factor == 4.0 else 1)
+    for d, want in zip(dsts, singles):
+        assert np.array_equal(d.cpu().numpy(), want)
