@@ -254,6 +254,228 @@ __global__ void __launch_bounds__(THREADS, 4) conv_kernel(const __grid_constant_
     if (warp == 0) tc::tmem_dealloc(tmem, TMEM_COLS);
 }
 
+// Two layers per launch (a residual block of ARNet<8>, or two ACNet<8>
+// layers): layer A = conv + PReLU over the whole 64x32 window, drained in
+// place into the shared-memory planes once all its MMAs completed (with the
+// clamp-to-edge replicas at image borders); layer B = conv + MODE on the
+// 60x28 tile, the residual skip being layer A's input map.  Map traffic per
+// block: one window read, one skip read, one write (two layers apart: two
+// reads, a skip read and two writes).
+constexpr int TW2 = WW - 4, TH2 = WH - 4;  // 60 x 28 tile, window origin 2 pixels up and left
+
+struct Conv2Params
+{
+    const uint4* bwA;  // packed B of layer A
+    const uint4* bwB;  // packed B of layer B
+    float bA[8], aA[8];
+    float b[8], a[8];  // layer B (a: PReLU mode)
+    float k1[64], b1[8], a1[8];
+    int* status;
+    int nimg;
+    ConvImg img[kMaxImg];  // in: layer A's input (the skip), out, feat; tiles of TW2 x TH2
+};
+
+template <int MODE, bool BF16>
+__global__ void __launch_bounds__(THREADS, 4) conv2_kernel(const __grid_constant__ Conv2Params P)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* plane = smem;  // E plane, then O plane
+    unsigned char* bsmA = smem + 2 * PLANE_BYTES;
+    unsigned char* bsmB = bsmA + B_BYTES;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(bsmB + B_BYTES);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bsmB + B_BYTES + 8);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    int im = 0;
+    while (im + 1 < P.nimg && P.img[im + 1].tile0 <= static_cast<int>(blockIdx.x)) im++;
+    const ConvImg& I = P.img[im];
+    const int local = static_cast<int>(blockIdx.x) - I.tile0;
+    const int x0 = (local % I.tiles_x) * TW2 - 2, y0 = (local / I.tiles_x) * TH2 - 2;
+    // the window's in-image extent
+    const int ix0 = max(0, -x0), ix1 = min(WW - 1, I.w - 1 - x0);
+    const int iy0 = max(0, -y0), iy1 = min(WH - 1, I.h - 1 - y0);
+    const bool edges = ix0 > 0 || ix1 < WW - 1 || iy0 > 0 || iy1 < WH - 1;
+
+    if (tid == 0)
+    {
+        tc::mbar_init(mbar, 1);
+        tc::fence_mbar_init();
+    }
+    if (warp == 0)
+    {
+        tc::tmem_alloc(tmem_slot, TMEM_COLS);
+        tc::tmem_relinquish();
+    }
+    for (int i = tid; i < B_BYTES / 16; i += THREADS)
+    {
+        reinterpret_cast<uint4*>(bsmA)[i] = P.bwA[i];
+        reinterpret_cast<uint4*>(bsmB)[i] = P.bwB[i];
+    }
+    for (int i = tid; i < 4 * PADP; i += THREADS)
+    {
+        const int pl = i / (2 * PADP), k = i % (2 * PADP);
+        reinterpret_cast<uint4*>(plane + pl * PLANE_BYTES)[k < PADP ? k : NBLK * 128 + k] = make_uint4(0, 0, 0, 0);
+    }
+    constexpr int PER = WW * WH / THREADS;  // 16
+#pragma unroll
+    for (int k0 = 0; k0 < PER; k0 += 8)
+    {
+        uint4 px[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+        {
+            const int p = tid + (k0 + k) * THREADS;
+            const int wy = p / WW, wx = p - wy * WW;
+            const int gx = clampi(x0 + wx, 0, I.w - 1), gy = clampi(y0 + wy, 0, I.h - 1);
+            px[k] = I.in[static_cast<size_t>(gy) * I.w + gx];
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+        {
+            const int p = tid + (k0 + k) * THREADS;
+            reinterpret_cast<uint4*>(plane + ((p & 1) ? PLANE_BYTES : 0))[PADP + (p >> 1)] = px[k];
+        }
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+    constexpr uint32_t IDESC = tc::idesc_f16(128, 16, BF16);
+    const uint64_t a_desc0 = tc::smem_desc(tc::smem_u32(plane) + (PADP - PPR) * 16, PLANE_BYTES - 16, 128);
+
+    bool ok = true;
+#pragma unroll 1
+    for (int layer = 0; layer < 2; layer++)
+    {
+        if (tid == 0)
+        {
+            const uint64_t b_desc0 = tc::smem_desc(tc::smem_u32(layer ? bsmB : bsmA), 256, 128);
+            for (int b = 0; b < NBLK; b++)
+            {
+                const uint64_t a_desc = a_desc0 + static_cast<uint64_t>(b * 128);
+#pragma unroll
+                for (int dy = 0; dy < 3; dy++)
+#pragma unroll
+                    for (int h = 0; h < 2; h++)
+                        tc::mma_f16(tmem + static_cast<uint32_t>(b * 16), a_desc + static_cast<uint64_t>(dy * PPR + h),
+                                    b_desc0 + static_cast<uint64_t>((2 * dy + h) * 32), IDESC, (dy | h) ? 1u : 0u);
+            }
+            tc::mma_commit(mbar);
+        }
+        __syncwarp();
+        ok = __syncthreads_and((ok && tc::mbar_wait_ns(mbar, static_cast<uint32_t>(layer), kWaitNs)) ? 1 : 0) != 0;
+        tc::fence_after_sync();
+        if (!ok)
+        {
+            if (tid == 0) atomicExch(P.status, 1);
+            break;
+        }
+        if (layer == 0)
+        {
+            // layer A: prelu(conv + b) for window pixels 1 .. W-2 inside the image, in place
+            const int ry0 = max(1, iy0), ry1 = min(WH - 2, iy1), rx0 = max(1, ix0), rx1 = min(WW - 2, ix1);
+            for (int b = 0; b < NBLK; b++)
+            {
+                float v[16];
+                tc::tmem_ld16(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(b * 16), v);
+                tc::tmem_wait_ld();
+                const int r = b * 128 + warp * 32 + lane;
+#pragma unroll
+                for (int k = 0; k < 2; k++)
+                {
+                    const int p = 2 * r + k;
+                    const int y = p / WW, x = p - y * WW;
+                    if (y < ry0 || y > ry1 || x < rx0 || x > rx1) continue;
+                    float sv[8];
+#pragma unroll
+                    for (int c = 0; c < 8; c++) sv[c] = prelu(v[8 * k + c] + P.bA[c], P.aA[c]);
+                    const uint4 val = pack8<BF16>(sv);
+                    auto put = [&](int q) {
+                        reinterpret_cast<uint4*>(plane + ((q & 1) ? PLANE_BYTES : 0))[PADP + (q >> 1)] = val;
+                    };
+                    put(p);
+                    // clamp-to-edge for layer B (only tiles at an image edge)
+                    if (!edges) continue;
+                    const bool xl = x == ix0 && x > 0, xr = x == ix1 && x < WW - 1;
+                    const bool yt = y == iy0 && y > 0, yb = y == iy1 && y < WH - 1;
+                    if (xl) put(p - 1);
+                    if (xr) put(p + 1);
+                    if (yt)
+                    {
+                        put(p - WW);
+                        if (xl) put(p - WW - 1);
+                        if (xr) put(p - WW + 1);
+                    }
+                    if (yb)
+                    {
+                        put(p + WW);
+                        if (xl) put(p + WW - 1);
+                        if (xr) put(p + WW + 1);
+                    }
+                }
+            }
+            tc::fence_proxy_async_smem();
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+        }
+        else
+        {
+            // layer B on the tile: window pixels 2 .. W-3 inside the image
+            for (int b = 0; b < NBLK; b++)
+            {
+                float v[16];
+                tc::tmem_ld16(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(b * 16), v);
+                tc::tmem_wait_ld();
+                const int r = b * 128 + warp * 32 + lane;
+#pragma unroll
+                for (int k = 0; k < 2; k++)
+                {
+                    const int p = 2 * r + k;
+                    const int y = p / WW, x = p - y * WW;
+                    const int gx = x0 + x, gy = y0 + y;
+                    if (y < 2 || y > WH - 3 || x < 2 || x > WW - 3 || gx >= I.w || gy >= I.h) continue;
+                    const size_t o = static_cast<size_t>(gy) * I.w + gx;
+                    float sv[8];
+#pragma unroll
+                    for (int c = 0; c < 8; c++) sv[c] = v[8 * k + c] + P.b[c];
+                    if constexpr (MODE == kPReLU)
+                    {
+#pragma unroll
+                        for (int c = 0; c < 8; c++) sv[c] = prelu(sv[c], P.a[c]);
+                    }
+                    else
+                    {
+                        float sk[8];
+                        unpack8<BF16>(I.in[o], sk);
+#pragma unroll
+                        for (int c = 0; c < 8; c++) sv[c] = fmaf(sv[c], 0.2f, sk[c]);
+                        if constexpr (MODE == kTail)
+                        {
+                            float f[8], t[8];
+                            unpack8<BF16>(I.feat[o], f);
+#pragma unroll
+                            for (int n = 0; n < 8; n++)
+                            {
+                                float u = P.b1[n];
+#pragma unroll
+                                for (int c = 0; c < 8; c++) u = fmaf(sv[c], P.k1[n * 8 + c], u);
+                                t[n] = prelu(u, P.a1[n]) + f[n];
+                            }
+#pragma unroll
+                            for (int n = 0; n < 8; n++) sv[n] = t[n];
+                        }
+                    }
+                    I.out[o] = pack8<BF16>(sv);
+                }
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, TMEM_COLS);
+}
+
 struct HeadParams
 {
     float k[72];
@@ -342,6 +564,23 @@ cudaError_t launch_conv(const ConvParams& p, int tiles, cudaStream_t stream)
         configured = true;
     }
     conv_kernel<MODE, BF16><<<tiles, THREADS, SMEM_REQ, stream>>>(p);
+    return cudaGetLastError();
+}
+
+constexpr int SMEM2 = 2 * PLANE_BYTES + 2 * B_BYTES + 64;
+constexpr int SMEM2_REQ = SMEM2 > 48 * 1024 ? SMEM2 : 48 * 1024;  // at most four CTAs per SM (tensor memory)
+
+template <int MODE, bool BF16>
+cudaError_t launch_conv2(const Conv2Params& p, int tiles, cudaStream_t stream)
+{
+    static bool configured = false;
+    if (!configured)
+    {
+        cudaError_t err = cudaFuncSetAttribute(conv2_kernel<MODE, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_REQ);
+        if (err != cudaSuccess) return err;
+        configured = true;
+    }
+    conv2_kernel<MODE, BF16><<<tiles, THREADS, SMEM2_REQ, stream>>>(p);
     return cudaGetLastError();
 }
 
@@ -455,6 +694,23 @@ cudaError_t prepare_batch(int n, const Plane* in, const Plane* out, ConvParams& 
     return cudaSuccess;
 }
 
+// Tiles of the two-layer launches (TW2 x TH2) for the images of a prepared batch.
+int fill_tiles2(int n, const ConvParams& c, Conv2Params& c2)
+{
+    int tiles = 0;
+    for (int i = 0; i < n; i++)
+    {
+        ConvImg& I = c2.img[i];
+        I.w = c.img[i].w;
+        I.h = c.img[i].h;
+        I.tiles_x = (I.w + TW2 - 1) / TW2;
+        I.tile0 = tiles;
+        tiles += I.tiles_x * ((I.h + TH2 - 1) / TH2);
+    }
+    c2.nimg = n;
+    return tiles;
+}
+
 }  // namespace arnettc
 
 // Runs one ARNet x2 pass over n images in the tensor-core form, every layer
@@ -484,47 +740,46 @@ cudaError_t launch_arnet_tc_batch(const float* kernels, const float* biases, con
     hp.prelu = 0;
     for (int i = 0; i < n; i++) hp.feat[i] = static_cast<uint4*>(maps[3 * i]);
     if ((err = launch_head(hp, bf16, n, stream)) != cudaSuccess) return err;
-    // maps of image i: feat, x, t
-    auto conv = [&](int l, int mode, int src, int dst, int skip) -> cudaError_t {
-        ConvParams c = p;
+    // each residual block as one two-layer launch: maps of image i are
+    // feat, then two maps used in turn (the block's input and output)
+    constexpr int FEAT = 0;
+    Conv2Params c2;
+    std::memset(&c2, 0, sizeof(c2));
+    const int tiles2 = fill_tiles2(n, p, c2);
+    c2.status = status;
+    int cur = FEAT;
+    int l = 1;
+    for (int blk = 0; blk < blocks; blk++)
+    {
+        const bool tail = blk == blocks - 1;
+        const int nxt = cur == 1 ? 2 : 1;
+        Conv2Params c = c2;
         for (int i = 0; i < n; i++)
         {
-            c.img[i].in = static_cast<const uint4*>(maps[3 * i + src]);
-            c.img[i].out = static_cast<uint4*>(maps[3 * i + dst]);
-            c.img[i].skip = skip < 0 ? nullptr : static_cast<const uint4*>(maps[3 * i + skip]);
-            c.img[i].feat = static_cast<const uint4*>(maps[3 * i]);
+            c.img[i].in = static_cast<const uint4*>(maps[3 * i + cur]);
+            c.img[i].out = static_cast<uint4*>(maps[3 * i + nxt]);
+            c.img[i].feat = static_cast<const uint4*>(maps[3 * i + FEAT]);
         }
-        c.bw = static_cast<const uint4*>(packed) + static_cast<size_t>(l - 1) * (B_BYTES / 16);
-        for (int i = 0; i < 8; i++) c.b[i] = biases[8 * l + i];
-        for (int i = 0; i < 8; i++) c.a[i] = mode == kPReLU ? alphas[8 * ((l - 1) / 2) + i] : 0.0f;
-        if (mode == kTail)
+        // layer l: conv + PReLU; layer l+1: 0.2 conv + the block input (+ the 1x1 tail)
+        c.bwA = static_cast<const uint4*>(packed) + static_cast<size_t>(l - 1) * (B_BYTES / 16);
+        c.bwB = static_cast<const uint4*>(packed) + static_cast<size_t>(l) * (B_BYTES / 16);
+        for (int i = 0; i < 8; i++) c.bA[i] = biases[8 * l + i];
+        for (int i = 0; i < 8; i++) c.aA[i] = alphas[8 * ((l - 1) / 2) + i];
+        for (int i = 0; i < 8; i++) c.b[i] = biases[8 * (l + 1) + i];
+        if (tail)
         {
             for (int i = 0; i < 64; i++) c.k1[i] = kernels[72 + 576 * (2 * blocks) + i];
-            for (int i = 0; i < 8; i++) c.b1[i] = biases[8 * (l + 1) + i];
+            for (int i = 0; i < 8; i++) c.b1[i] = biases[8 * (l + 2) + i];
             for (int i = 0; i < 8; i++) c.a1[i] = alphas[8 * blocks + i];
+            err = bf16 ? launch_conv2<kTail, true>(c, tiles2, stream) : launch_conv2<kTail, false>(c, tiles2, stream);
         }
-        cudaError_t e;
-        if (mode == kPReLU) e = bf16 ? launch_conv<kPReLU, true>(c, tiles, stream) : launch_conv<kPReLU, false>(c, tiles, stream);
-        else if (mode == kResidual)
-            e = bf16 ? launch_conv<kResidual, true>(c, tiles, stream) : launch_conv<kResidual, false>(c, tiles, stream);
-        else e = bf16 ? launch_conv<kTail, true>(c, tiles, stream) : launch_conv<kTail, false>(c, tiles, stream);
-        if (e == cudaSuccess) count_launch();
-        return e;
-    };
-    constexpr int FEAT = 0, X = 1, T = 2;
-    // block 1: t = prelu(conv(feat)); x = 0.2 conv(t) + feat
-    int l = 1;
-    if ((err = conv(l++, kPReLU, FEAT, T, -1)) != cudaSuccess) return err;
-    if ((err = conv(l++, kResidual, T, X, FEAT)) != cudaSuccess) return err;
-    // blocks 2 .. B-1: t = prelu(conv(x)); x = 0.2 conv(t) + x (in place: each pixel reads its own skip)
-    for (int i = 0; i < blocks - 2; i++)
-    {
-        if ((err = conv(l++, kPReLU, X, T, -1)) != cudaSuccess) return err;
-        if ((err = conv(l++, kResidual, T, X, X)) != cudaSuccess) return err;
+        else err = bf16 ? launch_conv2<kResidual, true>(c, tiles2, stream) : launch_conv2<kResidual, false>(c, tiles2, stream);
+        if (err != cudaSuccess) return err;
+        count_launch();
+        l += 2;
+        cur = nxt;
     }
-    // block B with the 1x1 + PReLU + feat tail, into x in place
-    if ((err = conv(l++, kPReLU, X, T, -1)) != cudaSuccess) return err;
-    if ((err = conv(l++, kTail, T, X, X)) != cudaSuccess) return err;
+    const int X = cur;  // the last block's output
     l++;  // the 1x1 layer's bias index
     // upscale (FP32)
     for (int i = 0; i < 288; i++) u.k[i] = kernels[72 + 576 * (2 * blocks) + 64 + i];
@@ -571,7 +826,33 @@ cudaError_t launch_acnet8_tc_batch(const float* kernels, const float* biases, co
     for (int i = 0; i < n; i++) hp.feat[i] = static_cast<uint4*>(maps[2 * i]);
     if ((err = launch_head(hp, bf16, n, stream)) != cudaSuccess) return err;
     int a = 0;  // the map holding the current layer's input
-    for (int l = 1; l <= blocks; l++)
+    Conv2Params c2;
+    std::memset(&c2, 0, sizeof(c2));
+    const int tiles2 = fill_tiles2(n, c, c2);
+    c2.status = status;
+    int l = 1;
+    // pairs of layers as one two-layer launch
+    for (; l + 1 <= blocks; l += 2)
+    {
+        Conv2Params q = c2;
+        for (int i = 0; i < n; i++)
+        {
+            q.img[i].in = static_cast<const uint4*>(maps[2 * i + a]);
+            q.img[i].out = static_cast<uint4*>(maps[2 * i + 1 - a]);
+        }
+        q.bwA = static_cast<const uint4*>(packed) + static_cast<size_t>(l - 1) * (B_BYTES / 16);
+        q.bwB = static_cast<const uint4*>(packed) + static_cast<size_t>(l) * (B_BYTES / 16);
+        for (int i = 0; i < 8; i++) q.bA[i] = biases[8 * l + i];
+        for (int i = 0; i < 8; i++) q.aA[i] = alphas[8 * l + i];
+        for (int i = 0; i < 8; i++) q.b[i] = biases[8 * (l + 1) + i];
+        for (int i = 0; i < 8; i++) q.a[i] = alphas[8 * (l + 1) + i];
+        err = bf16 ? launch_conv2<kPReLU, true>(q, tiles2, stream) : launch_conv2<kPReLU, false>(q, tiles2, stream);
+        if (err != cudaSuccess) return err;
+        count_launch();
+        a = 1 - a;
+    }
+    // an odd last layer on its own
+    if (l == blocks)
     {
         for (int i = 0; i < n; i++)
         {
