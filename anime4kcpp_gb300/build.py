@@ -2,9 +2,9 @@
 
 Every CUDA translation unit is compiled for sm_103a only
 (``-gencode arch=compute_103a,code=sm_103a``); host translation units go
-through nvcc to g++.  The ACNetLegacy and ACNet<8> parameters are embedded
-from ``weights/acnet_legacy.bin`` and ``weights/acnet8.bin`` through
-generated C++ sources.  Object files
+through nvcc to g++.  The ACNetLegacy, ACNet<8>, ArtCNN and FSRCNNX
+parameters are embedded from the blobs in ``weights/`` through generated C++
+sources.  Object files
 are compiled in parallel and reused when newer than every source and header.
 
 Usage: python -m anime4kcpp_gb300.build [--force] [--jobs N]
@@ -56,21 +56,21 @@ def _gen_weights():
     return out
 
 
-def _gen_weights_acnet8():
-    """weights/acnet8.bin -> _build/weights_acnet8.cpp (the blob's words as
-    one array; models.cpp walks its per-variant headers)."""
-    src = os.path.join(HERE, "weights", "acnet8.bin")
-    out = os.path.join(BUILD, "weights_acnet8.cpp")
+def _gen_blob_words(name, magic, symbol):
+    """weights/<name>.bin -> _build/weights_<name>.cpp (the blob's words after
+    the magic as one array; models.cpp walks its per-variant headers)."""
+    src = os.path.join(HERE, "weights", name + ".bin")
+    out = os.path.join(BUILD, "weights_%s.cpp" % name)
     if os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src):
         return out
     raw = open(src, "rb").read()
-    if raw[:8] != b"ACGBW8F1":
+    if raw[:8] != magic:
         raise RuntimeError("bad weight blob " + src)
     words = struct.unpack("<%dI" % ((len(raw) - 8) // 4), raw[8:])
-    lines = ["// Generated by anime4kcpp_gb300/build.py from weights/acnet8.bin. Do not edit.",
+    lines = ["// Generated by anime4kcpp_gb300/build.py from weights/%s.bin. Do not edit." % name,
              "#include <cstdint>", "namespace acgb {",
-             "extern const int kAcnet8Words = %d;" % len(words),
-             "extern const uint32_t kAcnet8Blob[] = {"]
+             "extern const int %sWords = %d;" % (symbol, len(words)),
+             "extern const uint32_t %sBlob[] = {" % symbol]
     for i in range(0, len(words), 8):
         lines.append("    " + ", ".join("0x%08xu" % w for w in words[i:i + 8]) + ",")
     lines += ["};", "}  // namespace acgb", ""]
@@ -79,9 +79,17 @@ def _gen_weights_acnet8():
     return out
 
 
+def _gen_weights_acnet8():
+    return _gen_blob_words("acnet8", b"ACGBW8F1", "kAcnet8")
+
+
+def _gen_weights_f3():
+    return _gen_blob_words("artcnn_fsrcnnx", b"ACGBW9F1", "kArtFsr")
+
+
 def _sources():
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
-    return srcs + [_gen_weights(), _gen_weights_acnet8()]
+    return srcs + [_gen_weights(), _gen_weights_acnet8(), _gen_weights_f3()]
 
 
 def _headers():

@@ -164,6 +164,14 @@ cudaError_t launch_acnet8_tc_batch(const float* kernels, const float* biases, co
                                    const void* packed, bool bf16, int n, const Plane* in, const Plane* out,
                                    void* const* maps, int* status, cudaStream_t stream);
 
+// ArtCNN<F> (F = 16, 32) and FSRCNNX<F> (F = 8, 16) x2 passes in plain FP32
+// (one kernel per layer; parameters in the reference blob layout,
+// ArtCNN.hpp:44-56, FSRCNNX.hpp:46-66); maps: three [h][w][F] float arrays.
+cudaError_t launch_artcnn_fp32(const float* kernels, const float* biases, int F, int blocks, const Plane& in, const Plane& out,
+                               float* const maps[3], cudaStream_t stream);
+cudaError_t launch_fsrcnnx_fp32(const float* kernels, const float* biases, const float* alphas, int F, int blocks,
+                                const Plane& in, const Plane& out, float* const maps[3], cudaStream_t stream);
+
 // Merge for chroma resampled by exactly `factor` (2 or 4) on both axes:
 // phase_weights[k*4 + t] is the Catmull-Rom weight of tap t of output phase k,
 // whose first tap is source index + merge_int_phase_offset(factor, k).

@@ -21,6 +21,11 @@ extern const int kAcnetLegacyBiases;
 // floats} and the floats.
 extern const uint32_t kAcnet8Blob[];
 extern const int kAcnet8Words;
+// Generated at build time from weights/artcnn_fsrcnnx.bin: word 0 the variant
+// count (10), then per variant a header {family (1 ArtCNN, 2 FSRCNNX), F,
+// blocks, kind, kernel floats, bias floats, alpha floats} and the floats.
+extern const uint32_t kArtFsrBlob[];
+extern const int kArtFsrWords;
 
 bool parse_model(const char* model, ModelSpec& spec, std::string& error)
 {
@@ -29,10 +34,23 @@ bool parse_model(const char* model, ModelSpec& spec, std::string& error)
     spec = ModelSpec{};
     spec.name = model ? model : "";
     auto has = [&](const char* t) { return s.find(t) != std::string::npos; };
-    if (has("fsrcnnx") || has("artcnn"))
+    if (has("fsrcnnx"))
     {
-        error = "model family not provided by the GB300 backend: " + spec.name;
-        return false;
+        // Processor.cpp:40-55: f16 picks FSRCNNX<16>; "distort" or "dp" the DistortPlus variant
+        spec.family = Family::FSRCNNX;
+        spec.channels = has("f16") ? 16 : 8;
+        spec.blocks = 4;
+        spec.kind = (has("distort") || has("dp")) ? 1 : 0;
+        return true;
+    }
+    if (has("artcnn"))
+    {
+        // Processor.cpp:56-74: f32 picks ArtCNN<32>; "dn" then "ds" pick the variant
+        spec.family = Family::ArtCNN;
+        spec.channels = has("f32") ? 32 : 16;
+        spec.blocks = 4;
+        spec.kind = has("dn") ? 1 : (has("ds") ? 2 : 0);
+        return true;
     }
     if (has("arnet"))
     {
@@ -126,11 +144,11 @@ void arnet_synthetic_params(int blocks, uint64_t seed, ModelParams& out)
 const ModelParams& model_params(const ModelSpec& spec)
 {
     static std::mutex m;
-    static std::map<std::tuple<int, int, int>, ModelParams> cache;
+    static std::map<std::tuple<int, int, int, int>, ModelParams> cache;
     std::lock_guard<std::mutex> lock(m);
     const auto key = spec.family == Family::ACNetLegacy
-                         ? std::make_tuple(static_cast<int>(spec.family), spec.variant, 0)
-                         : std::make_tuple(static_cast<int>(spec.family), spec.blocks, spec.kind);
+                         ? std::make_tuple(static_cast<int>(spec.family), spec.variant, 0, 0)
+                         : std::make_tuple(static_cast<int>(spec.family), spec.blocks, spec.kind, spec.channels);
     auto it = cache.find(key);
     if (it != cache.end()) return it->second;
     ModelParams p;
@@ -162,6 +180,27 @@ const ModelParams& model_params(const ModelSpec& spec)
                 std::memcpy(p.alphas.data(), h + 4 + nk + nb, sizeof(float) * na);
             }
             at += 4 + nk + nb + na;
+        }
+    }
+    else if (spec.family == Family::ArtCNN || spec.family == Family::FSRCNNX)
+    {
+        const uint32_t fam = spec.family == Family::ArtCNN ? 1u : 2u;
+        size_t at = 1;
+        for (uint32_t v = 0; v < kArtFsrBlob[0]; v++)
+        {
+            const uint32_t* h = kArtFsrBlob + at;
+            const size_t nk = h[4], nb = h[5], na = h[6];
+            if (h[0] == fam && static_cast<int>(h[1]) == spec.channels && static_cast<int>(h[3]) == spec.kind)
+            {
+                p.kernels.resize(nk);
+                p.biases.resize(nb);
+                p.alphas.resize(na);
+                std::memcpy(p.kernels.data(), h + 7, sizeof(float) * nk);
+                std::memcpy(p.biases.data(), h + 7 + nk, sizeof(float) * nb);
+                if (na) std::memcpy(p.alphas.data(), h + 7 + nk + nb, sizeof(float) * na);
+                break;
+            }
+            at += 7 + nk + nb + na;
         }
     }
     else

@@ -495,6 +495,22 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
         const ModelParams& mp = model_params(spec_);
         err = launch_arnet_fp32(mp.kernels.data(), mp.biases.data(), mp.alphas.data(), spec_.blocks, in, out, maps, stream);
     }
+    else if (spec_.family == Family::ArtCNN || spec_.family == Family::FSRCNNX)
+    {
+        // the plain FP32 layer pipeline (every precision form)
+        const size_t bytes = static_cast<size_t>(in.w) * in.h * spec_.channels * sizeof(float);
+        float* maps[3];
+        for (int i = 0; i < 3; i++)
+        {
+            if ((err = ts.maps[i].ensure(bytes)) != cudaSuccess) return err;
+            maps[i] = static_cast<float*>(ts.maps[i].ptr);
+        }
+        const ModelParams& mp = model_params(spec_);
+        err = spec_.family == Family::ArtCNN
+                  ? launch_artcnn_fp32(mp.kernels.data(), mp.biases.data(), spec_.channels, spec_.blocks, in, out, maps, stream)
+                  : launch_fsrcnnx_fp32(mp.kernels.data(), mp.biases.data(), mp.alphas.data(), spec_.channels, spec_.blocks, in,
+                                        out, maps, stream);
+    }
     else if (spec_.family == Family::ACNet8)
     {
         const ModelParams& mp = model_params(spec_);
@@ -951,7 +967,8 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
     const bool tcBatch = spec_.family == Family::ACNetLegacy && precision_ != Precision::FP32 && tcKernel_ >= 3 && fused_;
     // ARNet / ACNet<8> in a tensor-core form: single-channel images of one
     // element type run every layer as one launch over all images
-    bool layered = spec_.family != Family::ACNetLegacy && precision_ != Precision::FP32 && arnetTc_ && n > 1 &&
+    bool layered = (spec_.family == Family::ARNet || spec_.family == Family::ACNet8) && precision_ != Precision::FP32 && arnetTc_ &&
+                   n > 1 &&
                    (factor == 2.0 || factor == 4.0);
     for (int i = 0; i < n && layered; i++)
         layered = src[i].c == 1 && src[i].type == src[0].type && dst[i].w == static_cast<int>(factor) * src[i].w &&

@@ -162,7 +162,8 @@ bool Server::check(Job& j, std::string& err)
     {
         if (c > 1) ws += static_cast<double>(y.w) * y.h * c * es;  // Y + UV(A) split
         ws += 2.0 * lw * lh * es;                                     // the luma ping-pong planes
-        if (spec.family != Family::ACNetLegacy) ws += 4.0 * (lw / 2) * (lh / 2) * 32.0;  // work maps of the last pass
+        if (spec.family != Family::ACNetLegacy)  // work maps of the last pass
+            ws += 4.0 * (lw / 2) * (lh / 2) * 4.0 * (spec.channels > 8 ? spec.channels : 8);
         if (s.planes > 1) ws += static_cast<double>(y.w) * y.h * es;  // shifted Y
     }
     j.bytes = io + static_cast<size_t>(ws);

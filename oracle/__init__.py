@@ -27,6 +27,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 WEIGHTS_BLOB = os.path.join(ROOT, "anime4kcpp_gb300", "weights", "acnet_legacy.bin")
 ACNET8_BLOB = os.path.join(ROOT, "anime4kcpp_gb300", "weights", "acnet8.bin")
+F3_BLOB = os.path.join(ROOT, "anime4kcpp_gb300", "weights", "artcnn_fsrcnnx.bin")
 
 U8, U16, F32 = 0x001, 0x002, 0x204
 _TYPE_OF = {np.dtype(np.uint8): U8, np.dtype(np.uint16): U16, np.dtype(np.float32): F32}
@@ -61,6 +62,8 @@ def lib():
             L.orc_arnet_x2_f64.argtypes = [vp, i, i, i, i, dp, fp, fp, fp, i, i]
             L.orc_acnet8_x2.argtypes = [vp, i, i, i, i, vp, i, fp, fp, fp, i, i]
             L.orc_acnet8_x2_f64.argtypes = [vp, i, i, i, i, dp, fp, fp, fp, i, i]
+            L.orc_artcnn_x2.argtypes = [vp, i, i, i, i, vp, i, fp, fp, i, i, i]
+            L.orc_fsrcnnx_x2.argtypes = [vp, i, i, i, i, vp, i, fp, fp, fp, i, i, i]
             L.orc_rgb2yuv.argtypes = [vp, i, i, i, i, i, vp, i, vp, i]
             L.orc_yuv2rgb.argtypes = [vp, i, vp, i, i, i, i, i, vp, i]
             L.orc_resize.argtypes = [vp, i, i, i, i, i, vp, i, i, i, i]
@@ -68,7 +71,7 @@ def lib():
             L.orc_resize_coeffs.argtypes = [i, i, i, vp, vp, i]
             L.orc_arnet_synth.argtypes = [i, ctypes.c_uint64, fp, fp, fp]
             for fn in ("orc_acnet_legacy_x2", "orc_acnet_legacy_x2_f64", "orc_arnet_x2", "orc_arnet_x2_f64",
-                       "orc_acnet8_x2", "orc_acnet8_x2_f64",
+                       "orc_acnet8_x2", "orc_acnet8_x2_f64", "orc_artcnn_x2", "orc_fsrcnnx_x2",
                        "orc_rgb2yuv", "orc_yuv2rgb", "orc_resize", "orc_resize_mt", "orc_resize_coeffs", "orc_arnet_synth"):
                 getattr(L, fn).restype = ctypes.c_int
             _lib = L
@@ -110,10 +113,11 @@ def _plane(a):
 # ------------------------------------------------------------------ models
 
 def parse_model(name):
-    """Model string -> (family, variant) following Processor.cpp:26-187 for the
-    ACNetLegacy, ACNet<8> and ARNet families.  Returns ("acnet_legacy", idx
-    0..4) with 0=GAN, 1..4=HDN0..3, ("acnet8", (blocks, kind)) or ("arnet",
-    (blocks, kind)); kind 0 normal, 1 HDN, 2 Box, 3 Box-HDN."""
+    """Model string -> (family, variant) following Processor.cpp:26-187.
+    Returns ("acnet_legacy", idx 0..4) with 0=GAN, 1..4=HDN0..3,
+    ("acnet8", (blocks, kind)) or ("arnet", (blocks, kind)) with kind 0
+    normal, 1 HDN, 2 Box, 3 Box-HDN, ("artcnn", (F, kind 0 normal / 1 DN /
+    2 DS)) or ("fsrcnnx", (F, kind 0 normal / 1 DistortPlus))."""
     s = (name or "").lower()
     if "arnet" in s:
         box = "box" in s
@@ -134,8 +138,12 @@ def parse_model(name):
                     idx = 1 + int(ch)
                     break
         return "acnet_legacy", idx
-    if "fsrcnnx" in s or "artcnn" in s:
-        raise ValueError("model family outside this backend's scope: %r" % name)
+    if "fsrcnnx" in s:
+        # Processor.cpp:40-55
+        return "fsrcnnx", (16 if "f16" in s else 8, 1 if ("distort" in s or "dp" in s) else 0)
+    if "artcnn" in s:
+        # Processor.cpp:56-74
+        return "artcnn", (32 if "f32" in s else 16, 1 if "dn" in s else (2 if "ds" in s else 0))
     if "acnet" in s:
         # Processor.cpp:146-184: b4, then b8, then b18; B8 by default.
         blocks = 8
@@ -194,6 +202,25 @@ def acnet8_weights(blocks, kind):
     return _weights_cache["acnet8"][(blocks, kind)]
 
 
+def f3_weights(family, F, kind):
+    """(kernels, biases, alphas) float32 of a trained ArtCNN ("artcnn") or
+    FSRCNNX ("fsrcnnx") variant, read from the blob extracted from the
+    reference's ArtCNN.p / FSRCNNX.p (4 blocks each)."""
+    if "f3" not in _weights_cache:
+        raw = open(F3_BLOB, "rb").read()
+        assert raw[:8] == b"ACGBW9F1"
+        n = int(np.frombuffer(raw[8:12], dtype="<u4")[0])
+        at, table = 12, {}
+        for _ in range(n):
+            fam, f, blocks, k, nk, nb, na = (int(x) for x in np.frombuffer(raw[at:at + 28], dtype="<u4"))
+            v = np.frombuffer(raw[at + 28:at + 28 + 4 * (nk + nb + na)], dtype="<f4")
+            table[(fam, f, k)] = (np.ascontiguousarray(v[:nk]), np.ascontiguousarray(v[nk:nk + nb]),
+                                  np.ascontiguousarray(v[nk + nb:]) if na else np.zeros(1, np.float32))
+            at += 28 + 4 * (nk + nb + na)
+        _weights_cache["f3"] = table
+    return _weights_cache["f3"][(1 if family == "artcnn" else 2, F, kind)]
+
+
 # --------------------------------------------------------------- primitives
 
 def luma_x2(y, model, threads=0, f64=False):
@@ -223,6 +250,13 @@ def luma_x2(y, model, threads=0, f64=False):
             k, b, a = acnet8_weights(*var)
             rc = lib().orc_acnet8_x2(_p(y), w, h, y.strides[0], t, _p(out), out.strides[0], _p(k), _p(b), _p(a), var[0],
                                      threads)
+        elif fam == "artcnn":
+            k, b, _ = f3_weights(fam, *var)
+            rc = lib().orc_artcnn_x2(_p(y), w, h, y.strides[0], t, _p(out), out.strides[0], _p(k), _p(b), var[0], 4, threads)
+        elif fam == "fsrcnnx":
+            k, b, a = f3_weights(fam, *var)
+            rc = lib().orc_fsrcnnx_x2(_p(y), w, h, y.strides[0], t, _p(out), out.strides[0], _p(k), _p(b), _p(a), var[0], 4,
+                                      threads)
         else:
             k, b, a = arnet_weights(*var)
             rc = lib().orc_arnet_x2(_p(y), w, h, y.strides[0], t, _p(out), out.strides[0], _p(k), _p(b), _p(a), var[0], threads)

@@ -21,7 +21,7 @@
  *       :290-342 conv3x3_pixelshuffle, :344-393 conv3x3_deconv2x2
  *   core/internal/AC/Core/Internal/Processor/CPU/Generic.hpp:19-81  summation order
  *   core/src/processor/cpu/CPUProcessor.cpp:1371-1390 (ACNetLegacy), :1417-1436 (ACNet<8>),
- *       :1464-1491 (ARNet)
+ *       :1464-1491 (ARNet), :1519-1600 (ArtCNN<16/32>), :1629-1715 (FSRCNNX<8/16>)
  *   core/src/ImageProcess.cpp:39-61 rgb2yuv, :114-138 rgba2yuva,
  *       :192-215 yuv2rgb, :276-308 yuva2rgba
  *   core/src/ImageResize.cpp:62-83,127-134,136-273  resize filters (the
@@ -436,6 +436,231 @@ int orc_acnet8_x2(const void* src, int w, int h, int sstride, int type,
     parallel_rows(lp_rows, &cp, h, threads);
     free(a);
     free(b);
+    return 0;
+}
+
+/* ---------------------------- generic-width layers (ArtCNN, FSRCNNX) */
+
+/* conv KxK (K = 3 or 5) 1 -> cout from the input plane, taps clamped to the
+ * plane (Common.hpp:166-197 conv3x3_cin1, :196-222 conv5x5_cin1), Generic
+ * conv_cin1 order (Generic.hpp:59-66: left-folded dot, then + bias), then
+ * the activation. */
+typedef struct {
+    const void* src; int w, h, sstride, type;
+    float* dst; int cout, K;
+    const float* k; const float* b; int act; const float* alphas;
+} g0_ctx;
+static void g0_rows(void* p, int y0, int y1)
+{
+    g0_ctx* c = (g0_ctx*)p;
+    const int K = c->K, R = K / 2;
+    for (int y = y0; y < y1; y++)
+        for (int x = 0; x < c->w; x++)
+        {
+            float r[25];
+            for (int i = 0; i < K; i++)
+            {
+                int yy = y + i - R;
+                yy = yy < 0 ? 0 : (yy > c->h - 1 ? c->h - 1 : yy);
+                for (int j = 0; j < K; j++)
+                {
+                    int xx = x + j - R;
+                    xx = xx < 0 ? 0 : (xx > c->w - 1 ? c->w - 1 : xx);
+                    r[i * K + j] = to_float(rowp(c->src, c->sstride, yy), (size_t)xx, c->type);
+                }
+            }
+            float* out = c->dst + ((size_t)y * c->w + x) * c->cout;
+            for (int n = 0; n < c->cout; n++)
+            {
+                const float* kp = c->k + n * K * K;
+                float s = r[0] * kp[0];
+                for (int t = 1; t < K * K; t++) { float m = r[t] * kp[t]; s = s + m; }
+                s = s + c->b[n];
+                out[n] = activate(s, c->act, c->alphas, n);
+            }
+        }
+}
+
+/* Generic conv<cin, cout, 9> (Generic.hpp:70-80): per output channel n, sum
+ * from 0 over input channels c of the left-folded tap products
+ * rp[p][c] * k[n*cin*9 + p*cin + c], then + bias. */
+static inline void convg_sum(const float* const* rp, const float* k, const float* b, int cin, int cout, float* out)
+{
+    for (int n = 0; n < cout; n++)
+    {
+        const float* kn = k + n * cin * 9;
+        float sum = 0.0f;
+        for (int c = 0; c < cin; c++)
+        {
+            float blk = rp[0][c] * kn[c];
+            for (int p = 1; p < 9; p++) { float m = rp[p][c] * kn[p * cin + c]; blk = blk + m; }
+            sum = sum + blk;
+        }
+        out[n] = sum + b[n];
+    }
+}
+
+/* conv3x3 cin -> cout + activation, optional residual sum*scale + id
+ * (Common.hpp:116-164). */
+typedef struct {
+    const float* src; float* dst; int w, h, cin, cout;
+    const float* k; const float* b; int act; const float* alphas;
+    const float* id; float scale;
+} gc_ctx;
+static void gc_rows(void* p, int y0, int y1)
+{
+    gc_ctx* c = (gc_ctx*)p;
+    float sum[32];
+    for (int y = y0; y < y1; y++)
+        for (int x = 0; x < c->w; x++)
+        {
+            int xs[3], ys[3];
+            taps3x3(x, y, c->w, c->h, xs, ys);
+            const float* rp[9];
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++)
+                    rp[i * 3 + j] = c->src + ((size_t)ys[i] * c->w + xs[j]) * c->cin;
+            convg_sum(rp, c->k, c->b, c->cin, c->cout, sum);
+            size_t off = ((size_t)y * c->w + x) * c->cout;
+            for (int n = 0; n < c->cout; n++)
+            {
+                float v = activate(sum[n], c->act, c->alphas, n);
+                if (c->id) { float m = v * c->scale; v = m + c->id[off + n]; }
+                c->dst[off + n] = v;
+            }
+        }
+}
+
+/* FSRCNNX tail (Common.hpp:223-288 with postactive1x1): conv3x3 F -> F +
+ * PReLU(a1), conv1x1 F -> F + bias, + feat, then PReLU(a2). */
+typedef struct {
+    const float* src; float* dst; int w, h, F;
+    const float* k1; const float* b1; const float* a1;
+    const float* k2; const float* b2; const float* a2; const float* feat;
+} gt_ctx;
+static void gt_rows(void* p, int y0, int y1)
+{
+    gt_ctx* c = (gt_ctx*)p;
+    const int F = c->F;
+    float buf[32];
+    for (int y = y0; y < y1; y++)
+        for (int x = 0; x < c->w; x++)
+        {
+            int xs[3], ys[3];
+            taps3x3(x, y, c->w, c->h, xs, ys);
+            const float* rp[9];
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++)
+                    rp[i * 3 + j] = c->src + ((size_t)ys[i] * c->w + xs[j]) * F;
+            convg_sum(rp, c->k1, c->b1, F, F, buf);
+            for (int n = 0; n < F; n++) buf[n] = activate(buf[n], ACT_PRELU, c->a1, n);
+            size_t off = ((size_t)y * c->w + x) * F;
+            for (int n = 0; n < F; n++)
+            {
+                const float* kn = c->k2 + n * F;
+                float sum = 0.0f;
+                for (int i = 0; i < F; i++) { float m = buf[i] * kn[i]; sum = sum + m; }
+                sum = sum + c->b2[n];
+                float m = sum * 1.0f;
+                sum = m + c->feat[off + n];
+                c->dst[off + n] = activate(sum, ACT_PRELU, c->a2, n);
+            }
+        }
+}
+
+/* conv3x3 F -> 4, identity, pixel shuffle 2x2, fromFloat; no nearest add
+ * (Common.hpp:290-342 without the interpolation argument). */
+typedef struct {
+    const float* src; int w, h, F;
+    void* dst; int dstride, type;
+    const float* k; const float* b;
+} gp_ctx;
+static void gp_rows(void* p, int y0, int y1)
+{
+    gp_ctx* c = (gp_ctx*)p;
+    for (int y = y0; y < y1; y++)
+        for (int x = 0; x < c->w; x++)
+        {
+            int xs[3], ys[3];
+            taps3x3(x, y, c->w, c->h, xs, ys);
+            const float* rp[9];
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++)
+                    rp[i * 3 + j] = c->src + ((size_t)ys[i] * c->w + xs[j]) * c->F;
+            float s[4];
+            convg_sum(rp, c->k, c->b, c->F, 4, s);
+            for (int n = 0; n < 4; n++)
+                from_float(rowpw(c->dst, c->dstride, 2 * y + (n >> 1)), (size_t)(2 * x + (n & 1)), c->type, s[n]);
+        }
+}
+
+/* ArtCNN<F> x2 pass, CPUProcessor.cpp:1519-1545 / :1574-1600 (F = 16 / 32): head conv3x3
+ * 1->F identity -> feat; conv F->F + ReLU, blocks-1 more; conv F->F identity
+ * + feat; conv F->4 + pixel shuffle.  Offsets ArtCNN.hpp:44-56. */
+int orc_artcnn_x2(const void* src, int w, int h, int sstride, int type,
+                  void* dst, int dstride, const float* kernels, const float* biases, int F, int blocks, int threads)
+{
+    if (!src || !dst || w <= 0 || h <= 0 || blocks < 1 || F < 1 || F > 32) return -22;
+    size_t n = (size_t)w * h * F;
+    float* feat = (float*)malloc(n * sizeof(float));
+    float* a = (float*)malloc(n * sizeof(float));
+    float* b = (float*)malloc(n * sizeof(float));
+    if (!feat || !a || !b) { free(feat); free(a); free(b); return -12; }
+    g0_ctx c0 = { src, w, h, sstride, type, feat, F, 3, kernels, biases, ACT_IDENTITY, NULL };
+    parallel_rows(g0_rows, &c0, h, threads);
+    const float* in = feat;
+    int l = 1;
+    for (int i = 0; i < blocks; i++, l++)
+    {
+        gc_ctx c = { in, a, w, h, F, F, kernels + F * 9 + F * F * 9 * (l - 1), biases + F * l, ACT_RELU, NULL, NULL, 0.0f };
+        parallel_rows(gc_rows, &c, h, threads);
+        in = a; float* t = a; a = b; b = t;
+    }
+    {
+        gc_ctx c = { in, a, w, h, F, F, kernels + F * 9 + F * F * 9 * (l - 1), biases + F * l, ACT_IDENTITY, NULL, feat, 1.0f };
+        parallel_rows(gc_rows, &c, h, threads);
+        in = a; l++;
+    }
+    gp_ctx cp = { in, w, h, F, dst, dstride, type, kernels + F * 9 + F * F * 9 * (l - 1), biases + F * l };
+    parallel_rows(gp_rows, &cp, h, threads);
+    free(feat); free(a); free(b);
+    return 0;
+}
+
+/* FSRCNNX<F> x2 pass, CPUProcessor.cpp:1629-1657 / :1687-1715 (F = 8 / 16): head conv5x5
+ * 1->F identity -> feat; conv F->F + PReLU, blocks-2 more; conv F->F + PReLU
+ * fused with conv1x1 F->F + feat + PReLU; conv F->4 + pixel shuffle.
+ * Offsets FSRCNNX.hpp:46-66 (slopes of layer l at F (l-1)). */
+int orc_fsrcnnx_x2(const void* src, int w, int h, int sstride, int type,
+                   void* dst, int dstride, const float* kernels, const float* biases, const float* alphas,
+                   int F, int blocks, int threads)
+{
+    if (!src || !dst || w <= 0 || h <= 0 || blocks < 2 || F < 1 || F > 32) return -22;
+    size_t n = (size_t)w * h * F;
+    float* feat = (float*)malloc(n * sizeof(float));
+    float* a = (float*)malloc(n * sizeof(float));
+    float* b = (float*)malloc(n * sizeof(float));
+    if (!feat || !a || !b) { free(feat); free(a); free(b); return -12; }
+    g0_ctx c0 = { src, w, h, sstride, type, feat, F, 5, kernels, biases, ACT_IDENTITY, NULL };
+    parallel_rows(g0_rows, &c0, h, threads);
+    const float* in = feat;
+    int l = 1;
+    for (; l < blocks; l++)
+    {
+        gc_ctx c = { in, a, w, h, F, F, kernels + F * 25 + F * F * 9 * (l - 1), biases + F * l, ACT_PRELU,
+                     alphas + F * (l - 1), NULL, 0.0f };
+        parallel_rows(gc_rows, &c, h, threads);
+        in = a; float* t = a; a = b; b = t;
+    }
+    {
+        gt_ctx c = { in, a, w, h, F, kernels + F * 25 + F * F * 9 * (l - 1), biases + F * l, alphas + F * (l - 1),
+                     kernels + F * 25 + F * F * 9 * blocks, biases + F * (l + 1), alphas + F * l, feat };
+        parallel_rows(gt_rows, &c, h, threads);
+        in = a; l += 2;
+    }
+    gp_ctx cp = { in, w, h, F, dst, dstride, type, kernels + F * 25 + F * F * 9 * blocks + F * F, biases + F * l };
+    parallel_rows(gp_rows, &cp, h, threads);
+    free(feat); free(a); free(b);
     return 0;
 }
 

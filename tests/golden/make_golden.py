@@ -4,8 +4,8 @@ Runs where the Anime4KCPP sources were compiled into ``oracle/_ref`` (``make -C
 oracle ref``).  Every case feeds a seeded synthetic input to the reference's
 ``ac::core::Processor`` (CPU, Generic backend = arch 1, and its automatic ISA
 choice = arch 0) and stores input and outputs in ``golden.npz`` with the case
-list in ``golden.json``.  ACNetLegacy and ACNet<8> cases use the reference's
-trained parameters.  The reference's ARNet parameters are absent, so the
+list in ``golden.json``.  ACNetLegacy, ACNet<8>, ArtCNN and FSRCNNX cases use
+the reference's trained parameters.  The reference's ARNet parameters are absent, so the
 ARNet cases use the seeded synthetic ARNet parameters of ``oracle``; the chroma
 resize inside the reference build is this project's restatement (the
 reference's stb_image_resize2 is not vendored), so RGB cases pin the
@@ -55,6 +55,14 @@ CASES = [
     ("gray_u8_acnet_f8b8_x4", "luma", (9, 14), "uint8", "acnet-f8b8", 4.0, 35),
     ("rgb_u8_acnet_f8b8_hdn_x2", "rgb", (14, 18), "uint8", "acnet-f8b8-hdn", 2.0, 36),
     ("gray_u8_acnet_1x3_x2", "luma", (1, 3), "uint8", "acnet-f8b4-hdn", 2.0, 37),
+    ("gray_u8_artcnn_c4f16_x2", "luma", (21, 29), "uint8", "artcnn-c4f16", 2.0, 38),
+    ("gray_f32_artcnn_c4f32_ds_x2", "luma", (11, 17), "float32", "artcnn-c4f32-ds", 2.0, 39),
+    ("gray_u16_artcnn_c4f16_dn_x2", "luma10", (13, 15), "uint16", "artcnn-c4f16-dn", 2.0, 40),
+    ("rgb_u8_artcnn_c4f32_x2", "rgb", (12, 14), "uint8", "artcnn-c4f32", 2.0, 41),
+    ("gray_u8_fsrcnnx_f8_x2", "luma", (19, 23), "uint8", "fsrcnnx-f8", 2.0, 42),
+    ("gray_u16_fsrcnnx_f16_dp_x2", "luma10", (13, 17), "uint16", "fsrcnnx-f16-dp", 2.0, 43),
+    ("gray_u8_fsrcnnx_f8_x4", "luma", (9, 11), "uint8", "fsrcnnx-f8-distort", 4.0, 44),
+    ("gray_u8_fsrcnnx_2x3_x2", "luma", (2, 3), "uint8", "fsrcnnx-f16", 2.0, 45),
 ]
 
 

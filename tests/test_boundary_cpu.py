@@ -68,8 +68,9 @@ def test_model_string_parsing(lib):
     for s, var in [("acnet-legacy-hdn", 1), ("ACNet-Legacy-HDN2", 3), ("acnet-legacy", 0), ("whatever", 0)]:
         k, _, _ = ac.model_params(s)
         assert np.array_equal(k, oracle.acnet_legacy_weights(var)[0])
-    with pytest.raises(ValueError):
-        ac.model_params("artcnn-c4f16")
+    # every family of the reference resolves (Processor.cpp:34-184)
+    for s in ("artcnn-c4f16", "fsrcnnx-f8", "arnet-b8", "acnet-f8b8"):
+        assert ac.model_params(s)[0].size > 0
 
 
 def test_cpu_and_opencl_types_are_refused(lib):
@@ -80,10 +81,29 @@ def test_cpu_and_opencl_types_are_refused(lib):
         assert p.type() == code
 
 
-def test_unsupported_family_is_refused(lib):
-    for m in ("artcnn-c4f16", "fsrcnnx-f8b4"):
-        p = ac.Processor("cuda", 0, m)
-        assert not p.ok() and "not provided" in p.error()
+def test_artcnn_fsrcnnx_parameters_match_the_reference_blob(lib):
+    """ArtCNN<16/32> (C4 x normal/DN/DS) and FSRCNNX<8/16> (B4 x normal /
+    DistortPlus) resolve as the reference's model strings do and carry its
+    trained parameters in the sizes of ArtCNN.hpp:28-31, FSRCNNX.hpp:28-33."""
+    for F in (16, 32):
+        for kind, tag in enumerate(("", "-dn", "-ds")):
+            name = "artcnn-c4f%d%s" % (F, tag)
+            assert oracle.parse_model(name) == ("artcnn", (F, kind))
+            k, b, a = ac.model_params(name)
+            assert (k.size, b.size, a.size) == (F * 9 + F * F * 9 * 5 + F * 36, F + 5 * F + 4, 0)
+            rk, rb, _ = oracle.f3_weights("artcnn", F, kind)
+            assert np.array_equal(k, rk) and np.array_equal(b, rb)
+    for F in (8, 16):
+        for kind, tag in enumerate(("", "-distortplus")):
+            name = "fsrcnnx-f%d%s" % (F, tag)
+            assert oracle.parse_model(name) == ("fsrcnnx", (F, kind))
+            k, b, a = ac.model_params(name)
+            assert (k.size, b.size, a.size) == (F * 25 + F * F * 9 * 4 + F * F + F * 36, F + 5 * F + 4, 5 * F)
+            rk, rb, ra = oracle.f3_weights("fsrcnnx", F, kind)
+            assert np.array_equal(k, rk) and np.array_equal(b, rb) and np.array_equal(a, ra)
+    # "dp" is DistortPlus too, and an unknown string is ACNetLegacy GAN (Processor.cpp:186)
+    assert np.array_equal(ac.model_params("FSRCNNX-dp")[0], oracle.f3_weights("fsrcnnx", 8, 1)[0])
+    assert ac.model_params("no-such-model")[0].size == 4712
 
 
 def test_acnet8_parameters_match_the_reference_blob(lib):

@@ -111,11 +111,13 @@ def test_budget_admission_and_rejection():
 def test_malformed_jobs_are_rejected():
     srv = ac.Server(0, "fp16", hbm_budget_gb=1.0, workers=1)
     x = synthetic.rgb_u8(32, 32, seed=1)
-    # a family outside this backend (unknown strings fall back to the default
-    # model, as the reference's model-string parsing does)
-    t = srv.submit(x, np.zeros((64, 64, 3), np.uint8), "artcnn-c4f16", 2.0)
+    # every family of the reference is served (here ArtCNN, FP32 pipeline):
+    # the job gives the ordinary processor's bytes
+    out = np.zeros((64, 64, 3), np.uint8)
+    t = srv.submit(x, out, "artcnn-c4f16", 2.0)
     r = srv.wait(t)
-    assert r["status"] == -2 and "not provided" in r["error"]
+    assert r["status"] == 0, r["error"]
+    assert np.array_equal(out, ac.Processor("cuda", 0, "artcnn-c4f16", precision="fp16").process(x, 2.0))
     t = srv.submit(x, np.zeros((64, 64, 3), np.uint16), "acnet-legacy-hdn0", 2.0)
     r = srv.wait(t)
     assert r["status"] == -2 and "differ" in r["error"]
