@@ -10,10 +10,13 @@
 //               conv3x3 F->4, pixel shuffle
 // All taps clamp to the map's edge.  The F-channel FP32 maps live in HBM
 // ([h][w][F]); a block of 256 threads computes a 32x8 pixel tile from its
-// haloed input tile staged in shared memory, one pixel per thread, with the
-// layer's weights in the constant bank (a by-value kernel parameter; a
-// 32-channel layer runs as two launches of 16 output channels each, so its
-// weights stay within the parameter limit).
+// haloed input tile staged in shared memory, one pixel per thread.  A layer's
+// weights travel as a by-value kernel parameter (a 32-channel layer runs as
+// two launches of 16 output channels each, so they stay within the parameter
+// limit); layers of more than 1,024 weights (the 16/32-channel ones) copy
+// them into shared memory per block, where the inner loop reads four channels
+// at a time as warp-wide broadcasts, the 8-channel ones use them straight from
+// the constant bank (they fit its cache).
 #include <cuda_runtime.h>
 
 #include "device_common.cuh"
@@ -83,6 +86,10 @@ struct ConvW
     float a[NB];            // PReLU slopes
 };
 
+// Whether a layer's weights go to shared memory (more than 1,024 floats).
+template <int CIN, int NB>
+constexpr bool kSmemWeights = NB * 9 * CIN > 1024;
+
 // Stage the haloed tile (SX x SY pixels of CIN floats, clamped) into smem.
 template <int CIN>
 __device__ __forceinline__ void stage(float4* s, const float* in, int w, int h, int x0, int y0)
@@ -106,8 +113,12 @@ __global__ void __launch_bounds__(THREADS) conv_kernel(const __grid_constant__ C
 {
     extern __shared__ float4 s4[];
     constexpr int V = CIN / 4;
+    float4* wsm = s4 + SX * SY * V;  // weights: [n][tap][CIN / 4]
     const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
     stage<CIN>(s4, in, w, h, x0, y0);
+    if constexpr (kSmemWeights<CIN, NB>)
+        for (int i = threadIdx.x; i < NB * 9 * V; i += THREADS)
+            wsm[i] = make_float4(W.k[4 * i], W.k[4 * i + 1], W.k[4 * i + 2], W.k[4 * i + 3]);
     __syncthreads();
     const int tx = threadIdx.x % BX, ty = threadIdx.x / BX;
     const int x = x0 + tx, y = y0 + ty;
@@ -115,19 +126,46 @@ __global__ void __launch_bounds__(THREADS) conv_kernel(const __grid_constant__ C
     float acc[NB];
 #pragma unroll
     for (int n = 0; n < NB; n++) acc[n] = W.b[n];
-#pragma unroll
-    for (int p = 0; p < 9; p++)
+    if constexpr (!kSmemWeights<CIN, NB>)
     {
-        const float4* px = s4 + ((ty + p / 3) * SX + tx + p % 3) * V;
+        // weights straight from the constant bank
 #pragma unroll
-        for (int v = 0; v < V; v++)
+        for (int p = 0; p < 9; p++)
         {
-            const float4 u = px[v];
-            const float xv[4] = {u.x, u.y, u.z, u.w};
+            const float4* px = s4 + ((ty + p / 3) * SX + tx + p % 3) * V;
 #pragma unroll
-            for (int j = 0; j < 4; j++)
+            for (int v = 0; v < V; v++)
+            {
+                const float4 u = px[v];
+                const float xv[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
-                for (int n = 0; n < NB; n++) acc[n] = fmaf(xv[j], W.k[n * 9 * CIN + p * CIN + 4 * v + j], acc[n]);
+                for (int j = 0; j < 4; j++)
+#pragma unroll
+                    for (int n = 0; n < NB; n++) acc[n] = fmaf(xv[j], W.k[n * 9 * CIN + p * CIN + 4 * v + j], acc[n]);
+            }
+        }
+    }
+    else
+    {
+#pragma unroll 1
+        for (int p = 0; p < 9; p++)
+        {
+            const float4* px = s4 + ((ty + p / 3) * SX + tx + p % 3) * V;
+            const float4* wp = wsm + p * V;
+#pragma unroll 2
+            for (int v = 0; v < V; v++)
+            {
+                const float4 u = px[v];
+#pragma unroll
+                for (int n = 0; n < NB; n++)
+                {
+                    const float4 k4 = wp[n * 9 * V + v];
+                    acc[n] = fmaf(u.x, k4.x, acc[n]);
+                    acc[n] = fmaf(u.y, k4.y, acc[n]);
+                    acc[n] = fmaf(u.z, k4.z, acc[n]);
+                    acc[n] = fmaf(u.w, k4.w, acc[n]);
+                }
+            }
         }
     }
     const size_t o = (static_cast<size_t>(y) * w + x) * cout + n0;
@@ -162,8 +200,12 @@ __global__ void __launch_bounds__(THREADS) tail_kernel(const __grid_constant__ T
 {
     extern __shared__ float4 s4[];
     constexpr int V = F / 4;
+    float4* wsm = s4 + SX * SY * V;  // 3x3 weights: [n][tap][F / 4]
     const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
     stage<F>(s4, in, w, h, x0, y0);
+    if constexpr (kSmemWeights<F, F>)
+        for (int i = threadIdx.x; i < F * 9 * V; i += THREADS)
+            wsm[i] = make_float4(W.c3.k[4 * i], W.c3.k[4 * i + 1], W.c3.k[4 * i + 2], W.c3.k[4 * i + 3]);
     __syncthreads();
     const int tx = threadIdx.x % BX, ty = threadIdx.x / BX;
     const int x = x0 + tx, y = y0 + ty;
@@ -171,19 +213,45 @@ __global__ void __launch_bounds__(THREADS) tail_kernel(const __grid_constant__ T
     float acc[F];
 #pragma unroll
     for (int n = 0; n < F; n++) acc[n] = W.c3.b[n];
-#pragma unroll
-    for (int p = 0; p < 9; p++)
+    if constexpr (!kSmemWeights<F, F>)
     {
-        const float4* px = s4 + ((ty + p / 3) * SX + tx + p % 3) * V;
 #pragma unroll
-        for (int v = 0; v < V; v++)
+        for (int p = 0; p < 9; p++)
         {
-            const float4 u = px[v];
-            const float xv[4] = {u.x, u.y, u.z, u.w};
+            const float4* px = s4 + ((ty + p / 3) * SX + tx + p % 3) * V;
 #pragma unroll
-            for (int j = 0; j < 4; j++)
+            for (int v = 0; v < V; v++)
+            {
+                const float4 u = px[v];
+                const float xv[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
-                for (int n = 0; n < F; n++) acc[n] = fmaf(xv[j], W.c3.k[n * 9 * F + p * F + 4 * v + j], acc[n]);
+                for (int j = 0; j < 4; j++)
+#pragma unroll
+                    for (int n = 0; n < F; n++) acc[n] = fmaf(xv[j], W.c3.k[n * 9 * F + p * F + 4 * v + j], acc[n]);
+            }
+        }
+    }
+    else
+    {
+#pragma unroll 1
+        for (int p = 0; p < 9; p++)
+        {
+            const float4* px = s4 + ((ty + p / 3) * SX + tx + p % 3) * V;
+            const float4* wp = wsm + p * V;
+#pragma unroll 2
+            for (int v = 0; v < V; v++)
+            {
+                const float4 u = px[v];
+#pragma unroll
+                for (int n = 0; n < F; n++)
+                {
+                    const float4 k4 = wp[n * 9 * V + v];
+                    acc[n] = fmaf(u.x, k4.x, acc[n]);
+                    acc[n] = fmaf(u.y, k4.y, acc[n]);
+                    acc[n] = fmaf(u.z, k4.z, acc[n]);
+                    acc[n] = fmaf(u.w, k4.w, acc[n]);
+                }
+            }
         }
     }
 #pragma unroll
@@ -253,6 +321,13 @@ constexpr int stage_bytes()
     return SX * SY * CIN * 4;
 }
 
+// input tile (+ NB output channels' weights when they go to shared memory)
+template <int CIN, int NB>
+constexpr int conv_bytes()
+{
+    return stage_bytes<CIN>() + (kSmemWeights<CIN, NB> ? NB * 9 * CIN * 4 : 0);
+}
+
 template <class Kern>
 cudaError_t allow_smem(Kern kern, int bytes)
 {
@@ -266,7 +341,7 @@ cudaError_t conv_layer(const float* k, const float* b, const float* a, const flo
 {
     constexpr int NB = F > 16 ? 16 : F;
     const dim3 grid((w + BX - 1) / BX, (h + BY - 1) / BY);
-    cudaError_t err = allow_smem(conv_kernel<F, NB, ACT, RES>, stage_bytes<F>());
+    cudaError_t err = allow_smem(conv_kernel<F, NB, ACT, RES>, conv_bytes<F, NB>());
     if (err != cudaSuccess) return err;
     for (int n0 = 0; n0 < F; n0 += NB)
     {
@@ -277,7 +352,7 @@ cudaError_t conv_layer(const float* k, const float* b, const float* a, const flo
             W.b[n] = b[n0 + n];
             W.a[n] = a ? a[n0 + n] : 0.0f;
         }
-        conv_kernel<F, NB, ACT, RES><<<grid, THREADS, stage_bytes<F>(), stream>>>(W, in, out, skip, F, n0, w, h);
+        conv_kernel<F, NB, ACT, RES><<<grid, THREADS, conv_bytes<F, NB>(), stream>>>(W, in, out, skip, F, n0, w, h);
         count_launch();
     }
     return cudaGetLastError();
@@ -372,10 +447,10 @@ cudaError_t fsrcnnx_typed(const float* kernels, const float* biases, const float
             W.a1[i] = alphas[F * l + i];
         }
         for (int i = 0; i < F * F; i++) W.k1[i] = kernels[F * 25 + F * F * 9 * blocks + i];
-        err = allow_smem(tail_kernel<F>, stage_bytes<F>());
+        err = allow_smem(tail_kernel<F>, conv_bytes<F, F>());
         if (err != cudaSuccess) return err;
         const dim3 grid((w + BX - 1) / BX, (h + BY - 1) / BY);
-        tail_kernel<F><<<grid, THREADS, stage_bytes<F>(), stream>>>(W, cur, feat, a, w, h);
+        tail_kernel<F><<<grid, THREADS, conv_bytes<F, F>(), stream>>>(W, cur, feat, a, w, h);
         count_launch();
         if ((err = cudaGetLastError()) != cudaSuccess) return err;
         l += 2;

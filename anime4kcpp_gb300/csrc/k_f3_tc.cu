@@ -1,0 +1,505 @@
+// ArtCNN<16/32> and FSRCNNX<16> x2 passes in a tensor-core form (FP16 or BF16
+// operands, FP32 accumulation): the 3x3 F->F layers on tcgen05, the head and
+// the upscale layer in FP32 on CUDA cores, F-channel 16-bit maps between
+// launches.
+//
+// Networks and CPU order as k_f3_fp32.cu (CPUProcessor.cpp:1519-1600,
+// 1629-1715).  GEMM shape: one GEMM row = one pixel, N = F output channels,
+// K = 9 taps x F input channels.  A window of 32 x 32 pixels (halo 1 around a
+// 30 x 30 tile) is held as F/8 channel planes (16 bytes = 8 channels per
+// pixel each); for tap (dy, dx) and channels 16 j .. 16 j + 15 the A operand
+// is a shifted view of planes 2 j and 2 j + 1 (leading byte offset = one
+// plane), so a tap is F/16 M128 x N F x K16 MMAs and a block of 128 pixels
+// 9 F/16 of them.  8 blocks per window, F tensor-memory columns each.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <vector>
+
+#include "device_common.cuh"
+#include "kernels.hpp"
+#include "tc_ptx.cuh"
+
+namespace acgb {
+namespace f3tc {
+
+constexpr int WW = 32, WH = 32, TW = WW - 2, TH = WH - 2;
+constexpr int NBLK = WW * WH / 128;  // 8
+constexpr int PAD = 40;              // >= WW + 1: taps of the first and last rows stay inside a plane
+constexpr int PLANE_BYTES = (PAD + NBLK * 128 + PAD) * 16;
+constexpr int THREADS = 128;
+constexpr uint64_t kWaitNs = 2000000000ull;
+constexpr int kMaxImg = 16;
+
+enum Mode { kReLU = 0, kPReLU = 1, kAddSkip = 2, kFsrTail = 3 };
+
+template <int F>
+struct Geo
+{
+    static constexpr int NP = F / 8;                  // channel planes
+    static constexpr int CHUNK = F * 32;              // B of one MMA: N F x K16 x 16 bit
+    static constexpr int B_BYTES = 9 * (F / 16) * CHUNK;
+    static constexpr uint32_t TMEM_COLS = NBLK * F;   // 128 (F = 16) or 256 (F = 32)
+    static constexpr int SMEM = NP * PLANE_BYTES + B_BYTES + 64;
+    // at most 512 / TMEM_COLS CTAs per SM: request enough shared memory to enforce it
+    static constexpr int MIN_SMEM = (228 * 1024) / (512 / TMEM_COLS + 1) + 1024;
+    static constexpr int SMEM_REQ = SMEM > MIN_SMEM ? SMEM : MIN_SMEM;
+};
+
+struct ImgW
+{
+    const uint4* in;    // [h][w] pixels of F 16-bit channels
+    uint4* out;
+    const uint4* skip;  // kAddSkip: the map added; kFsrTail: feat
+    int w, h, tiles_x, tile0;
+};
+
+template <int F>
+struct ConvWP
+{
+    const uint4* bw;  // packed B (pack_f3_conv)
+    float b[F], a[F];
+    float k1[F * F], b1[F], a1[F];  // kFsrTail: conv1x1 F->F, bias, PReLU
+    int* status;
+    int nimg;
+    ImgW img[kMaxImg];
+};
+
+template <bool BF16>
+__device__ __forceinline__ void unpack8(const uint4 u, float* v)
+{
+    const uint32_t r[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+    {
+        if constexpr (BF16)
+        {
+            v[2 * i] = __uint_as_float(r[i] << 16);
+            v[2 * i + 1] = __uint_as_float(r[i] & 0xFFFF0000u);
+        }
+        else
+        {
+            const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&r[i]));
+            v[2 * i] = f.x;
+            v[2 * i + 1] = f.y;
+        }
+    }
+}
+
+template <bool BF16>
+__device__ __forceinline__ uint4 pack8(const float* v)
+{
+    if constexpr (BF16)
+        return make_uint4(tc::pack_bf16x2(v[0], v[1]), tc::pack_bf16x2(v[2], v[3]), tc::pack_bf16x2(v[4], v[5]),
+                          tc::pack_bf16x2(v[6], v[7]));
+    else
+        return make_uint4(tc::pack_f16x2(v[0], v[1]), tc::pack_f16x2(v[2], v[3]), tc::pack_f16x2(v[4], v[5]),
+                          tc::pack_f16x2(v[6], v[7]));
+}
+
+__device__ __forceinline__ float prelu(float v, float a) { return fmaxf(v, 0.0f) + a * fminf(v, 0.0f); }
+
+template <int F, int MODE, bool BF16>
+__global__ void __launch_bounds__(THREADS) convw_kernel(const __grid_constant__ ConvWP<F> P)
+{
+    using G = Geo<F>;
+    constexpr int NP = G::NP;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* planes = smem;
+    unsigned char* bsm = smem + NP * PLANE_BYTES;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(bsm + G::B_BYTES);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bsm + G::B_BYTES + 8);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    int im = 0;
+    while (im + 1 < P.nimg && P.img[im + 1].tile0 <= static_cast<int>(blockIdx.x)) im++;
+    const ImgW& I = P.img[im];
+    const int local = static_cast<int>(blockIdx.x) - I.tile0;
+    const int x0 = (local % I.tiles_x) * TW - 1, y0 = (local / I.tiles_x) * TH - 1;
+
+    if (tid == 0)
+    {
+        tc::mbar_init(mbar, 1);
+        tc::fence_mbar_init();
+    }
+    if (warp == 0)
+    {
+        tc::tmem_alloc(tmem_slot, G::TMEM_COLS);
+        tc::tmem_relinquish();
+    }
+    for (int i = tid; i < G::B_BYTES / 16; i += THREADS) reinterpret_cast<uint4*>(bsm)[i] = P.bw[i];
+    // pads: read with zero weights by the window's first and last rows
+    for (int i = tid; i < NP * 2 * PAD; i += THREADS)
+    {
+        const int pl = i / (2 * PAD), k = i % (2 * PAD);
+        reinterpret_cast<uint4*>(planes + pl * PLANE_BYTES)[k < PAD ? k : NBLK * 128 + k] = make_uint4(0, 0, 0, 0);
+    }
+    // the window (clamped to the map): pixel p's channels 8 j .. 8 j + 7 into plane j
+    for (int i = tid; i < WW * WH * NP; i += THREADS)
+    {
+        const int p = i / NP, j = i - p * NP;
+        const int wy = p / WW, wx = p - wy * WW;
+        const int gx = clampi(x0 + wx, 0, I.w - 1), gy = clampi(y0 + wy, 0, I.h - 1);
+        reinterpret_cast<uint4*>(planes + j * PLANE_BYTES)[PAD + p] = I.in[(static_cast<size_t>(gy) * I.w + gx) * NP + j];
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+
+    if (tid == 0)
+    {
+        constexpr uint32_t IDESC = tc::idesc_f16(128, F, BF16);
+        const uint32_t pl0 = tc::smem_u32(planes), b0 = tc::smem_u32(bsm);
+        for (int b = 0; b < NBLK; b++)
+        {
+#pragma unroll
+            for (int t = 0; t < 9; t++)
+            {
+                const int slot = PAD + 128 * b + (t / 3 - 1) * WW + (t % 3 - 1);
+#pragma unroll
+                for (int j2 = 0; j2 < F / 16; j2++)
+                {
+                    const uint64_t a = tc::smem_desc(pl0 + static_cast<uint32_t>(2 * j2 * PLANE_BYTES + slot * 16), PLANE_BYTES, 128);
+                    const uint64_t bd =
+                        tc::smem_desc(b0 + static_cast<uint32_t>((t * (F / 16) + j2) * G::CHUNK), F * 16, 128);
+                    tc::mma_f16(tmem + static_cast<uint32_t>(b * F), a, bd, IDESC, (t | j2) ? 1u : 0u);
+                }
+            }
+        }
+        tc::mma_commit(mbar);
+    }
+    __syncwarp();
+    const bool ok = __syncthreads_and(tc::mbar_wait_ns(mbar, 0, kWaitNs) ? 1 : 0) != 0;
+    tc::fence_after_sync();
+    if (!ok)
+    {
+        if (tid == 0) atomicExch(P.status, 1);
+    }
+    else
+        for (int b = 0; b < NBLK; b++)
+        {
+            float v[F];
+#pragma unroll
+            for (int h = 0; h < F / 16; h++)
+            {
+                float q[16];
+                tc::tmem_ld16(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(b * F + 16 * h), q);
+                tc::tmem_wait_ld();
+#pragma unroll
+                for (int c = 0; c < 16; c++) v[16 * h + c] = q[c];
+            }
+            const int p = b * 128 + warp * 32 + lane;
+            const int y = p / WW, x = p - y * WW;
+            const int gx = x0 + x, gy = y0 + y;
+            if (y < 1 || y > TH || x < 1 || x > TW || gx >= I.w || gy >= I.h) continue;
+            const size_t o = (static_cast<size_t>(gy) * I.w + gx) * NP;
+#pragma unroll
+            for (int n = 0; n < F; n++) v[n] += P.b[n];
+            if constexpr (MODE == kReLU)
+            {
+#pragma unroll
+                for (int n = 0; n < F; n++) v[n] = fmaxf(v[n], 0.0f);
+            }
+            else if constexpr (MODE == kPReLU || MODE == kFsrTail)
+            {
+#pragma unroll
+                for (int n = 0; n < F; n++) v[n] = prelu(v[n], P.a[n]);
+            }
+            if constexpr (MODE == kAddSkip)
+            {
+#pragma unroll
+                for (int j = 0; j < NP; j++)
+                {
+                    float sk[8];
+                    unpack8<BF16>(I.skip[o + j], sk);
+#pragma unroll
+                    for (int c = 0; c < 8; c++) v[8 * j + c] += sk[c];
+                }
+            }
+            if constexpr (MODE == kFsrTail)
+            {
+                // conv1x1 F->F + bias, + feat, PReLU
+                float u[F];
+#pragma unroll
+                for (int n = 0; n < F; n++)
+                {
+                    float s = P.b1[n];
+#pragma unroll
+                    for (int c = 0; c < F; c++) s = fmaf(v[c], P.k1[n * F + c], s);
+                    u[n] = s;
+                }
+#pragma unroll
+                for (int j = 0; j < NP; j++)
+                {
+                    float f[8];
+                    unpack8<BF16>(I.skip[o + j], f);
+#pragma unroll
+                    for (int c = 0; c < 8; c++) v[8 * j + c] = prelu(u[8 * j + c] + f[c], P.a1[8 * j + c]);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < NP; j++) I.out[o + j] = pack8<BF16>(v + 8 * j);
+        }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, G::TMEM_COLS);
+}
+
+template <int K, int F>
+struct HeadP
+{
+    float k[F * K * K];
+    float b[F];
+};
+
+// conv KxK 1 -> F (identity) in FP32 from the input plane, taps clamped,
+// stored as an F-channel 16-bit map.
+template <typename T, int K, int F, bool BF16>
+__global__ void __launch_bounds__(256) head_kernel(const __grid_constant__ HeadP<K, F> W, Plane in, uint4* __restrict__ feat)
+{
+    constexpr int R = K / 2;
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= in.w || y >= in.h) return;
+    float t[K * K];
+#pragma unroll
+    for (int p = 0; p < K * K; p++)
+    {
+        const int gy = clampi(y + p / K - R, 0, in.h - 1), gx = clampi(x + p % K - R, 0, in.w - 1);
+        t[p] = to_float<T>(row_ptr<T>(in.ptr, in.pitch, gy)[gx]);
+    }
+    uint4* o = feat + (static_cast<size_t>(y) * in.w + x) * (F / 8);
+#pragma unroll
+    for (int j = 0; j < F / 8; j++)
+    {
+        float r[8];
+#pragma unroll
+        for (int c = 0; c < 8; c++)
+        {
+            float v = W.b[8 * j + c];
+#pragma unroll
+            for (int p = 0; p < K * K; p++) v = fmaf(t[p], W.k[(8 * j + c) * K * K + p], v);
+            r[c] = v;
+        }
+        o[j] = pack8<BF16>(r);
+    }
+}
+
+template <int F>
+struct UpP
+{
+    float k[4 * 9 * F];
+    float b[4];
+};
+
+// conv3x3 F -> 4 (identity) in FP32 from the 16-bit map, pixel shuffle 2x2,
+// fromFloat; no nearest add.
+template <typename T, int F, bool BF16>
+__global__ void __launch_bounds__(256) up_kernel(const __grid_constant__ UpP<F> U, const uint4* __restrict__ map, Plane src, Plane dst)
+{
+    const int w = src.w, h = src.h;
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= w || y >= h) return;
+    float acc[4];
+#pragma unroll
+    for (int n = 0; n < 4; n++) acc[n] = U.b[n];
+#pragma unroll
+    for (int p = 0; p < 9; p++)
+    {
+        const int gy = clampi(y + p / 3 - 1, 0, h - 1), gx = clampi(x + p % 3 - 1, 0, w - 1);
+        const uint4* px = map + (static_cast<size_t>(gy) * w + gx) * (F / 8);
+#pragma unroll
+        for (int j = 0; j < F / 8; j++)
+        {
+            float xv[8];
+            unpack8<BF16>(px[j], xv);
+#pragma unroll
+            for (int n = 0; n < 4; n++)
+#pragma unroll
+                for (int c = 0; c < 8; c++) acc[n] = fmaf(xv[c], U.k[n * 9 * F + p * F + 8 * j + c], acc[n]);
+        }
+    }
+#pragma unroll
+    for (int n = 0; n < 4; n++) row_ptr_w<T>(dst.ptr, dst.pitch, 2 * y + (n >> 1))[2 * x + (n & 1)] = from_float<T>(acc[n]);
+}
+
+uint16_t to_bits(float v, bool bf16)
+{
+    if (bf16)
+    {
+        uint32_t u;
+        std::memcpy(&u, &v, 4);
+        return static_cast<uint16_t>((u + 0x7FFFu + ((u >> 16) & 1u)) >> 16);
+    }
+    return __half_as_ushort(__float2half_rn(v));
+}
+
+// One 3x3 F->F layer k[n * 9F + tap * F + c] as the 9 F/16 B chunks of the
+// GEMM: chunk (tap t, channel pair j2) element (n, kk) = k[n][t][16 j2 + kk]
+// at byte (kk / 8) 16F + (n / 8) 128 + (n % 8) 16 + (kk % 8) 2.
+void pack_f3_conv(const float* k, int F, bool bf16, uint16_t* out)
+{
+    const int chunk = F * 32;
+    std::memset(out, 0, static_cast<size_t>(9) * (F / 16) * chunk);
+    for (int t = 0; t < 9; t++)
+        for (int j2 = 0; j2 < F / 16; j2++)
+        {
+            uint16_t* ch = out + (t * (F / 16) + j2) * (chunk / 2);
+            for (int n = 0; n < F; n++)
+                for (int kk = 0; kk < 16; kk++)
+                    ch[((kk >> 3) * 16 * F + (n >> 3) * 128 + (n & 7) * 16 + (kk & 7) * 2) / 2] =
+                        to_bits(k[n * 9 * F + t * F + 16 * j2 + kk], bf16);
+        }
+}
+
+template <int F, int MODE, bool BF16>
+cudaError_t launch_conv(const ConvWP<F>& p, int tiles, cudaStream_t stream)
+{
+    using G = Geo<F>;
+    static bool configured = false;
+    if (!configured)
+    {
+        cudaError_t err = cudaFuncSetAttribute(convw_kernel<F, MODE, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM_REQ);
+        if (err != cudaSuccess) return err;
+        configured = true;
+    }
+    convw_kernel<F, MODE, BF16><<<tiles, THREADS, G::SMEM_REQ, stream>>>(p);
+    return cudaGetLastError();
+}
+
+template <int F, bool BF16>
+cudaError_t conv_mode(int mode, const ConvWP<F>& p, int tiles, cudaStream_t stream)
+{
+    switch (mode)
+    {
+    case kReLU: return launch_conv<F, kReLU, BF16>(p, tiles, stream);
+    case kPReLU: return launch_conv<F, kPReLU, BF16>(p, tiles, stream);
+    case kAddSkip: return launch_conv<F, kAddSkip, BF16>(p, tiles, stream);
+    default: return launch_conv<F, kFsrTail, BF16>(p, tiles, stream);
+    }
+}
+
+// The network over one image: head, `layers` 3x3 F->F convolutions (mode per
+// layer from `plan`), upscale.  maps: three [h][w][F] 16-bit arrays.
+template <typename T, int F, int K, bool BF16>
+cudaError_t run_typed(const float* kernels, const float* biases, const float* alphas, bool artcnn, int blocks, const void* packed,
+                      const Plane& in, const Plane& out, void* const maps[3], int* status, cudaStream_t stream)
+{
+    const int w = in.w, h = in.h;
+    uint4* feat = static_cast<uint4*>(maps[0]);
+    uint4* a = static_cast<uint4*>(maps[1]);
+    uint4* bm = static_cast<uint4*>(maps[2]);
+    const dim3 pgrid((w + 31) / 32, (h + 7) / 8);
+    {
+        HeadP<K, F> hp;
+        for (int i = 0; i < F * K * K; i++) hp.k[i] = kernels[i];
+        for (int i = 0; i < F; i++) hp.b[i] = biases[i];
+        head_kernel<T, K, F, BF16><<<pgrid, 256, 0, stream>>>(hp, in, feat);
+        cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
+        count_launch();
+    }
+    ConvWP<F> c;
+    std::memset(&c, 0, sizeof(c));
+    c.status = status;
+    c.nimg = 1;
+    c.img[0].w = w;
+    c.img[0].h = h;
+    c.img[0].tiles_x = (w + TW - 1) / TW;
+    c.img[0].tile0 = 0;
+    const int tiles = c.img[0].tiles_x * ((h + TH - 1) / TH);
+    const size_t lb = static_cast<size_t>(9) * F * F;  // packed 16-bit values per layer
+    const int hk = F * K * K;                           // head kernel floats
+    const uint4* cur = feat;
+    // ArtCNN: blocks ReLU layers, then identity + feat.  FSRCNNX: blocks-1
+    // PReLU layers, then the tail (PReLU, 1x1 + feat, PReLU).
+    const int nconv = artcnn ? blocks + 1 : blocks;
+    for (int l = 1; l <= nconv; l++)
+    {
+        const bool last = l == nconv;
+        const int mode = artcnn ? (last ? kAddSkip : kReLU) : (last ? kFsrTail : kPReLU);
+        ConvWP<F> q = c;
+        q.img[0].in = cur;
+        q.img[0].out = a;
+        q.img[0].skip = feat;
+        q.bw = static_cast<const uint4*>(packed) + (l - 1) * lb * 2 / 16;
+        for (int i = 0; i < F; i++)
+        {
+            q.b[i] = biases[F * l + i];
+            q.a[i] = (!artcnn && alphas) ? alphas[F * (l - 1) + i] : 0.0f;
+        }
+        if (mode == kFsrTail)
+        {
+            for (int i = 0; i < F * F; i++) q.k1[i] = kernels[hk + F * F * 9 * blocks + i];
+            for (int i = 0; i < F; i++)
+            {
+                q.b1[i] = biases[F * (l + 1) + i];
+                q.a1[i] = alphas[F * l + i];
+            }
+        }
+        cudaError_t err = conv_mode<F, BF16>(mode, q, tiles, stream);
+        if (err != cudaSuccess) return err;
+        count_launch();
+        cur = a;
+        uint4* t = a;
+        a = bm;
+        bm = t;
+    }
+    // upscale: ArtCNN layer blocks+2, FSRCNNX layer blocks+2 (after the 1x1)
+    const int lu = blocks + 2;
+    UpP<F> u;
+    const float* uk = artcnn ? kernels + hk + F * F * 9 * (blocks + 1) : kernels + hk + F * F * 9 * blocks + F * F;
+    for (int i = 0; i < 4 * 9 * F; i++) u.k[i] = uk[i];
+    for (int i = 0; i < 4; i++) u.b[i] = biases[F * lu + i];
+    up_kernel<T, F, BF16><<<pgrid, 256, 0, stream>>>(u, cur, in, out);
+    cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess) count_launch();
+    return err;
+}
+
+template <int F, int K, bool BF16>
+cudaError_t run_type(const float* kernels, const float* biases, const float* alphas, bool artcnn, int blocks, const void* packed,
+                     const Plane& in, const Plane& out, void* const maps[3], int* status, cudaStream_t stream)
+{
+    switch (in.type)
+    {
+    case kU8: return run_typed<uint8_t, F, K, BF16>(kernels, biases, alphas, artcnn, blocks, packed, in, out, maps, status, stream);
+    case kU16: return run_typed<uint16_t, F, K, BF16>(kernels, biases, alphas, artcnn, blocks, packed, in, out, maps, status, stream);
+    case kF32: return run_typed<float, F, K, BF16>(kernels, biases, alphas, artcnn, blocks, packed, in, out, maps, status, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace f3tc
+
+// Packed B of the 3x3 F->F layers of an ArtCNN (blocks + 1 layers) or
+// FSRCNNX (blocks layers) model, F = 16 or 32.
+void pack_f3_tc_weights(const float* kernels, int F, bool artcnn, int blocks, bool bf16, std::vector<uint16_t>& packed)
+{
+    const int layers = artcnn ? blocks + 1 : blocks;
+    const int head = artcnn ? F * 9 : F * 25;
+    const size_t lb = static_cast<size_t>(9) * F * F;
+    packed.assign(layers * lb, 0);
+    for (int l = 0; l < layers; l++) f3tc::pack_f3_conv(kernels + head + F * F * 9 * l, F, bf16, packed.data() + l * lb);
+}
+
+cudaError_t launch_f3_tc(const float* kernels, const float* biases, const float* alphas, bool artcnn, int F, int blocks,
+                         const void* packed, bool bf16, const Plane& in, const Plane& out, void* const maps[3], int* status,
+                         cudaStream_t stream)
+{
+    using namespace f3tc;
+    if (in.w <= 0 || in.h <= 0) return cudaSuccess;
+    if (!packed || !status || blocks < 2 || (F != 16 && F != 32)) return cudaErrorInvalidValue;
+    if (artcnn)
+        return F == 32 ? (bf16 ? run_type<32, 3, true>(kernels, biases, alphas, true, blocks, packed, in, out, maps, status, stream)
+                               : run_type<32, 3, false>(kernels, biases, alphas, true, blocks, packed, in, out, maps, status, stream))
+                       : (bf16 ? run_type<16, 3, true>(kernels, biases, alphas, true, blocks, packed, in, out, maps, status, stream)
+                               : run_type<16, 3, false>(kernels, biases, alphas, true, blocks, packed, in, out, maps, status, stream));
+    if (F != 16) return cudaErrorInvalidValue;
+    return bf16 ? run_type<16, 5, true>(kernels, biases, alphas, false, blocks, packed, in, out, maps, status, stream)
+                : run_type<16, 5, false>(kernels, biases, alphas, false, blocks, packed, in, out, maps, status, stream);
+}
+
+}  // namespace acgb

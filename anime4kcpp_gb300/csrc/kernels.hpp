@@ -171,6 +171,14 @@ cudaError_t launch_artcnn_fp32(const float* kernels, const float* biases, int F,
                                float* const maps[3], cudaStream_t stream);
 cudaError_t launch_fsrcnnx_fp32(const float* kernels, const float* biases, const float* alphas, int F, int blocks,
                                 const Plane& in, const Plane& out, float* const maps[3], cudaStream_t stream);
+// Their tensor-core form for F = 16 or 32 (ArtCNN<16/32>, FSRCNNX<16>): the
+// 3x3 F->F layers on tcgen05 (one pixel per GEMM row, N = F), head and
+// upscale FP32, F-channel 16-bit maps.  `packed`: device copy of
+// pack_f3_tc_weights(); maps: three [h][w][F] 16-bit arrays.
+void pack_f3_tc_weights(const float* kernels, int F, bool artcnn, int blocks, bool bf16, std::vector<uint16_t>& packed);
+cudaError_t launch_f3_tc(const float* kernels, const float* biases, const float* alphas, bool artcnn, int F, int blocks,
+                         const void* packed, bool bf16, const Plane& in, const Plane& out, void* const maps[3], int* status,
+                         cudaStream_t stream);
 
 // Merge for chroma resampled by exactly `factor` (2 or 4) on both axes:
 // phase_weights[k*4 + t] is the Catmull-Rom weight of tap t of output phase k,

@@ -495,9 +495,33 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
         const ModelParams& mp = model_params(spec_);
         err = launch_arnet_fp32(mp.kernels.data(), mp.biases.data(), mp.alphas.data(), spec_.blocks, in, out, maps, stream);
     }
+    else if ((spec_.family == Family::ArtCNN || (spec_.family == Family::FSRCNNX && spec_.channels == 16)) &&
+             precision_ != Precision::FP32 && arnetTc_)
+    {
+        // tensor-core form: the 3x3 F->F layers on tcgen05, F-channel 16-bit maps
+        const bool bf16 = precision_ == Precision::BF16;
+        const void* w = arnetWeights(bf16);
+        const size_t bytes = static_cast<size_t>(in.w) * in.h * spec_.channels * 2;
+        void* maps[3];
+        err = w ? cudaSuccess : cudaErrorMemoryAllocation;
+        for (int i = 0; i < 3 && err == cudaSuccess; i++)
+        {
+            err = ts.maps[i].ensure(bytes);
+            maps[i] = ts.maps[i].ptr;
+        }
+        int* status = tc_status_buffer();
+        if (err == cudaSuccess && !status) err = cudaErrorMemoryAllocation;
+        if (err == cudaSuccess)
+        {
+            const ModelParams& mp = model_params(spec_);
+            err = launch_f3_tc(mp.kernels.data(), mp.biases.data(), mp.alphas.empty() ? nullptr : mp.alphas.data(),
+                               spec_.family == Family::ArtCNN, spec_.channels, spec_.blocks, w, bf16, in, out, maps, status,
+                               stream);
+        }
+    }
     else if (spec_.family == Family::ArtCNN || spec_.family == Family::FSRCNNX)
     {
-        // the plain FP32 layer pipeline (every precision form)
+        // the plain FP32 layer pipeline (FP32 form; FSRCNNX<8> in every form)
         const size_t bytes = static_cast<size_t>(in.w) * in.h * spec_.channels * sizeof(float);
         float* maps[3];
         for (int i = 0; i < 3; i++)
@@ -630,6 +654,19 @@ const void* GB300Processor::arnetWeights(bool bf16)
     if (!d.ptr)
     {
         const ModelParams& mp = model_params(spec_);
+        if (spec_.family == Family::ArtCNN || spec_.family == Family::FSRCNNX)
+        {
+            // the 3x3 F->F layers of the wide families
+            std::vector<uint16_t> packed;
+            pack_f3_tc_weights(mp.kernels.data(), spec_.channels, spec_.family == Family::ArtCNN, spec_.blocks, bf16, packed);
+            if (d.ensure(packed.size() * sizeof(uint16_t)) != cudaSuccess) return nullptr;
+            if (cudaMemcpy(d.ptr, packed.data(), packed.size() * sizeof(uint16_t), cudaMemcpyHostToDevice) != cudaSuccess)
+            {
+                d.release();
+                return nullptr;
+            }
+            return d.ptr;
+        }
         // the 3x3 8->8 layers: two per ARNet block, one per ACNet<8> block
         const int layers = spec_.family == Family::ARNet ? 2 * spec_.blocks : spec_.blocks;
         std::vector<uint16_t> packed(static_cast<size_t>(layers) * 1536);

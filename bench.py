@@ -24,6 +24,9 @@ Voronoi-edge images (no public dataset is attached to this workload).
 
   video  the video workload: 8 frames of 1080p 10-bit YUV 4:2:0 u16 per step,
          x4 with ARNet-B8 (two x2 luma passes), FP16 tensor-core form vs FP32
+  families  every network family of the reference on 1920x1080 u8 luma x2
+         (device-resident, one launch sequence per frame): the tensor-core
+         form where the family has one, and the plain FP32 form
   serve  the serving workload: Poisson arrivals (200 jobs/s) of mixed sizes,
          factors, models and formats through the serving loop; p50/p99
          latency and output Mpx/s, FP16 against FP32
@@ -390,6 +393,46 @@ def time_video(ac, torch, args):
     return res
 
 
+FAMILIES = [("acnet-legacy-hdn0", True), ("acnet-f8b8-hdn", True), ("arnet-b8", True), ("artcnn-c4f16", True),
+            ("artcnn-c4f32", True), ("fsrcnnx-f8", False), ("fsrcnnx-f16", True)]
+
+
+def time_families(ac, torch, args):
+    """Every network family on a 1920x1080 u8 luma plane x2 (Voronoi-edge
+    content), device-resident, CUDA events on the launching stream: output
+    Mpx/s of the FP16 tensor-core form (where the family has one) and of the
+    plain FP32 form."""
+    from anime4kcpp_gb300 import synthetic
+    x = synthetic.luma(H, W, np.uint8, cells=64, seed=90)
+    src = torch.from_numpy(x).cuda()
+    dst = torch.empty((OH, OW), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    out = {"workload": "1920x1080 u8 luma -> 3840x2160 x2 per family, one frame per step"}
+    for model, has_tc in FAMILIES:
+        rec = {}
+        for form in (("fp16", "fp32") if has_tc else ("fp32",)):
+            p = ac.Processor("cuda", 0, model, precision=form)
+            h = stream.cuda_stream
+            for _ in range(2):
+                p.process_device(src, dst, 2.0, stream=h, sync=False)
+            torch.cuda.synchronize()
+            steps = max(3, args.family_steps)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                p.process_device(src, dst, 2.0, stream=h, sync=False)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if not p.ok():
+                raise RuntimeError(p.error())
+            ms = e0.elapsed_time(e1) / steps
+            rec[form] = {"ms_per_frame": round(ms, 4), "value": OW * OH / (ms / 1e3) / 1e6, "unit": "Mpx/s"}
+        if has_tc:
+            rec["fp16_over_fp32"] = rec["fp16"]["value"] / rec["fp32"]["value"]
+        out[model] = rec
+    return out
+
+
 SERVE_RES = [(480, 854), (720, 1280), (1080, 1920), (2160, 3840)]
 SERVE_RES_W = [1, 2, 2, 1]
 SERVE_MODELS = ["acnet-legacy-hdn0", "acnet-legacy-hdn1", "acnet-legacy-hdn2", "acnet-legacy-hdn3", "arnet-b8"]
@@ -670,6 +713,8 @@ def run_gb300(args, rank, world, local_rank):
         out["batch"] = time_batch(ac, torch, args)
     if rank == 0 and world == 1 and args.video_steps > 0:
         out["video"] = time_video(ac, torch, args)
+    if rank == 0 and world == 1 and args.family_steps > 0:
+        out["families"] = time_families(ac, torch, args)
     if rank == 0 and world == 1 and args.serve_seconds > 0:
         out["serve"] = time_serve(ac, torch, args)
         out["serve"]["saturation"] = time_serve_saturation(ac, torch, args)
@@ -693,6 +738,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-image batching workload")
     ap.add_argument("--batch-steps", type=int, default=12)
     ap.add_argument("--video-steps", type=int, default=4, help="8-frame steps of the video workload (0: skip)")
+    ap.add_argument("--family-steps", type=int, default=10, help="frames per family and form in the families workload (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="serving workload length per form (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="serving workload arrival rate, jobs/s")
     ap.add_argument("--saturation-rate", type=float, default=4000.0, help="offered rate of the saturation run, jobs/s")
