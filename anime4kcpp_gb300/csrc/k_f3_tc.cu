@@ -29,7 +29,6 @@ constexpr int WW = 32, WH = 32, TW = WW - 2, TH = WH - 2;
 constexpr int NBLK = WW * WH / 128;  // 8
 constexpr int PAD = 40;              // >= WW + 1: taps of the first and last rows stay inside a plane
 constexpr int PLANE_BYTES = (PAD + NBLK * 128 + PAD) * 16;
-constexpr int THREADS = 128;
 constexpr uint64_t kWaitNs = 2000000000ull;
 constexpr int kMaxImg = 16;
 
@@ -46,6 +45,9 @@ struct Geo
     // at most 512 / TMEM_COLS CTAs per SM: request enough shared memory to enforce it
     static constexpr int MIN_SMEM = (228 * 1024) / (512 / TMEM_COLS + 1) + 1024;
     static constexpr int SMEM_REQ = SMEM > MIN_SMEM ? SMEM : MIN_SMEM;
+    // 1,024 threads per SM over the CTAs that fit (2 for F = 32, 4 for F = 16):
+    // many window loads in flight, several warps per tensor-memory lane quarter
+    static constexpr int THREADS = F == 32 ? 512 : 256;
 };
 
 struct ImgW
@@ -102,9 +104,10 @@ __device__ __forceinline__ uint4 pack8(const float* v)
 __device__ __forceinline__ float prelu(float v, float a) { return fmaxf(v, 0.0f) + a * fminf(v, 0.0f); }
 
 template <int F, int MODE, bool BF16>
-__global__ void __launch_bounds__(THREADS) convw_kernel(const __grid_constant__ ConvWP<F> P)
+__global__ void __launch_bounds__(Geo<F>::THREADS) convw_kernel(const __grid_constant__ ConvWP<F> P)
 {
     using G = Geo<F>;
+    constexpr int THREADS = G::THREADS;
     constexpr int NP = G::NP;
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* planes = smem;
@@ -135,13 +138,27 @@ __global__ void __launch_bounds__(THREADS) convw_kernel(const __grid_constant__ 
         const int pl = i / (2 * PAD), k = i % (2 * PAD);
         reinterpret_cast<uint4*>(planes + pl * PLANE_BYTES)[k < PAD ? k : NBLK * 128 + k] = make_uint4(0, 0, 0, 0);
     }
-    // the window (clamped to the map): pixel p's channels 8 j .. 8 j + 7 into plane j
-    for (int i = tid; i < WW * WH * NP; i += THREADS)
+    // the window (clamped to the map): pixel p's channels 8 j .. 8 j + 7 into
+    // plane j, four loads in flight per thread
+    constexpr int NLD = WW * WH * NP / THREADS;
+    static_assert(NLD % 4 == 0 && NLD * THREADS == WW * WH * NP, "whole load batches");
+#pragma unroll 1
+    for (int k0 = 0; k0 < NLD; k0 += 4)
     {
-        const int p = i / NP, j = i - p * NP;
-        const int wy = p / WW, wx = p - wy * WW;
-        const int gx = clampi(x0 + wx, 0, I.w - 1), gy = clampi(y0 + wy, 0, I.h - 1);
-        reinterpret_cast<uint4*>(planes + j * PLANE_BYTES)[PAD + p] = I.in[(static_cast<size_t>(gy) * I.w + gx) * NP + j];
+        uint4 v[4];
+        int dst[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+        {
+            const int i = tid + (k0 + k) * THREADS;
+            const int p = i / NP, j = i - p * NP;
+            const int wy = p / WW, wx = p - wy * WW;
+            const int gx = clampi(x0 + wx, 0, I.w - 1), gy = clampi(y0 + wy, 0, I.h - 1);
+            v[k] = I.in[(static_cast<size_t>(gy) * I.w + gx) * NP + j];
+            dst[k] = j * (PLANE_BYTES / 16) + PAD + p;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) reinterpret_cast<uint4*>(planes)[dst[k]] = v[k];
     }
     tc::fence_proxy_async_smem();
     tc::fence_before_sync();
@@ -179,19 +196,21 @@ __global__ void __launch_bounds__(THREADS) convw_kernel(const __grid_constant__ 
         if (tid == 0) atomicExch(P.status, 1);
     }
     else
-        for (int b = 0; b < NBLK; b++)
+        // warp w drains lane quarter w % 4 of blocks w / 4, w / 4 + THREADS / 128, ...
+        for (int b = warp >> 2; b < NBLK; b += THREADS / 128)
         {
+            const int q4 = warp & 3;
             float v[F];
 #pragma unroll
             for (int h = 0; h < F / 16; h++)
             {
                 float q[16];
-                tc::tmem_ld16(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(b * F + 16 * h), q);
+                tc::tmem_ld16(tmem + (static_cast<uint32_t>(q4 * 32) << 16) + static_cast<uint32_t>(b * F + 16 * h), q);
                 tc::tmem_wait_ld();
 #pragma unroll
                 for (int c = 0; c < 16; c++) v[16 * h + c] = q[c];
             }
-            const int p = b * 128 + warp * 32 + lane;
+            const int p = b * 128 + q4 * 32 + lane;
             const int y = p / WW, x = p - y * WW;
             const int gx = x0 + x, gy = y0 + y;
             if (y < 1 || y > TH || x < 1 || x > TW || gx >= I.w || gy >= I.h) continue;
@@ -365,7 +384,7 @@ cudaError_t launch_conv(const ConvWP<F>& p, int tiles, cudaStream_t stream)
         if (err != cudaSuccess) return err;
         configured = true;
     }
-    convw_kernel<F, MODE, BF16><<<tiles, THREADS, G::SMEM_REQ, stream>>>(p);
+    convw_kernel<F, MODE, BF16><<<tiles, G::THREADS, G::SMEM_REQ, stream>>>(p);
     return cudaGetLastError();
 }
 
