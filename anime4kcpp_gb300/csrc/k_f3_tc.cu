@@ -1,6 +1,6 @@
 // ArtCNN<16/32> and FSRCNNX<16> x2 passes in a tensor-core form (FP16 or BF16
-// operands, FP32 accumulation): the 3x3 F->F layers on tcgen05, the head and
-// the upscale layer in FP32 on CUDA cores, F-channel 16-bit maps between
+// operands, FP32 accumulation): the 3x3 F->F layers and the F->4 upscale on
+// tcgen05, the 1->F head in FP32 on CUDA cores, F-channel 16-bit maps between
 // launches.
 //
 // Networks and CPU order as k_f3_fp32.cu (CPUProcessor.cpp:1519-1600,
@@ -11,6 +11,11 @@
 // is a shifted view of planes 2 j and 2 j + 1 (leading byte offset = one
 // plane), so a tap is F/16 M128 x N F x K16 MMAs and a block of 128 pixels
 // 9 F/16 of them.  8 blocks per window, F tensor-memory columns each.
+//
+// Two kernels run these GEMMs: convw_kernel, one CTA per tile (the 16-channel
+// layers), and convp_kernel, persistent CTAs with a TMA-fed two-stage
+// pipeline (the 32-channel layers and every upscale layer, which it runs with
+// N = 16 and the weights split into 16-bit high parts and residuals).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -21,6 +26,7 @@
 #include "device_common.cuh"
 #include "kernels.hpp"
 #include "tc_ptx.cuh"
+#include "tma_host.hpp"
 
 namespace acgb {
 namespace f3tc {
@@ -32,7 +38,7 @@ constexpr int PLANE_BYTES = (PAD + NBLK * 128 + PAD) * 16;
 constexpr uint64_t kWaitNs = 2000000000ull;
 constexpr int kMaxImg = 16;
 
-enum Mode { kReLU = 0, kPReLU = 1, kAddSkip = 2, kFsrTail = 3 };
+enum Mode { kReLU = 0, kPReLU = 1, kAddSkip = 2, kFsrTail = 3, kUp = 4 };
 
 template <int F>
 struct Geo
@@ -267,6 +273,360 @@ __global__ void __launch_bounds__(Geo<F>::THREADS) convw_kernel(const __grid_con
     if (warp == 0) tc::tmem_dealloc(tmem, G::TMEM_COLS);
 }
 
+// ---- persistent form ----
+// One CTA per SM (F = 32) or two (F = 16) walk the tiles of a layer with a
+// two-stage pipeline: while the epilogue warps drain tile t's accumulators,
+// the MMA lane runs tile t + 1 and the producer warp loads tile t + 2's window
+// with TMA (one 8 x 32 x 32 box per channel plane; the out-of-image ring that
+// clamp-to-edge needs is then copied in from its neighbours).  Stage s of
+// tile t (s = t % 2, u = t / 2):
+//   full[s]   TMA bytes of the window landed          (producer waits)
+//   ready[s]  window complete, edge ring filled       (MMA lane waits)
+//   mdone[s]  MMAs of the stage completed (commit)    (epilogue, producer wait)
+//   tfree[s]  accumulators drained by every epilogue warp (MMA lane waits)
+// Each wait targets completion u (or u - 1) of a barrier whose next completion
+// needs the waiter's own progress, so no phase is ever skipped.  Every wait is
+// bounded; a timeout raises the CTA's abort flag and the status word.
+constexpr int NSTAGE = 2;
+
+template <int F>
+struct GeoP
+{
+    static constexpr int NP = F / 8;
+    static constexpr int WIN_BYTES = NP * PLANE_BYTES;
+    static constexpr int CHUNK = F * 32;
+    static constexpr int B_BYTES = 9 * (F / 16) * CHUNK;
+    static constexpr uint32_t TMEM_COLS = NSTAGE * NBLK * F;  // 256 (F = 16) or 512 (F = 32)
+    static constexpr int NEPI = F == 32 ? 16 : 8;            // epilogue warps, a multiple of 4
+    static constexpr int THREADS = (2 + NEPI) * 32;
+    static constexpr int MINB = F == 32 ? 1 : 2;             // CTAs per SM
+    static constexpr int BAR_OFF = NSTAGE * WIN_BYTES + B_BYTES;
+    static constexpr int SMEM = BAR_OFF + 128;
+    // at most 512 / TMEM_COLS CTAs per SM: request enough shared memory to enforce it
+    static constexpr int MIN_SMEM = (228 * 1024) / (512 / TMEM_COLS + 1) + 1024;
+    static constexpr int SMEM_REQ = SMEM > MIN_SMEM ? SMEM : MIN_SMEM;
+    static constexpr uint32_t BOX_BYTES = 8 * WW * WH * 2;  // one channel plane of the window
+    static_assert((PAD * 16) % 128 == 0 && PLANE_BYTES % 128 == 0, "TMA destinations 128-byte aligned");
+};
+
+struct ImgP
+{
+    const uint4* skip;  // kAddSkip: the map added; kFsrTail: feat
+    uint4* out;
+    int w, h, tiles_x, tile0;
+    Plane dst;  // kUp: the 2w x 2h output plane
+};
+
+template <int F>
+struct ConvPP
+{
+    CUtensorMap tmap[kMaxImg];  // input map of each image: [h][w][F] 16-bit, box 8 x 32 x 32
+    const uint4* bw;            // packed B (pack_f3_conv)
+    float b[F], a[F];
+    float k1[F * F], b1[F], a1[F];  // kFsrTail: conv1x1 F->F, bias, PReLU
+    int* status;
+    int nimg, ntiles;
+    ImgP img[kMaxImg];
+};
+
+__device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity, volatile int* abort_flag)
+{
+    if (tc::mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = tc::global_timer_ns();
+    while (!tc::mbar_try_wait_hint(bar, parity, 20000u))
+    {
+        if (*abort_flag) return false;
+        if (tc::global_timer_ns() - t0 > kWaitNs)
+        {
+            *abort_flag = 1;
+            return false;
+        }
+    }
+    return true;
+}
+
+template <int F>
+__device__ __forceinline__ int image_of(const ConvPP<F>& P, int tile)
+{
+    int im = 0;
+    while (im + 1 < P.nimg && P.img[im + 1].tile0 <= tile) im++;
+    return im;
+}
+
+// MODE kUp: the F -> 4 upscale layer with N = 16 (columns 0-3 the weights'
+// 16-bit high parts, 4-7 their residuals), pixel shuffle into the OT plane.
+template <int F, int MODE, bool BF16, typename OT>
+__global__ void __launch_bounds__(GeoP<F>::THREADS, GeoP<F>::MINB) convp_kernel(const __grid_constant__ ConvPP<F> P)
+{
+    using G = GeoP<F>;
+    constexpr int NP = G::NP, NEPI = G::NEPI;
+    constexpr int NM = MODE == kUp ? 16 : F;           // MMA N
+    constexpr int CHUNK_M = NM * 32;                   // B of one MMA
+    constexpr int BB = 9 * (F / 16) * CHUNK_M;         // this layer's B
+    static_assert(BB <= G::B_BYTES, "B fits its buffer");
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* bsm = smem + NSTAGE * G::WIN_BYTES;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + G::BAR_OFF);
+    uint64_t* full = bars;       // [NSTAGE]
+    uint64_t* ready = bars + 2;  // [NSTAGE]
+    uint64_t* mdone = bars + 4;  // [NSTAGE]
+    uint64_t* tfree = bars + 6;  // [NSTAGE]
+    uint64_t* bbar = bars + 8;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 9);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 10);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (tid == 0)
+    {
+        for (int i = 0; i < NSTAGE; i++)
+        {
+            tc::mbar_init(&full[i], 1);
+            tc::mbar_init(&ready[i], 1);
+            tc::mbar_init(&mdone[i], 1);
+            tc::mbar_init(&tfree[i], NEPI);
+        }
+        tc::mbar_init(bbar, 1);
+        *abort_flag = 0;
+        tc::fence_mbar_init();
+    }
+    // the planes' pads (never loaded): read with zero weights by the window's first and last rows
+    for (int i = tid; i < NSTAGE * NP * 2 * PAD; i += G::THREADS)
+    {
+        const int pl = i / (2 * PAD), k = i % (2 * PAD);
+        reinterpret_cast<uint4*>(smem + pl * PLANE_BYTES)[k < PAD ? k : NBLK * 128 + k] = make_uint4(0, 0, 0, 0);
+    }
+    if (warp == 1)
+    {
+        tc::tmem_alloc(tmem_slot, G::TMEM_COLS);
+        tc::tmem_relinquish();
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0)
+    {
+        // ---- producer ----
+        if (lane == 0)
+        {
+            tc::mbar_arrive_expect_tx(bbar, BB);
+            tc::bulk_load(bsm, P.bw, BB, bbar);
+        }
+        int it = 0;
+        bool pending = false;  // a window load issued and not yet seen complete
+        for (int tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x, it++)
+        {
+            const int s = it & 1;
+            const uint32_t u = static_cast<uint32_t>(it) >> 1;
+            bool ok = u == 0 || wait_bar(&mdone[s], (u - 1) & 1u, abort_flag);
+            if (!__all_sync(0xffffffffu, ok ? 1 : 0)) break;
+            const int im = image_of(P, tile);
+            const ImgP& I = P.img[im];
+            const int local = tile - I.tile0;
+            const int x0 = (local % I.tiles_x) * TW - 1, y0 = (local / I.tiles_x) * TH - 1;
+            unsigned char* win = smem + s * G::WIN_BYTES;
+            if (lane == 0)
+            {
+                tc::mbar_arrive_expect_tx(&full[s], NP * G::BOX_BYTES);
+#pragma unroll
+                for (int j = 0; j < NP; j++) tc::tma_load_3d(win + j * PLANE_BYTES + PAD * 16, &P.tmap[im], 8 * j, x0, y0, &full[s]);
+            }
+            pending = true;
+            ok = wait_bar(&full[s], u & 1u, abort_flag);
+            if (!__all_sync(0xffffffffu, ok ? 1 : 0)) break;
+            pending = false;
+            // clamp-to-edge: the window column / row just outside the image
+            // takes its inner neighbour (columns first, so corners follow)
+            const int xl = x0 < 0 ? 0 : -1, xr = I.w - x0 < WW ? I.w - x0 : -1;
+            const int yt = y0 < 0 ? 0 : -1, yb = I.h - y0 < WH ? I.h - y0 : -1;
+            if (xl >= 0 || xr >= 0 || yt >= 0 || yb >= 0)
+            {
+                uint4* pw = reinterpret_cast<uint4*>(win) + PAD;
+                for (int i = lane; i < WH * NP; i += 32)
+                {
+                    uint4* row = pw + (i % NP) * (PLANE_BYTES / 16) + (i / NP) * WW;
+                    if (xl >= 0) row[xl] = row[xl + 1];
+                    if (xr >= 0) row[xr] = row[xr - 1];
+                }
+                __syncwarp();
+                for (int i = lane; i < WW * NP; i += 32)
+                {
+                    uint4* col = pw + (i % NP) * (PLANE_BYTES / 16) + i / NP;
+                    if (yt >= 0) col[yt * WW] = col[(yt + 1) * WW];
+                    if (yb >= 0) col[yb * WW] = col[(yb - 1) * WW];
+                }
+                tc::fence_proxy_async_smem();
+            }
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&ready[s]);
+        }
+        // loads still in flight (after an abort) land before the CTA exits;
+        // bounded by time, not cut short by the abort
+        if (lane == 0)
+        {
+            if (pending && !tc::mbar_wait_ns(&full[it & 1], (static_cast<uint32_t>(it) >> 1) & 1u, kWaitNs)) *abort_flag = 1;
+            if (!tc::mbar_wait_ns(bbar, 0, kWaitNs)) *abort_flag = 1;
+        }
+        __syncwarp();
+    }
+    else if (warp == 1)
+    {
+        // ---- MMA issue ----
+        if (lane == 0)
+        {
+            constexpr uint32_t IDESC = tc::idesc_f16(128, NM, BF16);
+            const uint32_t b0 = tc::smem_u32(bsm);
+            bool ok = wait_bar(bbar, 0, abort_flag);
+            int it = 0, last = -1;
+            for (int tile = blockIdx.x; ok && tile < P.ntiles; tile += gridDim.x, it++)
+            {
+                const int s = it & 1;
+                const uint32_t u = static_cast<uint32_t>(it) >> 1;
+                ok = wait_bar(&ready[s], u & 1u, abort_flag);
+                if (ok && u >= 1) ok = wait_bar(&tfree[s], (u - 1) & 1u, abort_flag);
+                if (!ok) break;
+                tc::fence_after_sync();
+                // descriptors: stage s plane 0 slot 0 and B chunk 0, then
+                // compile-time offsets in 16-byte units per tap and channel pair
+                const uint64_t adesc = tc::smem_desc(tc::smem_u32(smem + s * G::WIN_BYTES), PLANE_BYTES, 128);
+                const uint64_t bdesc = tc::smem_desc(b0, NM * 16, 128);
+#pragma unroll 1
+                for (int b = 0; b < NBLK; b++)
+                {
+                    const uint32_t d = tmem + static_cast<uint32_t>((s * NBLK + b) * F);
+                    const uint64_t ab = adesc + static_cast<uint64_t>(PAD + 128 * b);
+#pragma unroll
+                    for (int t = 0; t < 9; t++)
+#pragma unroll
+                        for (int j2 = 0; j2 < F / 16; j2++)
+                        {
+                            constexpr int PL16 = PLANE_BYTES / 16;
+                            const int off = 2 * j2 * PL16 + (t / 3 - 1) * WW + (t % 3 - 1);
+                            tc::mma_f16(d, ab + static_cast<uint64_t>(static_cast<int64_t>(off)),
+                                        bdesc + static_cast<uint64_t>((t * (F / 16) + j2) * (CHUNK_M / 16)), IDESC,
+                                        (t | j2) ? 1u : 0u);
+                        }
+                }
+                tc::mma_commit(&mdone[s]);
+                last = it;
+            }
+            // the last MMAs complete before tensor memory is released
+            if (last >= 0 && !tc::mbar_wait_ns(&mdone[last & 1], (static_cast<uint32_t>(last) >> 1) & 1u, kWaitNs))
+                *abort_flag = 1;
+        }
+        __syncwarp();
+    }
+    else
+    {
+        // ---- epilogue: warp w drains lane quarter w % 4 of blocks (w - 2) / 4 + k NEPI / 4 ----
+        const int q4 = warp & 3, part = (warp - 2) >> 2;
+        int it = 0;
+        for (int tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x, it++)
+        {
+            const int s = it & 1;
+            const uint32_t u = static_cast<uint32_t>(it) >> 1;
+            const bool got = wait_bar(&mdone[s], u & 1u, abort_flag);
+            if (!__all_sync(0xffffffffu, got ? 1 : 0)) break;
+            tc::fence_after_sync();
+            const ImgP& I = P.img[image_of(P, tile)];
+            const int local = tile - I.tile0;
+            const int x0 = (local % I.tiles_x) * TW - 1, y0 = (local / I.tiles_x) * TH - 1;
+            for (int b = part; b < NBLK; b += NEPI / 4)
+            {
+                if constexpr (MODE == kUp)
+                {
+                    float q[16];
+                    tc::tmem_ld16(tmem + (static_cast<uint32_t>(q4 * 32) << 16) + static_cast<uint32_t>((s * NBLK + b) * F), q);
+                    tc::tmem_wait_ld();
+                    const int p = b * 128 + q4 * 32 + lane;
+                    const int y = p / WW, x = p - y * WW;
+                    const int gx = x0 + x, gy = y0 + y;
+                    if (y < 1 || y > TH || x < 1 || x > TW || gx >= I.w || gy >= I.h) continue;
+                    // conv3x3 F -> 4 + bias, pixel shuffle 2x2, fromFloat (no nearest add)
+                    OT* r0 = row_ptr_w<OT>(I.dst.ptr, I.dst.pitch, 2 * gy) + 2 * gx;
+                    OT* r1 = row_ptr_w<OT>(I.dst.ptr, I.dst.pitch, 2 * gy + 1) + 2 * gx;
+                    r0[0] = from_float<OT>(q[0] + q[4] + P.b[0]);
+                    r0[1] = from_float<OT>(q[1] + q[5] + P.b[1]);
+                    r1[0] = from_float<OT>(q[2] + q[6] + P.b[2]);
+                    r1[1] = from_float<OT>(q[3] + q[7] + P.b[3]);
+                    continue;
+                }
+                float v[F];
+#pragma unroll
+                for (int h = 0; h < F / 16; h++)
+                {
+                    float q[16];
+                    tc::tmem_ld16(tmem + (static_cast<uint32_t>(q4 * 32) << 16) + static_cast<uint32_t>((s * NBLK + b) * F + 16 * h), q);
+                    tc::tmem_wait_ld();
+#pragma unroll
+                    for (int c = 0; c < 16; c++) v[16 * h + c] = q[c];
+                }
+                const int p = b * 128 + q4 * 32 + lane;
+                const int y = p / WW, x = p - y * WW;
+                const int gx = x0 + x, gy = y0 + y;
+                if (y < 1 || y > TH || x < 1 || x > TW || gx >= I.w || gy >= I.h) continue;
+                const size_t o = (static_cast<size_t>(gy) * I.w + gx) * NP;
+#pragma unroll
+                for (int n = 0; n < F; n++) v[n] += P.b[n];
+                if constexpr (MODE == kReLU)
+                {
+#pragma unroll
+                    for (int n = 0; n < F; n++) v[n] = fmaxf(v[n], 0.0f);
+                }
+                else if constexpr (MODE == kPReLU || MODE == kFsrTail)
+                {
+#pragma unroll
+                    for (int n = 0; n < F; n++) v[n] = prelu(v[n], P.a[n]);
+                }
+                if constexpr (MODE == kAddSkip)
+                {
+#pragma unroll
+                    for (int j = 0; j < NP; j++)
+                    {
+                        float sk[8];
+                        unpack8<BF16>(I.skip[o + j], sk);
+#pragma unroll
+                        for (int c = 0; c < 8; c++) v[8 * j + c] += sk[c];
+                    }
+                }
+                if constexpr (MODE == kFsrTail)
+                {
+                    // conv1x1 F->F + bias, + feat, PReLU
+                    float uo[F];
+#pragma unroll
+                    for (int n = 0; n < F; n++)
+                    {
+                        float a1 = P.b1[n];
+#pragma unroll
+                        for (int c = 0; c < F; c++) a1 = fmaf(v[c], P.k1[n * F + c], a1);
+                        uo[n] = a1;
+                    }
+#pragma unroll
+                    for (int j = 0; j < NP; j++)
+                    {
+                        float f[8];
+                        unpack8<BF16>(I.skip[o + j], f);
+#pragma unroll
+                        for (int c = 0; c < 8; c++) v[8 * j + c] = prelu(uo[8 * j + c] + f[c], P.a1[8 * j + c]);
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < NP; j++) I.out[o + j] = pack8<BF16>(v + 8 * j);
+            }
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&tfree[s]);
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0 && *abort_flag) atomicExch(P.status, 1);
+    if (warp == 1) tc::tmem_dealloc(tmem, G::TMEM_COLS);
+}
+
 template <int K, int F>
 struct HeadP
 {
@@ -306,44 +666,6 @@ __global__ void __launch_bounds__(256) head_kernel(const __grid_constant__ HeadP
     }
 }
 
-template <int F>
-struct UpP
-{
-    float k[4 * 9 * F];
-    float b[4];
-};
-
-// conv3x3 F -> 4 (identity) in FP32 from the 16-bit map, pixel shuffle 2x2,
-// fromFloat; no nearest add.
-template <typename T, int F, bool BF16>
-__global__ void __launch_bounds__(256) up_kernel(const __grid_constant__ UpP<F> U, const uint4* __restrict__ map, Plane src, Plane dst)
-{
-    const int w = src.w, h = src.h;
-    const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
-    if (x >= w || y >= h) return;
-    float acc[4];
-#pragma unroll
-    for (int n = 0; n < 4; n++) acc[n] = U.b[n];
-#pragma unroll
-    for (int p = 0; p < 9; p++)
-    {
-        const int gy = clampi(y + p / 3 - 1, 0, h - 1), gx = clampi(x + p % 3 - 1, 0, w - 1);
-        const uint4* px = map + (static_cast<size_t>(gy) * w + gx) * (F / 8);
-#pragma unroll
-        for (int j = 0; j < F / 8; j++)
-        {
-            float xv[8];
-            unpack8<BF16>(px[j], xv);
-#pragma unroll
-            for (int n = 0; n < 4; n++)
-#pragma unroll
-                for (int c = 0; c < 8; c++) acc[n] = fmaf(xv[c], U.k[n * 9 * F + p * F + 8 * j + c], acc[n]);
-        }
-    }
-#pragma unroll
-    for (int n = 0; n < 4; n++) row_ptr_w<T>(dst.ptr, dst.pitch, 2 * y + (n >> 1))[2 * x + (n & 1)] = from_float<T>(acc[n]);
-}
-
 uint16_t to_bits(float v, bool bf16)
 {
     if (bf16)
@@ -373,6 +695,42 @@ void pack_f3_conv(const float* k, int F, bool bf16, uint16_t* out)
         }
 }
 
+float from_bits(uint16_t b, bool bf16)
+{
+    if (bf16)
+    {
+        const uint32_t u = static_cast<uint32_t>(b) << 16;
+        float v;
+        std::memcpy(&v, &u, 4);
+        return v;
+    }
+    return __half2float(__ushort_as_half(b));
+}
+
+// The upscale layer k[n * 9F + tap * F + c] (n < 4) as the 9 F/16 B chunks of
+// an N = 16 GEMM: column n < 4 holds the 16-bit weight, column n + 4 the
+// 16-bit residual w - hi (together exact to about 2^-22), columns 8..15 zero.
+// Chunk (tap t, channel pair j2) element (n, kk) at byte
+// (kk / 8) 256 + (n / 8) 128 + (n % 8) 16 + (kk % 8) 2.
+void pack_f3_up(const float* k, int F, bool bf16, uint16_t* out)
+{
+    constexpr int N = 16;
+    std::memset(out, 0, static_cast<size_t>(9) * F * N * 2);
+    for (int t = 0; t < 9; t++)
+        for (int j2 = 0; j2 < F / 16; j2++)
+        {
+            uint16_t* ch = out + (t * (F / 16) + j2) * (N * 16);
+            for (int n = 0; n < 8; n++)
+                for (int kk = 0; kk < 16; kk++)
+                {
+                    const float wv = k[(n & 3) * 9 * F + t * F + 16 * j2 + kk];
+                    const uint16_t hi = to_bits(wv, bf16);
+                    ch[((kk >> 3) * 16 * N + (n >> 3) * 128 + (n & 7) * 16 + (kk & 7) * 2) / 2] =
+                        n < 4 ? hi : to_bits(wv - from_bits(hi, bf16), bf16);
+                }
+        }
+}
+
 template <int F, int MODE, bool BF16>
 cudaError_t launch_conv(const ConvWP<F>& p, int tiles, cudaStream_t stream)
 {
@@ -386,6 +744,42 @@ cudaError_t launch_conv(const ConvWP<F>& p, int tiles, cudaStream_t stream)
     }
     convw_kernel<F, MODE, BF16><<<tiles, G::THREADS, G::SMEM_REQ, stream>>>(p);
     return cudaGetLastError();
+}
+
+template <int F, int MODE, bool BF16, typename OT = uint8_t>
+cudaError_t launch_convp(const ConvPP<F>& p, cudaStream_t stream)
+{
+    using G = GeoP<F>;
+    static int per_sm = 0, sms = 0;
+    if (per_sm == 0)
+    {
+        cudaError_t err =
+            cudaFuncSetAttribute(convp_kernel<F, MODE, BF16, OT>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM_REQ);
+        if (err != cudaSuccess) return err;
+        int occ = 0, dev = 0;
+        if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, convp_kernel<F, MODE, BF16, OT>, G::THREADS, G::SMEM_REQ)) !=
+            cudaSuccess)
+            return err;
+        if ((err = cudaGetDevice(&dev)) != cudaSuccess) return err;
+        if ((err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return err;
+        if (occ < 1) return cudaErrorInvalidConfiguration;
+        per_sm = occ < static_cast<int>(512 / G::TMEM_COLS) ? occ : static_cast<int>(512 / G::TMEM_COLS);
+    }
+    const int grid = p.ntiles < per_sm * sms ? p.ntiles : per_sm * sms;
+    convp_kernel<F, MODE, BF16, OT><<<grid, G::THREADS, G::SMEM_REQ, stream>>>(p);
+    return cudaGetLastError();
+}
+
+template <int F, bool BF16>
+cudaError_t convp_mode(int mode, const ConvPP<F>& p, cudaStream_t stream)
+{
+    switch (mode)
+    {
+    case kReLU: return launch_convp<F, kReLU, BF16>(p, stream);
+    case kPReLU: return launch_convp<F, kPReLU, BF16>(p, stream);
+    case kAddSkip: return launch_convp<F, kAddSkip, BF16>(p, stream);
+    default: return launch_convp<F, kFsrTail, BF16>(p, stream);
+    }
 }
 
 template <int F, bool BF16>
@@ -432,6 +826,13 @@ cudaError_t run_typed(const float* kernels, const float* biases, const float* al
     const size_t lb = static_cast<size_t>(9) * F * F;  // packed 16-bit values per layer
     const int hk = F * K * K;                           // head kernel floats
     const uint4* cur = feat;
+    // parameters of the persistent kernel (large: thread-local, not on the stack)
+    static thread_local ConvPP<F> pp_storage;
+    ConvPP<F>& r = pp_storage;
+    std::memset(&r, 0, sizeof(r));
+    r.status = status;
+    r.nimg = 1;
+    r.ntiles = tiles;
     // ArtCNN: blocks ReLU layers, then identity + feat.  FSRCNNX: blocks-1
     // PReLU layers, then the tail (PReLU, 1x1 + feat, PReLU).
     const int nconv = artcnn ? blocks + 1 : blocks;
@@ -458,7 +859,23 @@ cudaError_t run_typed(const float* kernels, const float* biases, const float* al
                 q.a1[i] = alphas[F * l + i];
             }
         }
-        cudaError_t err = conv_mode<F, BF16>(mode, q, tiles, stream);
+        cudaError_t err;
+        if constexpr (F == 32)
+        {
+            // 32 channels: the persistent TMA-fed pipeline (one CTA per SM)
+            r.bw = q.bw;
+            std::memcpy(r.b, q.b, sizeof(r.b));
+            std::memcpy(r.a, q.a, sizeof(r.a));
+            std::memcpy(r.k1, q.k1, sizeof(r.k1));
+            std::memcpy(r.b1, q.b1, sizeof(r.b1));
+            std::memcpy(r.a1, q.a1, sizeof(r.a1));
+            r.img[0] = ImgP{feat, a, w, h, c.img[0].tiles_x, 0, Plane{}};
+            if (!encode_tmap_3d_u16(&r.tmap[0], cur, F, w, h, 8, WW, WH)) return cudaErrorInvalidValue;
+            err = convp_mode<F, BF16>(mode, r, stream);
+        }
+        else
+            // 16 channels: one CTA per tile, four per SM (measured faster here)
+            err = conv_mode<F, BF16>(mode, q, tiles, stream);
         if (err != cudaSuccess) return err;
         count_launch();
         cur = a;
@@ -466,14 +883,14 @@ cudaError_t run_typed(const float* kernels, const float* biases, const float* al
         a = bm;
         bm = t;
     }
-    // upscale: ArtCNN layer blocks+2, FSRCNNX layer blocks+2 (after the 1x1)
+    // upscale (ArtCNN layer blocks+2, FSRCNNX layer blocks+2 after the 1x1) on
+    // the tensor core: its packed B follows the 3x3 layers'
     const int lu = blocks + 2;
-    UpP<F> u;
-    const float* uk = artcnn ? kernels + hk + F * F * 9 * (blocks + 1) : kernels + hk + F * F * 9 * blocks + F * F;
-    for (int i = 0; i < 4 * 9 * F; i++) u.k[i] = uk[i];
-    for (int i = 0; i < 4; i++) u.b[i] = biases[F * lu + i];
-    up_kernel<T, F, BF16><<<pgrid, 256, 0, stream>>>(u, cur, in, out);
-    cudaError_t err = cudaGetLastError();
+    r.bw = static_cast<const uint4*>(packed) + nconv * lb * 2 / 16;
+    for (int i = 0; i < 4; i++) r.b[i] = biases[F * lu + i];
+    r.img[0] = ImgP{nullptr, nullptr, w, h, c.img[0].tiles_x, 0, out};
+    if (!encode_tmap_3d_u16(&r.tmap[0], cur, F, w, h, 8, WW, WH)) return cudaErrorInvalidValue;
+    cudaError_t err = launch_convp<F, kUp, BF16, T>(r, stream);
     if (err == cudaSuccess) count_launch();
     return err;
 }
@@ -494,14 +911,16 @@ cudaError_t run_type(const float* kernels, const float* biases, const float* alp
 }  // namespace f3tc
 
 // Packed B of the 3x3 F->F layers of an ArtCNN (blocks + 1 layers) or
-// FSRCNNX (blocks layers) model, F = 16 or 32.
+// FSRCNNX (blocks layers) model, F = 16 or 32, then the upscale layer's.
 void pack_f3_tc_weights(const float* kernels, int F, bool artcnn, int blocks, bool bf16, std::vector<uint16_t>& packed)
 {
     const int layers = artcnn ? blocks + 1 : blocks;
     const int head = artcnn ? F * 9 : F * 25;
     const size_t lb = static_cast<size_t>(9) * F * F;
-    packed.assign(layers * lb, 0);
+    packed.assign(layers * lb + static_cast<size_t>(9) * F * 16, 0);
     for (int l = 0; l < layers; l++) f3tc::pack_f3_conv(kernels + head + F * F * 9 * l, F, bf16, packed.data() + l * lb);
+    const float* up = kernels + head + F * F * 9 * layers + (artcnn ? 0 : F * F);  // FSRCNNX: after the 1x1
+    f3tc::pack_f3_up(up, F, bf16, packed.data() + layers * lb);
 }
 
 cudaError_t launch_f3_tc(const float* kernels, const float* biases, const float* alphas, bool artcnn, int F, int blocks,

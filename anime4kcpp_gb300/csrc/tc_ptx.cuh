@@ -215,6 +215,17 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, int x, 
         "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(smem_u32(mbar))
         : "memory");
 }
+// 3-D tiled tensor load into shared memory; completion counted in bytes on
+// mbar.  The innermost coordinate c times the element size must be a multiple
+// of 16; x and y may be negative or past the end (those elements read zero).
+__device__ __forceinline__ void tma_load_3d(void* dst, const void* tmap, int c, int x, int y, uint64_t* mbar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(c), "r"(x), "r"(y), "r"(smem_u32(mbar))
+        : "memory");
+}
 // 2-D tiled tensor store from shared memory (bulk group); x, y >= 0.
 __device__ __forceinline__ void tma_store_2d(const void* tmap, int x, int y, const void* src)
 {

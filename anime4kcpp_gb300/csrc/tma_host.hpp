@@ -18,4 +18,9 @@ bool tma_plane_ok(const void* base, int pitch);
 // out-of-bounds elements read as zero.
 bool encode_tmap_2d(CUtensorMap* map, const void* base, int elem_bytes, int dim_x, int dim_y, int pitch, int box_x, int box_y);
 
+// 3-D tiled tensor map over a dense [d2][d1][d0] array of 16-bit elements
+// (d0 * 2 a multiple of 16 bytes); box of b0 x b1 x b2 elements (b0 * 2 a
+// multiple of 16), no swizzle, out-of-bounds elements read as zero.
+bool encode_tmap_3d_u16(CUtensorMap* map, const void* base, int d0, int d1, int d2, int b0, int b1, int b2);
+
 }  // namespace acgb
