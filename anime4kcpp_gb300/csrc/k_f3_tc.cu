@@ -13,9 +13,11 @@
 // 9 F/16 of them.  8 blocks per window, F tensor-memory columns each.
 //
 // Two kernels run these GEMMs: convw_kernel, one CTA per tile (the 16-channel
-// layers), and convp_kernel, persistent CTAs with a TMA-fed two-stage
-// pipeline (the 32-channel layers and every upscale layer, which it runs with
-// N = 16 and the weights split into 16-bit high parts and residuals).
+// 3x3 layers but FSRCNNX's tail), and convp_kernel, persistent CTAs with a
+// TMA-fed two-stage pipeline (the 32-channel layers, FSRCNNX's tail, whose
+// FP32 1x1 epilogue it overlaps with the MMAs, and every upscale layer, which
+// it runs with N = 16 and the weights split into 16-bit high parts and
+// residuals).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -639,16 +641,23 @@ struct HeadP
 template <typename T, int K, int F, bool BF16>
 __global__ void __launch_bounds__(256) head_kernel(const __grid_constant__ HeadP<K, F> W, Plane in, uint4* __restrict__ feat)
 {
-    constexpr int R = K / 2;
-    const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    constexpr int R = K / 2, SW = 32 + 2 * R, SH = 8 + 2 * R;
+    // the block's 32 x 8 pixels with their clamped halo, converted once
+    __shared__ float s[SH][SW];
+    const int bx = blockIdx.x * 32, by = blockIdx.y * 8;
+    for (int i = threadIdx.x; i < SW * SH; i += 256)
+    {
+        const int sy = i / SW, sx = i - sy * SW;
+        const int gx = clampi(bx - R + sx, 0, in.w - 1), gy = clampi(by - R + sy, 0, in.h - 1);
+        s[sy][sx] = to_float<T>(row_ptr<T>(in.ptr, in.pitch, gy)[gx]);
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int x = bx + tx, y = by + ty;
     if (x >= in.w || y >= in.h) return;
     float t[K * K];
 #pragma unroll
-    for (int p = 0; p < K * K; p++)
-    {
-        const int gy = clampi(y + p / K - R, 0, in.h - 1), gx = clampi(x + p % K - R, 0, in.w - 1);
-        t[p] = to_float<T>(row_ptr<T>(in.ptr, in.pitch, gy)[gx]);
-    }
+    for (int p = 0; p < K * K; p++) t[p] = s[ty + p / K][tx + p % K];
     uint4* o = feat + (static_cast<size_t>(y) * in.w + x) * (F / 8);
 #pragma unroll
     for (int j = 0; j < F / 8; j++)
@@ -860,9 +869,10 @@ cudaError_t run_typed(const float* kernels, const float* biases, const float* al
             }
         }
         cudaError_t err;
-        if constexpr (F == 32)
+        if (F == 32 || mode == kFsrTail)
         {
-            // 32 channels: the persistent TMA-fed pipeline (one CTA per SM)
+            // 32 channels, and FSRCNNX's tail with its FP32 1x1 epilogue: the
+            // persistent TMA-fed pipeline, epilogue overlapped with the MMAs
             r.bw = q.bw;
             std::memcpy(r.b, q.b, sizeof(r.b));
             std::memcpy(r.a, q.a, sizeof(r.a));
@@ -874,7 +884,7 @@ cudaError_t run_typed(const float* kernels, const float* biases, const float* al
             err = convp_mode<F, BF16>(mode, r, stream);
         }
         else
-            // 16 channels: one CTA per tile, four per SM (measured faster here)
+            // the other 16-channel layers: one CTA per tile, four per SM (measured faster here)
             err = conv_mode<F, BF16>(mode, q, tiles, stream);
         if (err != cudaSuccess) return err;
         count_launch();
