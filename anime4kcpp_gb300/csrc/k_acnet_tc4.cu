@@ -22,23 +22,18 @@ uint16_t bits16(float v, bool bf16)
     return __half_as_ushort(__float2half_rn(v));
 }
 
-// One layer of 3x3 8->8 weights k[n * 72 + tap * 8 + c] (reference NHWC
-// order) as the nine N32 x K16 B chunks of the quad GEMM.  Chunk 3 dy + j
-// multiplies tap row dy; its K halves hold the 8 channels of the input
-// pixels at offsets (0, -1), (+1, +2), (+4, +3) from the row's first pixel
-// 4r for j = 0, 1, 2.  Output column n is pixel 4r + n / 8, channel n % 8;
-// input offset o feeds output pixel k through tap dx = o - k + 1 (zero
-// weight outside 0..2).  Bytes of element (n, kk) in a chunk: (kk / 8) 512 +
-// (n / 8) 128 + (n % 8) 16 + (kk % 8) 2 (K-major, no swizzle, leading byte
-// offset 512, stride byte offset 128).
+}  // namespace
+
+namespace tcv4 {
+
 void pack_quad_conv8(const float* k, bool bf16, uint16_t* out)
 {
     static const int off[3][2] = {{0, -1}, {1, 2}, {4, 3}};
-    std::memset(out, 0, tcv4::BL_BYTES);
+    std::memset(out, 0, BL_BYTES);
     for (int dy = 0; dy < 3; dy++)
         for (int j = 0; j < 3; j++)
         {
-            uint16_t* ch = out + (3 * dy + j) * (tcv4::CHUNK_BYTES / 2);
+            uint16_t* ch = out + (3 * dy + j) * (CHUNK_BYTES / 2);
             for (int n = 0; n < 32; n++)
                 for (int kk = 0; kk < 16; kk++)
                 {
@@ -50,7 +45,25 @@ void pack_quad_conv8(const float* k, bool bf16, uint16_t* out)
         }
 }
 
-}  // namespace
+void pack_quad_layer0(const float* k, bool bf16, uint16_t* out)
+{
+    auto round16 = [bf16](float v) {
+        return bf16 ? __bfloat162float(__float2bfloat16_rn(v)) : __half2float(__float2half_rn(v));
+    };
+    std::vector<float> k0(576, 0.0f);
+    for (int n = 0; n < 8; n++)
+        for (int t = 0; t < 9; t++)
+        {
+            const float v = k[n * 9 + t];
+            const float hi = round16(v);
+            k0[n * 72 + t * 8 + 0] = hi;
+            k0[n * 72 + t * 8 + 1] = hi;
+            k0[n * 72 + t * 8 + 2] = v - hi;
+        }
+    pack_quad_conv8(k0.data(), bf16, out);
+}
+
+}  // namespace tcv4
 
 int acnet_tc4_max_images() { return tcv4::kMaxImages; }
 
@@ -65,21 +78,9 @@ void acnet_tc4_shape(int* tw, int* th)
 void pack_acnet_tc4_weights(const AcnetLegacyWeights& w, bool bf16, std::vector<uint16_t>& packed)
 {
     using namespace tcv4;
+    constexpr int NL = NetLegacy::NL;
     packed.assign(static_cast<size_t>(NL) * BL_BYTES / 2, 0);
-    auto round16 = [bf16](float v) {
-        return bf16 ? __bfloat162float(__float2bfloat16_rn(v)) : __half2float(__float2half_rn(v));
-    };
-    std::vector<float> k0(576, 0.0f);
-    for (int n = 0; n < 8; n++)
-        for (int t = 0; t < 9; t++)
-        {
-            const float v = w.k[n * 9 + t];
-            const float hi = round16(v);
-            k0[n * 72 + t * 8 + 0] = hi;
-            k0[n * 72 + t * 8 + 1] = hi;
-            k0[n * 72 + t * 8 + 2] = v - hi;
-        }
-    pack_quad_conv8(k0.data(), bf16, packed.data());
+    pack_quad_layer0(w.k, bf16, packed.data());
     for (int l = 1; l < NL; l++)
         pack_quad_conv8(w.k + 72 + 576 * (l - 1), bf16, packed.data() + static_cast<size_t>(l) * BL_BYTES / 2);
 }
@@ -101,7 +102,7 @@ cudaError_t launch_acnet_legacy_tc4_core(const AcnetLegacyWeights& wts, const vo
     std::memset(&p, 0, sizeof(p));
     p.bw = static_cast<const uint4*>(packed4);
     for (int i = 0; i < 32; i++) p.k2[i] = wts.k[72 + 576 * 8 + i];
-    for (int l = 0; l < NL; l++)
+    for (int l = 0; l < NetLegacy::NL; l++)
         for (int k = 0; k < 8; k++) p.bias[l][k] = wts.b[8 * l + k];
     if (phase2) p.ph = *phase2;
     constexpr int TW = Geo0::TW, TH = Geo0::TH;
@@ -122,7 +123,7 @@ cudaError_t launch_acnet_legacy_tc4_core(const AcnetLegacyWeights& wts, const vo
     cudaError_t err = cudaMemsetAsync(counter, 0, sizeof(int), stream);
     if (err != cudaSuccess) return err;
     const int grid = tiles < ctas ? tiles : ctas;
-    err = launch_shape<Geo0>(type, c, bf16, p, grid, per_sm_cap, stream);
+    err = launch_shape<Geo0, NetLegacy>(type, c, bf16, p, grid, per_sm_cap, stream);
     if (err == cudaSuccess) count_launch();
     return err;
 }

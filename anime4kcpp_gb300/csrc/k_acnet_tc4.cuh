@@ -27,6 +27,15 @@
 //    the CTA's tiles) into the slot of layer G - 1 once every MMA of layer
 //    G - 1 completed, so the weights of all nine layers never sit in shared
 //    memory at once and two CTAs still share an SM.
+//
+// The same kernel runs ACNet<8> with 4 or 8 blocks (NetAcn8; reference
+// CPUProcessor.cpp:1417-1436, Common.hpp:290-342): layer 0 and the blocks
+// with PReLU (per layer and channel slopes) instead of ReLU, and as its last
+// MMA layer the conv3x3 8 -> 4 (channels 4..7 carry the 16-bit residuals of
+// the weights of channels 0..3, summed in the epilogue) whose outputs are
+// pixel-shuffled and added to the source pixel (nearest) instead of
+// ACNetLegacy's 2x2 transposed conv.  The halo is the number of 3x3
+// layers: 9 (ACNetLegacy), 6 (ACNet<8> B4), 10 (B8).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -42,14 +51,12 @@
 namespace acgb {
 namespace tcv4 {
 
-constexpr int HALO = 9;
 constexpr int NBLK = 8;                      // 8 x 128 quad rows per window
 constexpr int NROUND = 4;                    // two blocks (one per issuer) per round
 constexpr int KCH = 9;                       // MMAs (K16 chunks) per block and layer
 constexpr int CHUNK_BYTES = 1024;            // B of one MMA: N32 x K16 x 16 bit
 constexpr int BL_BYTES = KCH * CHUNK_BYTES;  // one layer's B
-constexpr int NL = 9;                        // MMA layers: layer 0 and the eight 3x3 8->8 layers
-constexpr int LAST = NL - 1;
+constexpr int NLMAX = 10;  // MMA layers of the deepest network run here (ACNet<8> B8)
 constexpr int NBUF = 3;                      // B ring slots
 constexpr int B_BYTES = NBUF * BL_BYTES;
 constexpr int NEPI = 8;
@@ -60,10 +67,24 @@ constexpr uint64_t kWaitNs = 2000000000ull;
 constexpr int kMaxImages = 64;
 static_assert(NBLK * 32 <= static_cast<int>(TMEM_COLS), "one 32-column accumulator per block");
 
-template <int TW_, int TH_>
+// ACNetLegacy: layer 0, eight 3x3 8->8 layers (ReLU), 2x2 transposed conv.
+struct NetLegacy
+{
+    static constexpr int NL = 9;  // MMA layers (3x3 convolutions)
+    static constexpr bool ACN8 = false;
+};
+// ACNet<8> with B blocks: layer 0, B 3x3 8->8 layers (PReLU), conv3x3 8->4.
+template <int B>
+struct NetAcn8
+{
+    static constexpr int NL = B + 2;
+    static constexpr bool ACN8 = true;
+};
+
+template <int TW_, int TH_, int HALO_>
 struct Geo
 {
-    static constexpr int TW = TW_, TH = TH_;
+    static constexpr int TW = TW_, TH = TH_, HALO = HALO_;
     static constexpr int WW = TW + 2 * HALO, WH = TH + 2 * HALO;
     static constexpr int QPR = WW / 4;  // quads per window row
     static constexpr int PADQ = QPR + 2;
@@ -102,7 +123,8 @@ struct Params
 {
     const uint4* bw;    // NL packed B matrices in global memory (pack_acnet_tc4_weights)
     float k2[32];
-    float bias[NL][8];  // layers 0..8, preloaded into the accumulators
+    float bias[NLMAX][8];   // per MMA layer, preloaded into the accumulators
+    float alpha[NLMAX][8];  // ACNet<8>: PReLU slopes of layers 0 .. NL - 2
     Phase2 ph;
     int nimg;
     int ntiles;
@@ -110,6 +132,17 @@ struct Params
     int* status;
     Image4 img[kMaxImages];
 };
+
+template <bool BF16>
+__device__ __forceinline__ uint4 pack8_plain(const float* v)
+{
+    if constexpr (BF16)
+        return make_uint4(tc::pack_bf16x2(v[0], v[1]), tc::pack_bf16x2(v[2], v[3]), tc::pack_bf16x2(v[4], v[5]),
+                          tc::pack_bf16x2(v[6], v[7]));
+    else
+        return make_uint4(tc::pack_f16x2(v[0], v[1]), tc::pack_f16x2(v[2], v[3]), tc::pack_f16x2(v[4], v[5]),
+                          tc::pack_f16x2(v[6], v[7]));
+}
 
 template <bool BF16>
 __device__ __forceinline__ uint4 pack8(const float* v)
@@ -193,11 +226,13 @@ struct LayerRange
     }
 };
 
-template <class G, typename T, int C, bool BF16>
+template <class G, class NET, typename T, int C, bool BF16>
 __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_constant__ Params P)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     using L = Layout<G, T, C>;
+    constexpr int NL = NET::NL, LAST = NL - 1, HALO = G::HALO;
+    static_assert(HALO == NL && NL <= NLMAX, "one halo pixel per 3x3 layer");
     constexpr int TW = G::TW, TH = G::TH, WW = G::WW, WH = G::WH, QPR = G::QPR, PADQ = G::PADQ;
     constexpr int PLANE_BYTES = G::PLANE_BYTES, ACT_BYTES = G::ACT_BYTES;
     constexpr int UVW = G::UVW, UVH = G::UVH, UVX0 = G::UVX0;
@@ -475,7 +510,20 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
                                 if (!row_ok || x < R.rx0 || x > R.rx1) continue;
                                 if (l < LAST)
                                 {
-                                    const uint4 val = pack8<BF16>(v + 8 * kk);
+                                    uint4 val;
+                                    if constexpr (NET::ACN8)
+                                    {
+                                        float a8[8];
+#pragma unroll
+                                        for (int c = 0; c < 8; c++)
+                                        {
+                                            const float u = v[8 * kk + c];
+                                            a8[c] = fmaxf(u, 0.0f) + P.alpha[l][c] * fminf(u, 0.0f);
+                                        }
+                                        val = pack8_plain<BF16>(a8);
+                                    }
+                                    else
+                                        val = pack8<BF16>(v + 8 * kk);
                                     *slot<G>(act, p) = val;
                                     // clamp-to-edge for the next layer (only tiles at an image edge)
                                     if (!edges) continue;
@@ -498,22 +546,45 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
                                 }
                                 else
                                 {
-                                    float s[8];
-#pragma unroll
-                                    for (int c = 0; c < 8; c++) s[c] = fmaxf(v[8 * kk + c], 0.0f);
                                     T o[2][2];
-#pragma unroll
-                                    for (int dy = 0; dy < 2; dy++)
-#pragma unroll
-                                        for (int dx = 0; dx < 2; dx++)
+                                    if constexpr (NET::ACN8)
+                                    {
+                                        // conv3x3 8 -> 4 (+ bias, in the accumulator), pixel
+                                        // shuffle, + the source pixel's luma (nearest), fromFloat
+                                        const int gx = gx0 + x, gy = gy0 + y;
+                                        const T* sp = row_ptr<T>(I.in.ptr, I.in.pitch, gy) + gx * C;
+                                        T yq;
+                                        if constexpr (C == 1) yq = sp[0];
+                                        else
                                         {
-                                            const int ko = 8 * (dy * 2 + dx);
-                                            float d = s[0] * P.k2[ko];
+                                            T px[C], uvq[C - 1];
 #pragma unroll
-                                            for (int c = 1; c < 7; c++) d = fmaf(s[c], P.k2[ko + c], d);
-                                            if constexpr (sizeof(T) < 4) o[dy][dx] = from_unit<T>(fma_sat(s[7], P.k2[ko + 7], d));
-                                            else o[dy][dx] = from_float<T>(fmaf(s[7], P.k2[ko + 7], d));
+                                            for (int c = 0; c < C; c++) px[c] = sp[c];
+                                            rgb_to_yuv_q_lut<T, C>(px, yq, uvq, lut);
                                         }
+                                        const float nearv = to_float_lut<T>(yq, lut);
+#pragma unroll
+                                        for (int n = 0; n < 4; n++)
+                                            o[n >> 1][n & 1] = from_float<T>((v[8 * kk + n] + v[8 * kk + n + 4]) + nearv);
+                                    }
+                                    else
+                                    {
+                                        float s[8];
+#pragma unroll
+                                        for (int c = 0; c < 8; c++) s[c] = fmaxf(v[8 * kk + c], 0.0f);
+#pragma unroll
+                                        for (int dy = 0; dy < 2; dy++)
+#pragma unroll
+                                            for (int dx = 0; dx < 2; dx++)
+                                            {
+                                                const int ko = 8 * (dy * 2 + dx);
+                                                float d = s[0] * P.k2[ko];
+#pragma unroll
+                                                for (int c = 1; c < 7; c++) d = fmaf(s[c], P.k2[ko + c], d);
+                                                if constexpr (sizeof(T) < 4) o[dy][dx] = from_unit<T>(fma_sat(s[7], P.k2[ko + 7], d));
+                                                else o[dy][dx] = from_float<T>(fmaf(s[7], P.k2[ko + 7], d));
+                                            }
+                                    }
                                     const int ox = 2 * (gx0 + x), oy = 2 * (gy0 + y);
                                     T* row0 = row_ptr_w<T>(I.out.ptr, I.out.pitch, oy) + ox * C;
                                     T* row1 = row_ptr_w<T>(I.out.ptr, I.out.pitch, oy + 1) + ox * C;
@@ -553,22 +624,22 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
     if (warp == 0) tc::tmem_dealloc(tmem, TMEM_COLS);
 }
 
-template <class G, typename T, int C, bool BF16>
+template <class G, class NET, typename T, int C, bool BF16>
 cudaError_t launch_typed(const Params& p, int grid, int per_sm_cap, cudaStream_t stream)
 {
     static int per_sm = 0;
     if (per_sm == 0)
     {
-        cudaError_t err = cudaFuncSetAttribute(acnet_tc4_kernel<G, T, C, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t err = cudaFuncSetAttribute(acnet_tc4_kernel<G, NET, T, C, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                Layout<G, T, C>::smem);
         if (err != cudaSuccess) return err;
-        err = cudaFuncSetAttribute(acnet_tc4_kernel<G, T, C, BF16>, cudaFuncAttributePreferredSharedMemoryCarveout,
+        err = cudaFuncSetAttribute(acnet_tc4_kernel<G, NET, T, C, BF16>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                    cudaSharedmemCarveoutMaxShared);
         if (err != cudaSuccess) return err;
         // CTAs per SM from shared memory, registers and threads (as for the
         // pair kernel: two CTAs of 256 tensor-memory columns share an SM).
         cudaFuncAttributes fa;
-        err = cudaFuncGetAttributes(&fa, acnet_tc4_kernel<G, T, C, BF16>);
+        err = cudaFuncGetAttributes(&fa, acnet_tc4_kernel<G, NET, T, C, BF16>);
         if (err != cudaSuccess) return err;
         int dev = 0, smem_sm = 0, reserved = 0, regs_sm = 0;
         if ((err = cudaGetDevice(&dev)) != cudaSuccess) return err;
@@ -583,41 +654,57 @@ cudaError_t launch_typed(const Params& p, int grid, int per_sm_cap, cudaStream_t
                          C, BF16 ? 1 : 0, per_sm, Layout<G, T, C>::smem, fa.numRegs);
     }
     const int k = per_sm < per_sm_cap ? per_sm : (per_sm_cap < 1 ? 1 : per_sm_cap);
-    acnet_tc4_kernel<G, T, C, BF16><<<grid * k, THREADS, Layout<G, T, C>::smem, stream>>>(p);
+    acnet_tc4_kernel<G, NET, T, C, BF16><<<grid * k, THREADS, Layout<G, T, C>::smem, stream>>>(p);
     return cudaGetLastError();
 }
 
-template <class G, typename T, bool BF16>
+template <class G, class NET, typename T, bool BF16>
 cudaError_t launch_channels(int c, const Params& p, int grid, int per_sm_cap, cudaStream_t stream)
 {
     switch (c)
     {
-    case 1: return launch_typed<G, T, 1, BF16>(p, grid, per_sm_cap, stream);
-    case 3: return launch_typed<G, T, 3, BF16>(p, grid, per_sm_cap, stream);
-    case 4: return launch_typed<G, T, 4, BF16>(p, grid, per_sm_cap, stream);
+    case 1: return launch_typed<G, NET, T, 1, BF16>(p, grid, per_sm_cap, stream);
+    case 3: return launch_typed<G, NET, T, 3, BF16>(p, grid, per_sm_cap, stream);
+    case 4: return launch_typed<G, NET, T, 4, BF16>(p, grid, per_sm_cap, stream);
     default: return cudaErrorInvalidValue;
     }
 }
 
-template <class G>
+template <class G, class NET>
 cudaError_t launch_shape(int type, int c, bool bf16, const Params& p, int grid, int per_sm_cap, cudaStream_t stream)
 {
     switch (type)
     {
     case kU8:
-        return bf16 ? launch_channels<G, uint8_t, true>(c, p, grid, per_sm_cap, stream)
-                    : launch_channels<G, uint8_t, false>(c, p, grid, per_sm_cap, stream);
+        return bf16 ? launch_channels<G, NET, uint8_t, true>(c, p, grid, per_sm_cap, stream)
+                    : launch_channels<G, NET, uint8_t, false>(c, p, grid, per_sm_cap, stream);
     case kU16:
-        return bf16 ? launch_channels<G, uint16_t, true>(c, p, grid, per_sm_cap, stream)
-                    : launch_channels<G, uint16_t, false>(c, p, grid, per_sm_cap, stream);
+        return bf16 ? launch_channels<G, NET, uint16_t, true>(c, p, grid, per_sm_cap, stream)
+                    : launch_channels<G, NET, uint16_t, false>(c, p, grid, per_sm_cap, stream);
     case kF32:
-        return bf16 ? launch_channels<G, float, true>(c, p, grid, per_sm_cap, stream)
-                    : launch_channels<G, float, false>(c, p, grid, per_sm_cap, stream);
+        return bf16 ? launch_channels<G, NET, float, true>(c, p, grid, per_sm_cap, stream)
+                    : launch_channels<G, NET, float, false>(c, p, grid, per_sm_cap, stream);
     default: return cudaErrorInvalidValue;
     }
 }
 
-using Geo0 = Geo<46, 46>;  // 64 x 64 window
+using Geo0 = Geo<46, 46, 9>;     // ACNetLegacy: 64 x 64 window
+using GeoA8B4 = Geo<52, 48, 6>;  // ACNet<8> B4: 64 x 60 window (chroma sums of a 52 x 52 tile would not fit)
+using GeoA8B8 = Geo<44, 44, 10>; // ACNet<8> B8
+
+// One layer of 3x3 8->8 weights k[n * 72 + tap * 8 + c] (reference NHWC
+// order) as the nine N32 x K16 B chunks of the quad GEMM.  Chunk 3 dy + j
+// multiplies tap row dy; its K halves hold the 8 channels of the input
+// pixels at offsets (0, -1), (+1, +2), (+4, +3) from the row's first pixel
+// 4r for j = 0, 1, 2.  Output column n is pixel 4r + n / 8, channel n % 8;
+// input offset o feeds output pixel k through tap dx = o - k + 1 (zero
+// weight outside 0..2).  Bytes of element (n, kk) in a chunk: (kk / 8) 512 +
+// (n / 8) 128 + (n % 8) 16 + (kk % 8) 2 (K-major, no swizzle, leading byte
+// offset 512, stride byte offset 128).
+void pack_quad_conv8(const float* k, bool bf16, uint16_t* out);
+// Layer 0 (1 -> 8, k[n * 9 + tap]) as an 8-channel layer over the input slots
+// (y_hi, y_lo, y_hi) with weights (w_hi, w_hi, w_lo).
+void pack_quad_layer0(const float* k, bool bf16, uint16_t* out);
 
 }  // namespace tcv4
 }  // namespace acgb

@@ -109,6 +109,16 @@ cudaError_t launch_acnet_legacy_tc4(const AcnetLegacyWeights& wts, const void* p
 cudaError_t launch_acnet_legacy_tc4_core(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n, const Plane* in,
                                          const Plane* out, const Phase2* phase2, int* counter, int* status, int ctas,
                                          cudaStream_t stream, int per_sm_cap);
+// ACNet<8> with 4 or 8 blocks in the quad kernel (PReLU layers, conv3x3
+// 8 -> 4 pixel-shuffle tail with the nearest-source add; fused colour path as
+// for ACNetLegacy).  `packed4` is the device copy of pack_acnet8_tc4_weights();
+// biases / alphas in the reference layout (8 + 8 blocks + 4 / 8 (blocks + 1)).
+bool acnet8_tc4_supported(int blocks);
+void acnet8_tc4_shape(int blocks, int* tw, int* th);
+void pack_acnet8_tc4_weights(const float* kernels, int blocks, bool bf16, std::vector<uint16_t>& packed);
+cudaError_t launch_acnet8_tc4(const float* biases, const float* alphas, int blocks, const void* packed4, bool bf16, int n,
+                              const Plane* in, const Plane* out, const Phase2* phase2, int* counter, int ctas,
+                              cudaStream_t stream, int per_sm_cap = 2);
 // The quad launch with its tile counter and status word in the static
 // scratch of the allocation-free entry (see launch_acnet_legacy_tc3_noalloc).
 cudaError_t launch_acnet_legacy_tc4_noalloc(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n,

@@ -538,7 +538,20 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
     else if (spec_.family == Family::ACNet8)
     {
         const ModelParams& mp = model_params(spec_);
-        if (precision_ != Precision::FP32 && arnetTc_)
+        if (acnet8Quad())
+        {
+            // B4 / B8: every layer in the persistent quad kernel (with the fused colour path)
+            const bool bf16 = precision_ == Precision::BF16;
+            const void* w = tcWeights(precision_, 3);
+            if (!w) err = cudaErrorMemoryAllocation;
+            else if ((err = ts.counter.ensure(256)) == cudaSuccess)
+            {
+                int* counter = static_cast<int*>(ts.counter.ptr) + (ts.counterSlot++ & 63);
+                err = launch_acnet8_tc4(mp.biases.data(), mp.alphas.data(), spec_.blocks, w, bf16, 1, &in, &out, ph, counter,
+                                        tc3Ctas_ > 0 ? tc3Ctas_ : smCount_, stream, tc3PerSm_ > 0 ? tc3PerSm_ : 2);
+            }
+        }
+        else if (precision_ != Precision::FP32 && arnetTc_)
         {
             // tensor-core form: the 8->8 layers on tcgen05, 16-bit maps between layers
             const bool bf16 = precision_ == Precision::BF16;
@@ -690,7 +703,9 @@ const void* GB300Processor::tcWeights(Precision p, int form)
     if (!deviceWeights_[idx].ptr)
     {
         std::vector<uint16_t> packed;
-        if (form == 3) pack_acnet_tc4_weights(*acnet_, bf16, packed);
+        if (form == 3 && spec_.family == Family::ACNet8)
+            pack_acnet8_tc4_weights(model_params(spec_).kernels.data(), spec_.blocks, bf16, packed);
+        else if (form == 3) pack_acnet_tc4_weights(*acnet_, bf16, packed);
         else if (form == 2) pack_acnet_tc3_weights(*acnet_, bf16, packed);
         else if (form == 1) pack_acnet_tc2_weights(*acnet_, bf16, packed);
         else pack_acnet_tc_weights(*acnet_, bf16, packed);
@@ -819,7 +834,7 @@ bool GB300Processor::run(ThreadState& ts, const DeviceImage& src, const DeviceIm
     // Fused path: RGB(A) x2 in one kernel (split, CNN, chroma resample and
     // merge), when the chroma resample is the exact x2 Catmull-Rom.
     if (c > 1 && power == 1 && fxy == 1.0 && dst.w == 2 * src.w && dst.h == 2 * src.h && fused_ &&
-        spec_.family == Family::ACNetLegacy)
+        (spec_.family == Family::ACNetLegacy || acnet8Quad()))
     {
         Phase2 ph;
         if (phase_weights(2, &ph.w[0][0]))
@@ -1001,12 +1016,13 @@ int GB300Processor::processDevice(const DeviceImage& src, const DeviceImage& dst
 bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, const DeviceImage* dst, double factor,
                               cudaStream_t s)
 {
-    const bool tcBatch = spec_.family == Family::ACNetLegacy && precision_ != Precision::FP32 && tcKernel_ >= 3 && fused_;
-    // ARNet / ACNet<8> in a tensor-core form: single-channel images of one
+    const bool acn8 = acnet8Quad();
+    const bool tcBatch =
+        ((spec_.family == Family::ACNetLegacy && precision_ != Precision::FP32 && tcKernel_ >= 3) || acn8) && fused_;
+    // ARNet / ACNet<8> B18 in a tensor-core form: single-channel images of one
     // element type run every layer as one launch over all images
-    bool layered = (spec_.family == Family::ARNet || spec_.family == Family::ACNet8) && precision_ != Precision::FP32 && arnetTc_ &&
-                   n > 1 &&
-                   (factor == 2.0 || factor == 4.0);
+    bool layered = (spec_.family == Family::ARNet || spec_.family == Family::ACNet8) && !acn8 &&
+                   precision_ != Precision::FP32 && arnetTc_ && n > 1 && (factor == 2.0 || factor == 4.0);
     for (int i = 0; i < n && layered; i++)
         layered = src[i].c == 1 && src[i].type == src[0].type && dst[i].w == static_cast<int>(factor) * src[i].w &&
                   dst[i].h == static_cast<int>(factor) * src[i].h;
@@ -1094,6 +1110,12 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
             mix(static_cast<uint64_t>(quad));
             const int ctas = tc3Ctas_ > 0 ? tc3Ctas_ : smCount_;
             auto launchGroup = [&]() {
+                if (acn8)
+                {
+                    const ModelParams& mp = model_params(spec_);
+                    return launch_acnet8_tc4(mp.biases.data(), mp.alphas.data(), spec_.blocks, w, bf16, m, in, out, php,
+                                             counter, ctas, s, plan.perSm);
+                }
                 return quad ? launch_acnet_legacy_tc4(*acnet_, w, bf16, m, in, out, php, counter, ctas, s, plan.perSm)
                             : launch_acnet_legacy_tc3(*acnet_, w, bf16, m, in, out, php, counter, ctas, s, plan.shape,
                                                       plan.perSm);

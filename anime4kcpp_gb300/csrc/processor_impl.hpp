@@ -137,6 +137,12 @@ private:
     // quad kernel.
     const void* tcWeights(Precision p, int form);
     const void* arnetWeights(bool bf16);  // packed 8->8 layers of the ARNet / ACNet<8> tensor-core forms
+    // ACNet<8> B4 / B8 in a tensor-core form run the quad kernel (fused colour path, batching)
+    bool acnet8Quad() const
+    {
+        return spec_.family == Family::ACNet8 && precision_ != Precision::FP32 && arnetTc_ && tcKernel_ == 4 &&
+               acnet8_tc4_supported(spec_.blocks);
+    }
     // Tile shape and CTAs per SM for a persistent launch over these images:
     // forced by AC_GB300_TC3_SHAPE / AC_GB300_TC3_PER_SM, else measured once
     // per batch class (element type, channels, form, log2 of the total and

@@ -3,10 +3,15 @@ on the GPU against the oracle (GPU required).
 
 Tolerances: the plain FP32 form holds the ACNetLegacy gate (integer outputs
 never more than 1 LSB from the reference CPU processor; f32 within 1e-4).
-The tensor-core forms (FP16 / BF16 8->8 layers, FP32 head and upscale, 16-bit
-maps between layers): FP16 PSNR >= 50 dB against the FP64 oracle and u8 within
+The tensor-core forms (B4 / B8: every layer in the persistent quad kernel,
+layer 0 and the tail with split 16-bit weights, activations in 16 bits inside
+the tile; B18: two layers per launch, FP32 head and upscale, 16-bit maps
+between launches): FP16 PSNR >= 50 dB against the FP64 oracle and u8 within
 2 LSB of the reference CPU output (>= 99 % of pixels within 1); BF16 PSNR >=
-40 dB and within 8 LSB; f32 outputs within 2e-3 (FP16) / 2e-2 (BF16).
+40 dB and within 8 LSB; f32 outputs within 2e-3 (FP16) / 2e-2 (BF16).  RGB(A)
+through the fused colour path: the ACNetLegacy FP16 RGB gate, within 6 LSB and
+>= 99 % of values within 1 (RGBA un-premultiplies by alpha, which scales a
+1-LSB luma difference up where alpha is small).
 """
 import numpy as np
 import pytest
@@ -114,3 +119,70 @@ def test_acnet8_tc_and_fp32_forms_close(monkeypatch):
     monkeypatch.setenv("AC_GB300_ARNET_TC", "0")
     fp32 = run("acnet-f8b18", x, 2.0, "fp16")  # FP16 requested, tensor-core form disabled: the FP32 pipeline
     assert np.abs(tc.astype(int) - fp32.astype(int)).max() <= 2
+
+
+@pytest.mark.parametrize("model", ["acnet-f8b4-hdn", "acnet-f8b8"])
+@pytest.mark.parametrize("c", [3, 4])
+@pytest.mark.parametrize("dtype", ["uint8", "uint16", "float32"])
+def test_acnet8_quad_rgb_vs_oracle(model, c, dtype):
+    """B4 / B8 RGB(A) x2: split, every CNN layer, chroma resample and merge in
+    the one persistent quad kernel, against the reference CPU pipeline."""
+    x = synthetic.rgb_u8(53, 101, seed=21, alpha=(c == 4))
+    if dtype == "uint16":
+        x = (x.astype(np.uint16) * 257).astype(np.uint16)
+    elif dtype == "float32":
+        x = (x.astype(np.float32) / 255.0).astype(np.float32)
+    got = run(model, x, 2.0, "fp16")
+    want = oracle.process(x, 2.0, model)
+    assert got.shape == want.shape
+    if dtype == "float32":
+        assert np.abs(got - want).max() <= 3e-3
+        return
+    lsb = 1 if dtype == "uint8" else 257
+    d = np.abs(got.astype(np.int64) - want.astype(np.int64))
+    assert d.max() <= 6 * lsb and (d <= lsb).mean() >= 0.99, (d.max(), (d <= lsb).mean())
+
+
+@pytest.mark.parametrize("c", [3, 4])
+@pytest.mark.parametrize("form", ["fp16", "bf16"])
+def test_acnet8_quad_fused_colour_matches_unfused(c, form, monkeypatch):
+    """The fused RGB(A) kernel equals split + quad luma kernel + merge bit for bit."""
+    x = synthetic.rgb_u8(61, 83, seed=5, alpha=(c == 4))
+    outs = []
+    for fused in ("1", "0"):
+        monkeypatch.setenv("AC_GB300_FUSED", fused)
+        p = ac.Processor("cuda", 0, "acnet-f8b8-hdn", precision=form)
+        outs.append(p.process(x, 2.0))
+        assert p.ok(), p.error()
+    assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("model", ["acnet-f8b4", "acnet-f8b8-box-hdn"])
+@pytest.mark.parametrize("c", [1, 3])
+def test_acnet8_quad_batch_equals_single(model, c):
+    """One launch over a batch of uneven images gives each image the bytes of
+    its own launch (direct launch, graph capture, graph replay)."""
+    import torch
+    sizes = [(37, 53), (64, 64), (95, 140), (1, 7), (44, 44), (47, 93)]
+    imgs = [synthetic.luma(h, w, np.uint8, seed=h + w) if c == 1 else synthetic.rgb_u8(h, w, seed=h + w) for h, w in sizes]
+    p = ac.Processor("cuda", 0, model, precision="fp16")
+    singles = [p.process(x, 2.0) for x in imgs]
+    assert p.ok(), p.error()
+    srcs = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in imgs]
+    dsts = [torch.empty((2 * x.shape[0], 2 * x.shape[1]) + x.shape[2:], dtype=torch.uint8, device="cuda") for x in imgs]
+    for _ in range(3):
+        p.process_batch_device(srcs, dsts, 2.0)
+        assert p.ok(), p.error()
+        for d, want in zip(dsts, singles):
+            assert np.array_equal(d.cpu().numpy(), want)
+
+
+def test_acnet8_quad_close_to_layer_pair_form(monkeypatch):
+    """B8 through the quad kernel and through the two-layers-per-launch form
+    (AC_GB300_TC_KERNEL=3 keeps ACNet<8> on the latter) agree within the
+    tensor-core tolerance."""
+    x = synthetic.luma(90, 160, np.uint8, seed=2)
+    quad = run("acnet-f8b8-hdn", x, 2.0, "fp16")
+    monkeypatch.setenv("AC_GB300_TC_KERNEL", "3")
+    pair = run("acnet-f8b8-hdn", x, 2.0, "fp16")
+    assert np.abs(quad.astype(int) - pair.astype(int)).max() <= 2
