@@ -144,6 +144,35 @@ __device__ __forceinline__ uint4 pack8_plain(const float* v)
                           tc::pack_f16x2(v[6], v[7]));
 }
 
+// PReLU on the packed 16-bit pairs: fma(a, min(x, 0), max(x, 0)) per lane
+// of each pair (slopes rounded to 16 bits), four instructions per two values.
+template <bool BF16>
+__device__ __forceinline__ uint4 pack8_prelu(const float* v, const float* a)
+{
+    uint32_t r[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+    {
+        if constexpr (BF16)
+        {
+            const __nv_bfloat162 x = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+            const __nv_bfloat162 s = __floats2bfloat162_rn(a[2 * i], a[2 * i + 1]);
+            const __nv_bfloat162 z = __float2bfloat162_rn(0.0f);
+            const __nv_bfloat162 y = __hfma2(s, __hmin2(x, z), __hmax2(x, z));
+            r[i] = *reinterpret_cast<const uint32_t*>(&y);
+        }
+        else
+        {
+            const __half2 x = __floats2half2_rn(v[2 * i], v[2 * i + 1]);
+            const __half2 s = __floats2half2_rn(a[2 * i], a[2 * i + 1]);
+            const __half2 z = __float2half2_rn(0.0f);
+            const __half2 y = __hfma2(s, __hmin2(x, z), __hmax2(x, z));
+            r[i] = *reinterpret_cast<const uint32_t*>(&y);
+        }
+    }
+    return make_uint4(r[0], r[1], r[2], r[3]);
+}
+
 template <bool BF16>
 __device__ __forceinline__ uint4 pack8(const float* v)
 {
@@ -512,16 +541,7 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
                                 {
                                     uint4 val;
                                     if constexpr (NET::ACN8)
-                                    {
-                                        float a8[8];
-#pragma unroll
-                                        for (int c = 0; c < 8; c++)
-                                        {
-                                            const float u = v[8 * kk + c];
-                                            a8[c] = fmaxf(u, 0.0f) + P.alpha[l][c] * fminf(u, 0.0f);
-                                        }
-                                        val = pack8_plain<BF16>(a8);
-                                    }
+                                        val = pack8_prelu<BF16>(v + 8 * kk, P.alpha[l]);
                                     else
                                         val = pack8<BF16>(v + 8 * kk);
                                     *slot<G>(act, p) = val;

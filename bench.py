@@ -27,6 +27,9 @@ Voronoi-edge images (no public dataset is attached to this workload).
   families  every network family of the reference on 1920x1080 u8 luma x2
          (device-resident, one launch sequence per frame): the tensor-core
          form where the family has one, and the plain FP32 form
+  cli_default  the reference CLI's default model (ACNet<8> B8 HDN) on the
+         headline's frames (8 RGB u8 1080p frames x2 per step, device
+         resident): FP16 as one fused launch per step, FP32 frame by frame
   serve  the serving workload: Poisson arrivals (200 jobs/s) of mixed sizes,
          factors, models and formats through the serving loop; p50/p99
          latency and output Mpx/s, FP16 against FP32
@@ -433,6 +436,47 @@ def time_families(ac, torch, args):
     return out
 
 
+CLI_MODEL = "acnet-f8b8-hdn"  # the reference CLI's default model
+
+
+def time_cli_default(ac, torch, args):
+    """ACNet<8> B8 HDN on 8 RGB u8 1920x1080 frames x2 per step, inputs
+    resident in HBM, CUDA events on the launching stream.  FP16: the batch
+    entry point, one persistent launch per step (split, CNN, chroma resample
+    and merge fused); FP32: the per-layer FP32 pipeline frame by frame."""
+    frames = make_frames(8, seed=200)
+    srcs = [torch.from_numpy(f).cuda() for f in frames]
+    dsts = [torch.empty((OH, OW, 3), dtype=torch.uint8, device="cuda") for _ in frames]
+    stream = torch.cuda.Stream()
+    h = stream.cuda_stream
+    out = {"workload": "%s, 8 x 1920x1080 RGB u8 -> 3840x2160 per step" % CLI_MODEL}
+    for form, steps in (("fp16", max(3, args.cli_steps)), ("fp32", max(3, args.cli_steps // 2))):
+        p = ac.Processor("cuda", 0, CLI_MODEL, precision=form)
+
+        def step():
+            if form == "fp32":
+                for a, b in zip(srcs, dsts):
+                    p.process_device(a, b, 2.0, stream=h, sync=False)
+            else:
+                p.process_batch_device(srcs, dsts, 2.0, stream=h, sync=False)
+
+        for _ in range(3):
+            step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if not p.ok():
+            raise RuntimeError(p.error())
+        ms = e0.elapsed_time(e1) / steps
+        out[form] = {"ms_per_step": round(ms, 4), "value": 8 * OW * OH / (ms / 1e3) / 1e6, "unit": "Mpx/s"}
+    out["fp16_over_fp32"] = out["fp16"]["value"] / out["fp32"]["value"]
+    return out
+
+
 SERVE_RES = [(480, 854), (720, 1280), (1080, 1920), (2160, 3840)]
 SERVE_RES_W = [1, 2, 2, 1]
 SERVE_MODELS = ["acnet-legacy-hdn0", "acnet-legacy-hdn1", "acnet-legacy-hdn2", "acnet-legacy-hdn3", "arnet-b8"]
@@ -715,6 +759,8 @@ def run_gb300(args, rank, world, local_rank):
         out["video"] = time_video(ac, torch, args)
     if rank == 0 and world == 1 and args.family_steps > 0:
         out["families"] = time_families(ac, torch, args)
+    if rank == 0 and world == 1 and args.cli_steps > 0:
+        out["cli_default"] = time_cli_default(ac, torch, args)
     if rank == 0 and world == 1 and args.serve_seconds > 0:
         out["serve"] = time_serve(ac, torch, args)
         out["serve"]["saturation"] = time_serve_saturation(ac, torch, args)
@@ -739,6 +785,7 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=12)
     ap.add_argument("--video-steps", type=int, default=4, help="8-frame steps of the video workload (0: skip)")
     ap.add_argument("--family-steps", type=int, default=10, help="frames per family and form in the families workload (0: skip)")
+    ap.add_argument("--cli-steps", type=int, default=10, help="steps of the CLI-default-model workload (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="serving workload length per form (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="serving workload arrival rate, jobs/s")
     ap.add_argument("--saturation-rate", type=float, default=4000.0, help="offered rate of the saturation run, jobs/s")
