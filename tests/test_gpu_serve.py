@@ -122,3 +122,23 @@ def test_malformed_jobs_are_rejected():
     r = srv.wait(t)
     assert r["status"] == -2 and "differ" in r["error"]
     srv.close()
+
+
+def test_cli_default_model_jobs_batched():
+    """Jobs of the reference CLI's default model (ACNet<8> B8 HDN, RGB) and of
+    ACNet<8> B4 (gray), submitted together: the server batches them through
+    the quad kernel, and each gets the ordinary processor's bytes."""
+    srv = ac.Server(0, "fp16", hbm_budget_gb=4.0, workers=2)
+    jobs = [("acnet-f8b8-hdn", synthetic.rgb_u8(90 + 7 * i, 130 + 11 * i, seed=30 + i)) for i in range(5)]
+    jobs.append(("acnet-f8b4", synthetic.luma(70, 90, np.uint8, seed=9)))
+    outs, tickets = [], []
+    for model, x in jobs:
+        o = np.zeros((2 * x.shape[0], 2 * x.shape[1]) + x.shape[2:], np.uint8)
+        outs.append(o)
+        tickets.append(srv.submit(x, o, model, 2.0))
+    for t in tickets:
+        r = srv.wait(t)
+        assert r["status"] == 0, r["error"]
+    srv.close()
+    for (model, x), o in zip(jobs, outs):
+        assert np.array_equal(o, ac.Processor("cuda", 0, model, precision="fp16").process(x, 2.0)), model
