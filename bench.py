@@ -203,6 +203,33 @@ def run_reference(args, rank):
     }
 
 
+def rank_barrier():
+    """Barrier over the ranks of the process group (nothing on one rank)."""
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.barrier()
+
+
+def max_over_ranks(x):
+    """The largest x over the ranks (x itself on one rank).  The reduction
+    tensor lives where the backend wants it: on the GPU for NCCL, on the host
+    for gloo."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_mpx(px_per_rank, seconds, world):
+    """Whole-job output Mpx/s of `world` replicas that each produced
+    px_per_rank pixels, the slowest in `seconds` (weak scaling)."""
+    return px_per_rank * world / seconds / 1e6
+
+
 def time_device(ac, torch, proc, srcs, dsts, frames, steps, warmup, profile=False, clocks=None, batched=False):
     # A dedicated stream: the kernels and the timing events share it.
     stream = torch.cuda.Stream()
@@ -227,12 +254,14 @@ def time_device(ac, torch, proc, srcs, dsts, frames, steps, warmup, profile=Fals
     launches0 = ac.launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ctx = clocks if clocks is not None else _Null()
+    rank_barrier()  # every rank starts its timed steps together
     with ctx:
         e0.record(stream)
         for i in range(steps):
             step(i)
         e1.record(stream)
         torch.cuda.synchronize()
+        rank_barrier()
         if clocks is not None:
             time.sleep(0.05)
     ms = e0.elapsed_time(e1)
@@ -282,10 +311,12 @@ def time_e2e(ac, torch, proc, frames_host, outs_host, frames, steps, warmup, thr
 
         ts = [threading.Thread(target=worker) for _ in range(threads)]
         [t.start() for t in ts]
+        rank_barrier()
         t0 = time.perf_counter()
         go.set()
         [t.join() for t in ts]
         el = time.perf_counter() - t0
+        rank_barrier()
         if errs:
             raise RuntimeError(errs[0])
         return el
@@ -692,11 +723,8 @@ def run_gb300(args, rank, world, local_rank):
 
     # max over ranks of the headline time
     if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([rec["ms_per_step"]], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        rec["ms_per_step"] = float(t.item())
-        rec["value"] = OW * OH * frames * world / (rec["ms_per_step"] / 1e3) / 1e6
+        rec["ms_per_step"] = max_over_ranks(rec["ms_per_step"])
+        rec["value"] = replica_mpx(OW * OH * frames, rec["ms_per_step"] / 1e3, world)
 
     # end to end through the C ABI with pinned host buffers
     pin_src = [torch.from_numpy(f).pin_memory() for f in host]
@@ -704,12 +732,7 @@ def run_gb300(args, rank, world, local_rank):
     e2e_steps = max(2, args.steps // 2)
     el = time_e2e(ac, torch, proc, [p.numpy() for p in pin_src], [p.numpy() for p in pin_dst], frames, e2e_steps,
                   max(1, args.warmup // 2), args.e2e_threads)
-    e2e_value = OW * OH * frames * e2e_steps / el / 1e6
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([el], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_value = OW * OH * frames * e2e_steps * world / float(t.item()) / 1e6
+    e2e_value = replica_mpx(OW * OH * frames * e2e_steps, max_over_ranks(el), world)
 
     peaks = measured_peaks()
     kernel_s = rec["kernel_ms_per_launch"] / 1e3
