@@ -48,12 +48,18 @@ bool encode_tmap_2d(CUtensorMap* map, const void* base, int elem_bytes, int dim_
 
 bool encode_tmap_3d_u16(CUtensorMap* map, const void* base, int d0, int d1, int d2, int b0, int b1, int b2)
 {
+    return encode_tmap_3d_u16_strided(map, base, d0, d1, d2, b0, b1, b2, 1);
+}
+
+bool encode_tmap_3d_u16_strided(CUtensorMap* map, const void* base, int d0, int d1, int d2, int b0, int b1, int b2, int s1)
+{
     auto fn = encoder();
     if (!fn || (reinterpret_cast<uintptr_t>(base) & 15u) != 0 || (d0 * 2) % 16 != 0 || (b0 * 2) % 16 != 0) return false;
     cuuint64_t dims[3] = {static_cast<cuuint64_t>(d0), static_cast<cuuint64_t>(d1), static_cast<cuuint64_t>(d2)};
     cuuint64_t strides[2] = {static_cast<cuuint64_t>(d0) * 2, static_cast<cuuint64_t>(d0) * d1 * 2};
     cuuint32_t box[3] = {static_cast<cuuint32_t>(b0), static_cast<cuuint32_t>(b1), static_cast<cuuint32_t>(b2)};
-    cuuint32_t estr[3] = {1, 1, 1};
+    if (s1 < 1 || s1 > 8) return false;
+    cuuint32_t estr[3] = {1, static_cast<cuuint32_t>(s1), 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, const_cast<void*>(base), dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);

@@ -22,5 +22,8 @@ bool encode_tmap_2d(CUtensorMap* map, const void* base, int elem_bytes, int dim_
 // (d0 * 2 a multiple of 16 bytes); box of b0 x b1 x b2 elements (b0 * 2 a
 // multiple of 16), no swizzle, out-of-bounds elements read as zero.
 bool encode_tmap_3d_u16(CUtensorMap* map, const void* base, int d0, int d1, int d2, int b0, int b1, int b2);
+// The same with a traversal stride s1 along dimension 1: a load starting at
+// x fetches elements x, x + s1, ... (ceil(b1 / s1) of them) along it.
+bool encode_tmap_3d_u16_strided(CUtensorMap* map, const void* base, int d0, int d1, int d2, int b0, int b1, int b2, int s1);
 
 }  // namespace acgb

@@ -3,7 +3,8 @@ GPU against the oracle (GPU required).
 
 Plain FP32 form: integer outputs never more than 1 LSB from the reference CPU
 processor, f32 outputs within 1e-4.  Tensor-core form (ArtCNN<16/32>,
-FSRCNNX<16>; FP16/BF16 3x3 layers, FP32 head and upscale, 16-bit maps): FP16
+FSRCNNX<16>; FP16/BF16 3x3 layers, the upscale with split 16-bit weights, FP32
+head, 16-bit maps between layers): FP16
 u8 outputs within 2 LSB on >= 99 % of pixels and never more than 6 LSB off,
 f32 within 5e-3; BF16 within 16 LSB, f32 within 3e-2.  FSRCNNX<8> runs the
 FP32 pipeline in every form.
