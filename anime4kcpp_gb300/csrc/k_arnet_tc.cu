@@ -56,6 +56,7 @@ enum Mode
     kPReLU = 0,     // prelu(conv + b)
     kResidual = 1,  // 0.2 * (conv + b) + skip
     kTail = 2,      // prelu(1x1(0.2 * (conv + b) + skip) + b1) + feat
+    kFsrTail = 3,   // FSRCNNX<8>'s last layer: prelu(1x1(prelu(conv + b)) + b1 + feat)
 };
 
 constexpr int kMaxImg = 16;  // images per launch (the frames of a batch)
@@ -444,6 +445,25 @@ __global__ void __launch_bounds__(THREADS, 4) conv2_kernel(const __grid_constant
 #pragma unroll
                         for (int c = 0; c < 8; c++) sv[c] = prelu(sv[c], P.a[c]);
                     }
+                    else if constexpr (MODE == kFsrTail)
+                    {
+                        // conv3x3 + PReLU, conv1x1 8->8 + bias + feat, PReLU
+                        // (CPUProcessor.cpp:1629-1715 order, as k_f3_fp32.cu's tail)
+                        float f[8], t[8];
+                        unpack8<BF16>(I.feat[o], f);
+#pragma unroll
+                        for (int c = 0; c < 8; c++) sv[c] = prelu(sv[c], P.a[c]);
+#pragma unroll
+                        for (int n = 0; n < 8; n++)
+                        {
+                            float u = P.b1[n];
+#pragma unroll
+                            for (int c = 0; c < 8; c++) u = fmaf(sv[c], P.k1[n * 8 + c], u);
+                            t[n] = prelu(u + f[n], P.a1[n]);
+                        }
+#pragma unroll
+                        for (int n = 0; n < 8; n++) sv[n] = t[n];
+                    }
                     else
                     {
                         float sk[8];
@@ -519,6 +539,7 @@ struct UpParams
 {
     float k[288];
     float b[4];
+    int no_nearest;  // FSRCNNX<8>: no nearest-input add
     const uint4* map[kMaxImg];  // image blockIdx.z
     Plane src[kMaxImg], dst[kMaxImg];
 };
@@ -548,7 +569,7 @@ __global__ void __launch_bounds__(256) up_kernel(const __grid_constant__ UpParam
 #pragma unroll
             for (int c = 0; c < 8; c++) acc[n] = fmaf(xv[c], U.k[n * 72 + p * 8 + c], acc[n]);
     }
-    const float near = to_float<T>(row_ptr<T>(src.ptr, src.pitch, y)[x]);
+    const float near = U.no_nearest ? 0.0f : to_float<T>(row_ptr<T>(src.ptr, src.pitch, y)[x]);
 #pragma unroll
     for (int n = 0; n < 4; n++) row_ptr_w<T>(dst.ptr, dst.pitch, 2 * y + (n >> 1))[2 * x + (n & 1)] = from_float<T>(acc[n] + near);
 }
@@ -879,6 +900,86 @@ cudaError_t launch_acnet8_tc(const float* kernels, const float* biases, const fl
 {
     if (in.w <= 0 || in.h <= 0) return cudaSuccess;
     return launch_acnet8_tc_batch(kernels, biases, alphas, blocks, packed, bf16, 1, &in, &out, maps, status, stream);
+}
+
+// FSRCNNX<8> (B4) x2 in the tensor-core form: the 5x5 head in FP32
+// (launch_f3_head8), layers 1 + 2 and 3 + the tail as two two-layer launches
+// (the tail: PReLU, conv1x1 8->8 + feat, PReLU), the upscale conv3x3 8->4 +
+// pixel shuffle in FP32 without the nearest-input add.  Parameters in the
+// reference layout (FSRCNNX.hpp:28-66): kernels head 200, 4 x 576, 1x1 64,
+// upscale 288; biases 8 per layer (head, 4 convs, 1x1) then 4; PReLU slopes
+// 8 per layer (4 convs, then the one after the 1x1).  packed: the 4 layers'
+// pack_pair_conv8 output; maps: three [h][w] arrays of 16-byte pixels.
+cudaError_t launch_fsrcnnx8_tc(const float* kernels, const float* biases, const float* alphas, const void* packed, bool bf16,
+                               const Plane& in, const Plane& out, void* const maps[3], int* status, cudaStream_t stream)
+{
+    using namespace arnettc;
+    if (in.w <= 0 || in.h <= 0) return cudaSuccess;
+    if (!packed || !status || !maps) return cudaErrorInvalidValue;
+    if (in.channels != 1 || out.channels != 1 || out.w != 2 * in.w || out.h != 2 * in.h) return cudaErrorInvalidValue;
+    cudaError_t err = launch_f3_head8(kernels, biases, bf16, in, maps[0], stream);
+    if (err != cudaSuccess) return err;
+    count_launch();
+    Conv2Params c2;
+    std::memset(&c2, 0, sizeof(c2));
+    ConvImg& I = c2.img[0];
+    I.w = in.w;
+    I.h = in.h;
+    I.tiles_x = (in.w + TW2 - 1) / TW2;
+    I.tile0 = 0;
+    I.feat = static_cast<const uint4*>(maps[0]);
+    const int tiles2 = I.tiles_x * ((in.h + TH2 - 1) / TH2);
+    c2.nimg = 1;
+    c2.status = status;
+    const uint4* pk = static_cast<const uint4*>(packed);
+    // layers 1 and 2 (PReLU)
+    {
+        Conv2Params q = c2;
+        q.img[0].in = static_cast<const uint4*>(maps[0]);
+        q.img[0].out = static_cast<uint4*>(maps[1]);
+        q.bwA = pk;
+        q.bwB = pk + (B_BYTES / 16);
+        for (int i = 0; i < 8; i++)
+        {
+            q.bA[i] = biases[8 + i];
+            q.aA[i] = alphas[i];
+            q.b[i] = biases[16 + i];
+            q.a[i] = alphas[8 + i];
+        }
+        err = bf16 ? launch_conv2<kPReLU, true>(q, tiles2, stream) : launch_conv2<kPReLU, false>(q, tiles2, stream);
+        if (err != cudaSuccess) return err;
+        count_launch();
+    }
+    // layer 3 (PReLU) and the tail
+    {
+        Conv2Params q = c2;
+        q.img[0].in = static_cast<const uint4*>(maps[1]);
+        q.img[0].out = static_cast<uint4*>(maps[2]);
+        q.bwA = pk + 2 * (B_BYTES / 16);
+        q.bwB = pk + 3 * (B_BYTES / 16);
+        for (int i = 0; i < 8; i++)
+        {
+            q.bA[i] = biases[24 + i];
+            q.aA[i] = alphas[16 + i];
+            q.b[i] = biases[32 + i];
+            q.a[i] = alphas[24 + i];
+            q.b1[i] = biases[40 + i];
+            q.a1[i] = alphas[32 + i];
+        }
+        for (int i = 0; i < 64; i++) q.k1[i] = kernels[200 + 4 * 576 + i];
+        err = bf16 ? launch_conv2<kFsrTail, true>(q, tiles2, stream) : launch_conv2<kFsrTail, false>(q, tiles2, stream);
+        if (err != cudaSuccess) return err;
+        count_launch();
+    }
+    UpParams u;
+    std::memset(&u, 0, sizeof(u));
+    for (int i = 0; i < 288; i++) u.k[i] = kernels[200 + 4 * 576 + 64 + i];
+    for (int i = 0; i < 4; i++) u.b[i] = biases[48 + i];
+    u.no_nearest = 1;
+    u.map[0] = static_cast<const uint4*>(maps[2]);
+    u.src[0] = in;
+    u.dst[0] = out;
+    return launch_up(u, bf16, 1, stream);
 }
 
 }  // namespace acgb

@@ -686,6 +686,36 @@ void pack_f3_tc_weights(const float* kernels, int F, bool artcnn, int blocks, bo
     f3tc::pack_f3_pair(up, F, true, bf16, packed.data() + layers * lb);
 }
 
+// FSRCNNX<8>'s conv5x5 1->8 head (identity) in FP32 into an 8-channel 16-bit
+// map [h][w] x 16 bytes.
+cudaError_t launch_f3_head8(const float* kernels, const float* biases, bool bf16, const Plane& in, void* feat, cudaStream_t stream)
+{
+    using namespace f3tc;
+    if (in.w <= 0 || in.h <= 0) return cudaSuccess;
+    HeadP<5, 8> hp;
+    for (int i = 0; i < 8 * 25; i++) hp.k[i] = kernels[i];
+    for (int i = 0; i < 8; i++) hp.b[i] = biases[i];
+    const dim3 grid((in.w + 31) / 32, (in.h + 7) / 8);
+    uint4* f = static_cast<uint4*>(feat);
+    switch (in.type)
+    {
+    case kU8:
+        bf16 ? head_kernel<uint8_t, 5, 8, true><<<grid, 256, 0, stream>>>(hp, in, f)
+             : head_kernel<uint8_t, 5, 8, false><<<grid, 256, 0, stream>>>(hp, in, f);
+        break;
+    case kU16:
+        bf16 ? head_kernel<uint16_t, 5, 8, true><<<grid, 256, 0, stream>>>(hp, in, f)
+             : head_kernel<uint16_t, 5, 8, false><<<grid, 256, 0, stream>>>(hp, in, f);
+        break;
+    case kF32:
+        bf16 ? head_kernel<float, 5, 8, true><<<grid, 256, 0, stream>>>(hp, in, f)
+             : head_kernel<float, 5, 8, false><<<grid, 256, 0, stream>>>(hp, in, f);
+        break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launch_f3_tc(const float* kernels, const float* biases, const float* alphas, bool artcnn, int F, int blocks,
                          const void* packed, bool bf16, const Plane& in, const Plane& out, void* const maps[3], int* status,
                          cudaStream_t stream)

@@ -495,6 +495,28 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
         const ModelParams& mp = model_params(spec_);
         err = launch_arnet_fp32(mp.kernels.data(), mp.biases.data(), mp.alphas.data(), spec_.blocks, in, out, maps, stream);
     }
+    else if (spec_.family == Family::FSRCNNX && spec_.channels == 8 && spec_.blocks == 4 && precision_ != Precision::FP32 &&
+             arnetTc_)
+    {
+        // FSRCNNX<8>: the 8->8 layers on the two-layer tcgen05 conv, 16-bit maps
+        const bool bf16 = precision_ == Precision::BF16;
+        const void* w = arnetWeights(bf16);
+        const size_t bytes = static_cast<size_t>(in.w) * in.h * 16;
+        void* maps[3];
+        err = w ? cudaSuccess : cudaErrorMemoryAllocation;
+        for (int i = 0; i < 3 && err == cudaSuccess; i++)
+        {
+            err = ts.maps[i].ensure(bytes);
+            maps[i] = ts.maps[i].ptr;
+        }
+        int* status = tc_status_buffer();
+        if (err == cudaSuccess && !status) err = cudaErrorMemoryAllocation;
+        if (err == cudaSuccess)
+        {
+            const ModelParams& mp = model_params(spec_);
+            err = launch_fsrcnnx8_tc(mp.kernels.data(), mp.biases.data(), mp.alphas.data(), w, bf16, in, out, maps, status, stream);
+        }
+    }
     else if ((spec_.family == Family::ArtCNN || (spec_.family == Family::FSRCNNX && spec_.channels == 16)) &&
              precision_ != Precision::FP32 && arnetTc_)
     {
@@ -521,7 +543,7 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
     }
     else if (spec_.family == Family::ArtCNN || spec_.family == Family::FSRCNNX)
     {
-        // the plain FP32 layer pipeline (FP32 form; FSRCNNX<8> in every form)
+        // the plain FP32 layer pipeline (FP32 form)
         const size_t bytes = static_cast<size_t>(in.w) * in.h * spec_.channels * sizeof(float);
         float* maps[3];
         for (int i = 0; i < 3; i++)
@@ -667,6 +689,20 @@ const void* GB300Processor::arnetWeights(bool bf16)
     if (!d.ptr)
     {
         const ModelParams& mp = model_params(spec_);
+        if (spec_.family == Family::FSRCNNX && spec_.channels == 8)
+        {
+            // FSRCNNX<8>: its four 3x3 8->8 layers (after the 5x5 head's 200 weights)
+            std::vector<uint16_t> packed(static_cast<size_t>(spec_.blocks) * 1536);
+            for (int l = 0; l < spec_.blocks; l++)
+                pack_pair_conv8(mp.kernels.data() + 200 + 576 * l, bf16, packed.data() + static_cast<size_t>(l) * 1536);
+            if (d.ensure(packed.size() * sizeof(uint16_t)) != cudaSuccess) return nullptr;
+            if (cudaMemcpy(d.ptr, packed.data(), packed.size() * sizeof(uint16_t), cudaMemcpyHostToDevice) != cudaSuccess)
+            {
+                d.release();
+                return nullptr;
+            }
+            return d.ptr;
+        }
         if (spec_.family == Family::ArtCNN || spec_.family == Family::FSRCNNX)
         {
             // the 3x3 F->F layers of the wide families

@@ -428,7 +428,7 @@ def time_video(ac, torch, args):
 
 
 FAMILIES = [("acnet-legacy-hdn0", True), ("acnet-f8b8-hdn", True), ("arnet-b8", True), ("artcnn-c4f16", True),
-            ("artcnn-c4f32", True), ("fsrcnnx-f8", False), ("fsrcnnx-f16", True)]
+            ("artcnn-c4f32", True), ("fsrcnnx-f8", True), ("fsrcnnx-f16", True)]
 
 
 def time_families(ac, torch, args):
