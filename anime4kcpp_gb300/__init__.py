@@ -78,7 +78,7 @@ EXPORTS = (
     "ac_processor_type_name", "ac_processor_info", "ac_processor_list_info",
     "ac_gb300_set_precision", "ac_gb300_get_precision", "ac_gb300_output_shape", "ac_gb300_process_device",
     "ac_gb300_launch_count", "ac_gb300_model_params", "ac_gb300_profile_enable", "ac_gb300_profile_collect",
-    "ac_gb300_tc_selftest", "ac_gb300_process_device_noalloc", "ac_gb300_process_batch_device",
+    "ac_gb300_tc_selftest", "ac_gb300_wait_selftest", "ac_gb300_process_device_noalloc", "ac_gb300_process_batch_device",
     "ac_gb300_graph_replays", "ac_gb300_process_yuv_device",
     "ac_gb300_server_create", "ac_gb300_server_error", "ac_gb300_server_submit", "ac_gb300_server_wait",
     "ac_gb300_server_stats", "ac_gb300_server_destroy",
@@ -131,6 +131,7 @@ def native():
             "ac_gb300_profile_enable": (I, [pproc, I]),
             "ac_gb300_profile_collect": (I, [pproc, P(D), P(I), P(D)]),
             "ac_gb300_tc_selftest": (I, [V, I, V, I, I, I, V]),
+            "ac_gb300_wait_selftest": (I, [I, P(ctypes.c_int), P(ctypes.c_double)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -445,6 +446,13 @@ def tc_selftest(x, b, shift, bf16=False):
     rc = native().ac_gb300_tc_selftest(x.ctypes.data, x.shape[0], b.ctypes.data, b.shape[1], int(shift), 1 if bf16 else 0,
                                        d.ctypes.data)
     return rc, d
+
+
+def wait_selftest(limit_ms=50):
+    """The kernels' bounded wait on a phase nothing completes: (rc, status, elapsed_ms)."""
+    st, el = ctypes.c_int(0), ctypes.c_double(0.0)
+    rc = native().ac_gb300_wait_selftest(int(limit_ms), ctypes.byref(st), ctypes.byref(el))
+    return rc, st.value, el.value
 
 
 def launch_count():

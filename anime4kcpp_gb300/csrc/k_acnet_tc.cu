@@ -327,11 +327,26 @@ void pack_acnet_tc_weights(const AcnetLegacyWeights& w, bool bf16, std::vector<u
 }
 
 // Device word that a tensor-core kernel sets when a bounded wait gave up.
+// The calling host thread's status word of the tensor-core kernels (0, or 1
+// after a timed-out wait): one per thread, as the reference keeps error state
+// per calling thread (CUDAProcessor.cpp:284), so one thread's reset never
+// clears or reports another thread's timeout.
+namespace {
+struct StatusWord
+{
+    int* p = nullptr;
+    ~StatusWord()
+    {
+        if (p) cudaFree(p);
+    }
+};
+}  // namespace
+
 int* tc_status_buffer()
 {
-    static int* p = nullptr;
-    if (!p && cudaMalloc(&p, sizeof(int)) == cudaSuccess) cudaMemset(p, 0, sizeof(int));
-    return p;
+    static thread_local StatusWord w;
+    if (!w.p && cudaMalloc(&w.p, sizeof(int)) == cudaSuccess) cudaMemset(w.p, 0, sizeof(int));
+    return w.p;
 }
 
 cudaError_t launch_acnet_legacy_tc(const AcnetLegacyWeights& wts, const void* packed, bool bf16, const Plane& in,

@@ -140,3 +140,57 @@ done:
     if (ds) cudaFree(ds);
     return rc;
 }
+
+namespace acgb {
+namespace {
+
+// One thread waits, with the tensor-core kernels' bounded wait
+// (tc::mbar_wait_ns), on an mbarrier phase that nothing completes: the wait
+// must give up after `ns` and the kernel must end with status 1 (2 would mean
+// the phase completed).  No asynchronous operation is in flight, so the kernel
+// exits cleanly and the context stays usable.
+__global__ void wait_selftest_kernel(uint64_t ns, int* status, unsigned long long* elapsed)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0)
+    {
+        tc::mbar_init(&bar, 1);
+        tc::fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        const uint64_t t0 = global_timer_ns();
+        const bool done = tc::mbar_wait_ns(&bar, 0, ns);
+        *elapsed = global_timer_ns() - t0;
+        *status = done ? 2 : 1;
+    }
+}
+
+}  // namespace
+}  // namespace acgb
+
+int ac_gb300_wait_selftest(int limit_ms, int* status, double* elapsed_ms)
+{
+    using namespace acgb;
+    if (!status || !elapsed_ms || limit_ms <= 0 || limit_ms > 2000) return -1;
+    int* ds = nullptr;
+    unsigned long long* de = nullptr;
+    int rc = -1;
+    if (cudaMalloc(&ds, sizeof(int)) != cudaSuccess) goto done;
+    if (cudaMalloc(&de, sizeof(unsigned long long)) != cudaSuccess) goto done;
+    cudaMemset(ds, 0, sizeof(int));
+    wait_selftest_kernel<<<1, 32>>>(static_cast<uint64_t>(limit_ms) * 1000000ull, ds, de);
+    if (cudaDeviceSynchronize() != cudaSuccess) goto done;
+    {
+        unsigned long long ns = 0;
+        if (cudaMemcpy(status, ds, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) goto done;
+        if (cudaMemcpy(&ns, de, sizeof(ns), cudaMemcpyDeviceToHost) != cudaSuccess) goto done;
+        *elapsed_ms = static_cast<double>(ns) / 1e6;
+        rc = 0;
+    }
+done:
+    if (ds) cudaFree(ds);
+    if (de) cudaFree(de);
+    return rc;
+}

@@ -123,6 +123,13 @@ AC_C_API int ac_gb300_profile_collect(ACProcessor* processor, double* ms, int* l
  * Returns 0, 1 if the tensor core did not complete within 2 s, -1 on error. */
 AC_C_API int ac_gb300_tc_selftest(const uint16_t* x, int px, const uint16_t* b, int k, int shift, int bf16, float* d);
 
+/* Diagnostic of the failure path: one GPU thread waits, with the kernels'
+ * bounded mbarrier wait limited to limit_ms (1..2000), on a phase that nothing
+ * completes.  *status receives 1 when the wait gave up (the designed outcome;
+ * 2 would mean the phase completed), *elapsed_ms how long it waited.  Returns
+ * 0, or -1 on error. */
+AC_C_API int ac_gb300_wait_selftest(int limit_ms, int* status, double* elapsed_ms);
+
 /* Number of kernels this library has launched in the process so far. */
 AC_C_API uint64_t ac_gb300_launch_count(void);
 
