@@ -261,13 +261,11 @@ __global__ void __launch_bounds__(THREADS, 1) acnet_tc_kernel(const __grid_const
 template <typename T, bool BF16>
 cudaError_t launch_typed(const Params& p, dim3 grid, cudaStream_t stream)
 {
-    static bool configured = false;
-    if (!configured)
-    {
-        cudaError_t err = cudaFuncSetAttribute(acnet_tc_kernel<T, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-        if (err != cudaSuccess) return err;
-        configured = true;
-    }
+    // one-time set-up, thread-safe (a function-local static is initialised once)
+    static const cudaError_t setup =
+        cudaFuncSetAttribute(acnet_tc_kernel<T, BF16>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (setup != cudaSuccess) return setup;
     acnet_tc_kernel<T, BF16><<<grid, THREADS, SMEM_BYTES, stream>>>(p);
     return cudaGetLastError();
 }

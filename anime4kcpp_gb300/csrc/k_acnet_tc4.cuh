@@ -647,32 +647,34 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
 template <class G, class NET, typename T, int C, bool BF16>
 cudaError_t launch_typed(const Params& p, int grid, int per_sm_cap, cudaStream_t stream)
 {
-    static int per_sm = 0;
-    if (per_sm == 0)
-    {
+    // one-time set-up, thread-safe (a function-local static is initialised once)
+    static const LaunchSetup setup = [] {
         cudaError_t err = cudaFuncSetAttribute(acnet_tc4_kernel<G, NET, T, C, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                Layout<G, T, C>::smem);
-        if (err != cudaSuccess) return err;
+        if (err != cudaSuccess) return LaunchSetup{err, 0, 0};
         err = cudaFuncSetAttribute(acnet_tc4_kernel<G, NET, T, C, BF16>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                    cudaSharedmemCarveoutMaxShared);
-        if (err != cudaSuccess) return err;
+        if (err != cudaSuccess) return LaunchSetup{err, 0, 0};
         // CTAs per SM from shared memory, registers and threads (as for the
         // pair kernel: two CTAs of 256 tensor-memory columns share an SM).
         cudaFuncAttributes fa;
         err = cudaFuncGetAttributes(&fa, acnet_tc4_kernel<G, NET, T, C, BF16>);
-        if (err != cudaSuccess) return err;
+        if (err != cudaSuccess) return LaunchSetup{err, 0, 0};
         int dev = 0, smem_sm = 0, reserved = 0, regs_sm = 0;
-        if ((err = cudaGetDevice(&dev)) != cudaSuccess) return err;
+        if ((err = cudaGetDevice(&dev)) != cudaSuccess) return LaunchSetup{err, 0, 0};
         cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
         cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
         cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
         const int regs_cta = (fa.numRegs + 7) / 8 * 8 * THREADS;
         const int need_smem = Layout<G, T, C>::smem + static_cast<int>(fa.sharedSizeBytes) + reserved;
-        per_sm = (2 * need_smem <= smem_sm && 2 * regs_cta <= regs_sm && 2 * TMEM_COLS <= 512) ? 2 : 1;
+        const int per_sm = (2 * need_smem <= smem_sm && 2 * regs_cta <= regs_sm && 2 * TMEM_COLS <= 512) ? 2 : 1;
         if (std::getenv("AC_GB300_DEBUG"))
             std::fprintf(stderr, "tc4 <%d,%d,%d>: %d CTAs per SM, %d bytes shared, %d registers\n", static_cast<int>(sizeof(T)),
                          C, BF16 ? 1 : 0, per_sm, Layout<G, T, C>::smem, fa.numRegs);
-    }
+        return LaunchSetup{cudaSuccess, per_sm, 0};
+    }();
+    if (setup.err != cudaSuccess) return setup.err;
+    const int per_sm = setup.per_sm;
     const int k = per_sm < per_sm_cap ? per_sm : (per_sm_cap < 1 ? 1 : per_sm_cap);
     acnet_tc4_kernel<G, NET, T, C, BF16><<<grid * k, THREADS, Layout<G, T, C>::smem, stream>>>(p);
     return cudaGetLastError();

@@ -551,21 +551,23 @@ template <int F, int MODE, bool BF16, typename OT = uint8_t>
 cudaError_t launch_convq(const ConvPP<F>& p, cudaStream_t stream)
 {
     using G = GeoQ<F>;
-    static int per_sm = 0, sms = 0;
-    if (per_sm == 0)
-    {
+    // one-time set-up, thread-safe (a function-local static is initialised once)
+    static const LaunchSetup setup = [] {
         cudaError_t err =
             cudaFuncSetAttribute(convq_kernel<F, MODE, BF16, OT>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM_REQ);
-        if (err != cudaSuccess) return err;
-        int occ = 0, dev = 0;
+        if (err != cudaSuccess) return LaunchSetup{err, 0, 0};
+        int occ = 0, dev = 0, sms = 0;
         if ((err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, convq_kernel<F, MODE, BF16, OT>, G::THREADS, G::SMEM_REQ)) !=
             cudaSuccess)
-            return err;
-        if ((err = cudaGetDevice(&dev)) != cudaSuccess) return err;
-        if ((err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return err;
-        if (occ < 1) return cudaErrorInvalidConfiguration;
-        per_sm = occ < static_cast<int>(512 / G::TMEM_COLS) ? occ : static_cast<int>(512 / G::TMEM_COLS);
-    }
+            return LaunchSetup{err, 0, 0};
+        if ((err = cudaGetDevice(&dev)) != cudaSuccess) return LaunchSetup{err, 0, 0};
+        if ((err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return LaunchSetup{err, 0, 0};
+        if (occ < 1) return LaunchSetup{cudaErrorInvalidConfiguration, 0, 0};
+        const int cap = static_cast<int>(512 / G::TMEM_COLS);
+        return LaunchSetup{cudaSuccess, occ < cap ? occ : cap, sms};
+    }();
+    if (setup.err != cudaSuccess) return setup.err;
+    const int per_sm = setup.per_sm, sms = setup.sms;
     const int grid = p.ntiles < per_sm * sms ? p.ntiles : per_sm * sms;
     convq_kernel<F, MODE, BF16, OT><<<grid, G::THREADS, G::SMEM_REQ, stream>>>(p);
     return cudaGetLastError();

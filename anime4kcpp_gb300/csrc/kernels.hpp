@@ -24,6 +24,16 @@ struct Plane
 // floats, 8 + 8*8 bias floats.
 constexpr int kAcnetKernels = 8 * 9 + 8 * 8 * 9 * 8 + 8 * 4;
 constexpr int kAcnetBiases = 8 + 8 * 8;
+// One-time launch set-up of a kernel (function attributes, CTAs per SM, SM
+// count), computed once per process by a function-local static initialiser,
+// which C++ runs exactly once even when several host threads launch at once.
+struct LaunchSetup
+{
+    cudaError_t err;
+    int per_sm;
+    int sms;
+};
+
 struct AcnetLegacyWeights
 {
     float k[kAcnetKernels];
