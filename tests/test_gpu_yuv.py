@@ -110,3 +110,32 @@ def test_yuv_rejects_bad_planes():
     with pytest.raises(RuntimeError, match="shift"):
         p.process_yuv_device([(f32,)], [(torch.empty((64, 64), dtype=torch.float32, device="cuda"),)], 2.0, 6)
     del y
+
+
+def test_video_config_full_size():
+    """The video workload at its full size: 8 frames of 1920x1080 10-bit 4:2:0
+    in one call, x4 with ARNet-B8, FP16 form.  Two frames are checked: their
+    chroma planes whole, their luma in two windows against the oracle on the
+    input crop with a 32-pixel margin (the two x2 passes see 18 + 9 pixels):
+    never more than 1 LSB of the 10-bit value off, >= 95 % exact (the exact
+    fraction depends on the content: 97.6 % on these frames)."""
+    H, W, n, M = 1080, 1920, 96, 32
+    frames = [_frame10(H, W, seed=300 + 3 * i) for i in range(8)]
+    p = ac.Processor("cuda", 0, "arnet-b8", precision="fp16")
+    got = _run(p, frames, 4.0, 6)
+    assert p.ok(), p.error()
+    for i in (0, 5):
+        y, u, v = frames[i]
+        gy, gu, gv = got[i]
+        assert gy.shape == (4 * H, 4 * W) and gu.shape == (2 * H, 2 * W)
+        for pl, g in ((u, gu), (v, gv)):
+            assert np.array_equal(g, oracle.resize(pl, 4 * pl.shape[1], 4 * pl.shape[0], oracle.RESIZE_CATMULL_ROM))
+        for wy, wx in ((0, 0), (H // 2 - n // 2, W // 2 - n // 2)):
+            y0, x0 = max(0, wy - M), max(0, wx - M)
+            y1, x1 = min(H, wy + n + M), min(W, wx + n + M)
+            crop = (y[y0:y1, x0:x1].astype(np.uint32) << 6).astype(np.uint16)
+            want = oracle.process(np.ascontiguousarray(crop), 4.0, "arnet-b8") >> 6
+            oy, ox = 4 * (wy - y0), 4 * (wx - x0)
+            d = np.abs(gy[4 * wy:4 * (wy + n), 4 * wx:4 * (wx + n)].astype(int) -
+                       want[oy:oy + 4 * n, ox:ox + 4 * n].astype(int))
+            assert d.max() <= 1 and (d == 0).mean() >= 0.95, (d.max(), (d == 0).mean())
