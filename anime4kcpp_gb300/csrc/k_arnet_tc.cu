@@ -898,41 +898,54 @@ cudaError_t launch_acnet8_tc(const float* kernels, const float* biases, const fl
     return launch_acnet8_tc_batch(kernels, biases, alphas, blocks, packed, bf16, 1, &in, &out, maps, status, stream);
 }
 
-// FSRCNNX<8> (B4) x2 in the tensor-core form: the 5x5 head in FP32
-// (launch_f3_head8), layers 1 + 2 and 3 + the tail as two two-layer launches
-// (the tail: PReLU, conv1x1 8->8 + feat, PReLU), the upscale conv3x3 8->4 +
-// pixel shuffle in FP32 without the nearest-input add.  Parameters in the
-// reference layout (FSRCNNX.hpp:28-66): kernels head 200, 4 x 576, 1x1 64,
+// FSRCNNX<8> (B4) x2 in the tensor-core form over n single-channel images of
+// one element type, every layer as one launch over all of them: the 5x5 head
+// in FP32 (launch_f3_head8), layers 1 + 2 and 3 + the tail as two two-layer
+// launches (the tail: PReLU, conv1x1 8->8 + feat, PReLU), the upscale conv3x3
+// 8->4 + pixel shuffle in FP32 without the nearest-input add.  Parameters in
+// the reference layout (FSRCNNX.hpp:28-66): kernels head 200, 4 x 576, 1x1 64,
 // upscale 288; biases 8 per layer (head, 4 convs, 1x1) then 4; PReLU slopes
 // 8 per layer (4 convs, then the one after the 1x1).  packed: the 4 layers'
-// pack_pair_conv8 output; maps: three [h][w] arrays of 16-byte pixels.
-cudaError_t launch_fsrcnnx8_tc(const float* kernels, const float* biases, const float* alphas, const void* packed, bool bf16,
-                               const Plane& in, const Plane& out, void* const maps[3], int* status, cudaStream_t stream)
+// pack_pair_conv8 output; maps[3 i + j]: image i's three [h][w] arrays of
+// 16-byte pixels.
+cudaError_t launch_fsrcnnx8_tc_batch(const float* kernels, const float* biases, const float* alphas, const void* packed, bool bf16,
+                                     int n, const Plane* in, const Plane* out, void* const* maps, int* status, cudaStream_t stream)
 {
     using namespace arnettc;
-    if (in.w <= 0 || in.h <= 0) return cudaSuccess;
-    if (!packed || !status || !maps) return cudaErrorInvalidValue;
-    if (in.channels != 1 || out.channels != 1 || out.w != 2 * in.w || out.h != 2 * in.h) return cudaErrorInvalidValue;
-    cudaError_t err = launch_f3_head8(kernels, biases, bf16, in, maps[0], stream);
-    if (err != cudaSuccess) return err;
-    count_launch();
+    if (n <= 0) return cudaSuccess;
+    if (n > kMaxImg || !packed || !status || !maps) return cudaErrorInvalidValue;
+    void* feat[kMaxImg];
     Conv2Params c2;
     std::memset(&c2, 0, sizeof(c2));
-    ConvImg& I = c2.img[0];
-    I.w = in.w;
-    I.h = in.h;
-    I.tiles_x = (in.w + TW2 - 1) / TW2;
-    I.tile0 = 0;
-    I.feat = static_cast<const uint4*>(maps[0]);
-    const int tiles2 = I.tiles_x * ((in.h + TH2 - 1) / TH2);
-    c2.nimg = 1;
+    int tiles2 = 0;
+    for (int i = 0; i < n; i++)
+    {
+        if (in[i].w <= 0 || in[i].h <= 0 || in[i].channels != 1 || out[i].channels != 1 || in[i].type != in[0].type ||
+            out[i].w != 2 * in[i].w || out[i].h != 2 * in[i].h)
+            return cudaErrorInvalidValue;
+        feat[i] = maps[3 * i];
+        ConvImg& I = c2.img[i];
+        I.w = in[i].w;
+        I.h = in[i].h;
+        I.tiles_x = (in[i].w + TW2 - 1) / TW2;
+        I.tile0 = tiles2;
+        I.feat = static_cast<const uint4*>(maps[3 * i]);
+        tiles2 += I.tiles_x * ((in[i].h + TH2 - 1) / TH2);
+    }
+    c2.nimg = n;
     c2.status = status;
+    cudaError_t err = launch_f3_head8(kernels, biases, bf16, n, in, feat, stream);
+    if (err != cudaSuccess) return err;
+    count_launch();
     const uint4* pk = static_cast<const uint4*>(packed);
-    // layers 1 and 2 (PReLU)
+    // layers 1 and 2 (PReLU): map 0 -> map 1
     {
         Conv2Params q = c2;
-        q.img[0].in = static_cast<const uint4*>(maps[0]);
-        q.img[0].out = static_cast<uint4*>(maps[1]);
+        for (int i = 0; i < n; i++)
+        {
+            q.img[i].in = static_cast<const uint4*>(maps[3 * i]);
+            q.img[i].out = static_cast<uint4*>(maps[3 * i + 1]);
+        }
         q.bwA = pk;
         q.bwB = pk + (B_BYTES / 16);
         for (int i = 0; i < 8; i++)
@@ -946,11 +959,14 @@ cudaError_t launch_fsrcnnx8_tc(const float* kernels, const float* biases, const 
         if (err != cudaSuccess) return err;
         count_launch();
     }
-    // layer 3 (PReLU) and the tail
+    // layer 3 (PReLU) and the tail: map 1 -> map 2
     {
         Conv2Params q = c2;
-        q.img[0].in = static_cast<const uint4*>(maps[1]);
-        q.img[0].out = static_cast<uint4*>(maps[2]);
+        for (int i = 0; i < n; i++)
+        {
+            q.img[i].in = static_cast<const uint4*>(maps[3 * i + 1]);
+            q.img[i].out = static_cast<uint4*>(maps[3 * i + 2]);
+        }
         q.bwA = pk + 2 * (B_BYTES / 16);
         q.bwB = pk + 3 * (B_BYTES / 16);
         for (int i = 0; i < 8; i++)
@@ -972,10 +988,20 @@ cudaError_t launch_fsrcnnx8_tc(const float* kernels, const float* biases, const 
     for (int i = 0; i < 288; i++) u.k[i] = kernels[200 + 4 * 576 + 64 + i];
     for (int i = 0; i < 4; i++) u.b[i] = biases[48 + i];
     u.no_nearest = 1;
-    u.map[0] = static_cast<const uint4*>(maps[2]);
-    u.src[0] = in;
-    u.dst[0] = out;
-    return launch_up(u, bf16, 1, stream);
+    for (int i = 0; i < n; i++)
+    {
+        u.map[i] = static_cast<const uint4*>(maps[3 * i + 2]);
+        u.src[i] = in[i];
+        u.dst[i] = out[i];
+    }
+    return launch_up(u, bf16, n, stream);
+}
+
+cudaError_t launch_fsrcnnx8_tc(const float* kernels, const float* biases, const float* alphas, const void* packed, bool bf16,
+                               const Plane& in, const Plane& out, void* const maps[3], int* status, cudaStream_t stream)
+{
+    if (in.w <= 0 || in.h <= 0) return cudaSuccess;
+    return launch_fsrcnnx8_tc_batch(kernels, biases, alphas, packed, bf16, 1, &in, &out, maps, status, stream);
 }
 
 }  // namespace acgb

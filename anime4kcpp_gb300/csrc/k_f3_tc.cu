@@ -450,17 +450,22 @@ struct HeadP
 {
     float k[F * K * K];
     float b[F];
+    Plane in[kMaxImg];  // image blockIdx.z
+    uint4* feat[kMaxImg];
 };
 
 // conv KxK 1 -> F (identity) in FP32 from the input plane, taps clamped,
-// stored as an F-channel 16-bit map.
+// stored as an F-channel 16-bit map; blockIdx.z picks the image.
 template <typename T, int K, int F, bool BF16>
-__global__ void __launch_bounds__(256) head_kernel(const __grid_constant__ HeadP<K, F> W, Plane in, uint4* __restrict__ feat)
+__global__ void __launch_bounds__(256) head_kernel(const __grid_constant__ HeadP<K, F> W)
 {
     constexpr int R = K / 2, SW = 32 + 2 * R, SH = 8 + 2 * R;
+    const Plane& in = W.in[blockIdx.z];
+    uint4* __restrict__ feat = W.feat[blockIdx.z];
     // the block's 32 x 8 pixels with their clamped halo, converted once
     __shared__ float s[SH][SW];
     const int bx = blockIdx.x * 32, by = blockIdx.y * 8;
+    if (bx >= in.w || by >= in.h) return;  // the grid covers the largest image of the launch
     for (int i = threadIdx.x; i < SW * SH; i += 256)
     {
         const int sy = i / SW, sx = i - sy * SW;
@@ -585,39 +590,56 @@ cudaError_t convq_mode(int mode, const ConvPP<F>& p, cudaStream_t stream)
     }
 }
 
-// The network over one image: head, the 3x3 F->F layers (ArtCNN: blocks ReLU
-// layers, then identity + feat; FSRCNNX: blocks - 1 PReLU layers, then the
-// tail: PReLU, 1x1 + feat, PReLU), upscale.  maps: three [h][w][F] 16-bit
-// arrays; packed: pack_f3_tc_weights().
+// One head launch over n images (grid z = image).
+template <typename T, int K, int F, bool BF16>
+cudaError_t launch_head(const float* kernels, const float* biases, int n, const Plane* in, uint4* const* feat, cudaStream_t stream)
+{
+    HeadP<K, F> hp;
+    for (int i = 0; i < F * K * K; i++) hp.k[i] = kernels[i];
+    for (int i = 0; i < F; i++) hp.b[i] = biases[i];
+    int mw = 0, mh = 0;
+    for (int i = 0; i < n; i++)
+    {
+        hp.in[i] = in[i];
+        hp.feat[i] = feat[i];
+        mw = in[i].w > mw ? in[i].w : mw;
+        mh = in[i].h > mh ? in[i].h : mh;
+    }
+    head_kernel<T, K, F, BF16><<<dim3((mw + 31) / 32, (mh + 7) / 8, n), 256, 0, stream>>>(hp);
+    return cudaGetLastError();
+}
+
+// The network over n images (one launch per layer over all of them): head,
+// the 3x3 F->F layers (ArtCNN: blocks ReLU layers, then identity + feat;
+// FSRCNNX: blocks - 1 PReLU layers, then the tail: PReLU, 1x1 + feat,
+// PReLU), upscale.  maps[3 i + j]: image i's three [h][w][F] 16-bit arrays;
+// packed: pack_f3_tc_weights().
 template <typename T, int F, int K, bool BF16>
 cudaError_t run_typed(const float* kernels, const float* biases, const float* alphas, bool artcnn, int blocks, const void* packed,
-                      const Plane& in, const Plane& out, void* const maps[3], int* status, cudaStream_t stream)
+                      int n, const Plane* in, const Plane* out, void* const* maps, int* status, cudaStream_t stream)
 {
-    const int w = in.w, h = in.h;
-    uint4* feat = static_cast<uint4*>(maps[0]);
-    uint4* a = static_cast<uint4*>(maps[1]);
-    uint4* bm = static_cast<uint4*>(maps[2]);
-    {
-        HeadP<K, F> hp;
-        for (int i = 0; i < F * K * K; i++) hp.k[i] = kernels[i];
-        for (int i = 0; i < F; i++) hp.b[i] = biases[i];
-        const dim3 pgrid((w + 31) / 32, (h + 7) / 8);
-        head_kernel<T, K, F, BF16><<<pgrid, 256, 0, stream>>>(hp, in, feat);
-        cudaError_t err = cudaGetLastError();
-        if (err != cudaSuccess) return err;
-        count_launch();
-    }
+    uint4* feat[kMaxImg];
+    for (int i = 0; i < n; i++) feat[i] = static_cast<uint4*>(maps[3 * i]);
+    cudaError_t err = launch_head<T, K, F, BF16>(kernels, biases, n, in, feat, stream);
+    if (err != cudaSuccess) return err;
+    count_launch();
     // kernel parameters (large: thread-local, not on the stack)
     static thread_local ConvPP<F> pp_storage;
     ConvPP<F>& r = pp_storage;
     std::memset(&r, 0, sizeof(r));
     r.status = status;
-    r.nimg = 1;
-    const int tiles_x = (w + TW - 1) / TW;
-    r.ntiles = tiles_x * ((h + TH - 1) / TH);
+    r.nimg = n;
+    int tiles_x[kMaxImg], tile0[kMaxImg];
+    r.ntiles = 0;
+    for (int i = 0; i < n; i++)
+    {
+        tiles_x[i] = (in[i].w + TW - 1) / TW;
+        tile0[i] = r.ntiles;
+        r.ntiles += tiles_x[i] * ((in[i].h + TH - 1) / TH);
+    }
     const size_t lb = static_cast<size_t>(24) * F * F;  // packed 16-bit values per 3x3 layer
     const int hk = F * K * K;                           // head kernel floats
-    const uint4* cur = feat;
+    int cur = 0, a = 1, bm = 2;                         // map slots: input, output, spare
     const int nconv = artcnn ? blocks + 1 : blocks;
     for (int l = 1; l <= nconv; l++)
     {
@@ -638,13 +660,16 @@ cudaError_t run_typed(const float* kernels, const float* biases, const float* al
                 r.a1[i] = alphas[F * l + i];
             }
         }
-        r.img[0] = ImgP{feat, a, w, h, tiles_x, 0, Plane{}};
-        if (!encode_tmap_3d_u16_strided(&r.tmap[0], cur, F, w, h, 8, WW, WH, 2)) return cudaErrorInvalidValue;
-        cudaError_t err = convq_mode<F, BF16>(mode, r, stream);
-        if (err != cudaSuccess) return err;
+        for (int i = 0; i < n; i++)
+        {
+            r.img[i] = ImgP{feat[i], static_cast<uint4*>(maps[3 * i + a]), in[i].w, in[i].h, tiles_x[i], tile0[i], Plane{}};
+            if (!encode_tmap_3d_u16_strided(&r.tmap[i], maps[3 * i + cur], F, in[i].w, in[i].h, 8, WW, WH, 2))
+                return cudaErrorInvalidValue;
+        }
+        if ((err = convq_mode<F, BF16>(mode, r, stream)) != cudaSuccess) return err;
         count_launch();
-        cur = a;
-        uint4* t = a;
+        cur = a;  // this layer's output feeds the next; output and spare swap
+        const int t = a;
         a = bm;
         bm = t;
     }
@@ -652,22 +677,29 @@ cudaError_t run_typed(const float* kernels, const float* biases, const float* al
     const int lu = blocks + 2;
     r.bw = static_cast<const uint4*>(packed) + nconv * lb * 2 / 16;
     for (int i = 0; i < 4; i++) r.b[i] = biases[F * lu + i];
-    r.img[0] = ImgP{nullptr, nullptr, w, h, tiles_x, 0, out};
-    if (!encode_tmap_3d_u16_strided(&r.tmap[0], cur, F, w, h, 8, WW, WH, 2)) return cudaErrorInvalidValue;
-    cudaError_t err = launch_convq<F, kUp, BF16, T>(r, stream);
+    for (int i = 0; i < n; i++)
+    {
+        r.img[i] = ImgP{nullptr, nullptr, in[i].w, in[i].h, tiles_x[i], tile0[i], out[i]};
+        if (!encode_tmap_3d_u16_strided(&r.tmap[i], maps[3 * i + cur], F, in[i].w, in[i].h, 8, WW, WH, 2))
+            return cudaErrorInvalidValue;
+    }
+    err = launch_convq<F, kUp, BF16, T>(r, stream);
     if (err == cudaSuccess) count_launch();
     return err;
 }
 
 template <int F, int K, bool BF16>
 cudaError_t run_type(const float* kernels, const float* biases, const float* alphas, bool artcnn, int blocks, const void* packed,
-                     const Plane& in, const Plane& out, void* const maps[3], int* status, cudaStream_t stream)
+                     int n, const Plane* in, const Plane* out, void* const* maps, int* status, cudaStream_t stream)
 {
-    switch (in.type)
+    switch (in[0].type)
     {
-    case kU8: return run_typed<uint8_t, F, K, BF16>(kernels, biases, alphas, artcnn, blocks, packed, in, out, maps, status, stream);
-    case kU16: return run_typed<uint16_t, F, K, BF16>(kernels, biases, alphas, artcnn, blocks, packed, in, out, maps, status, stream);
-    case kF32: return run_typed<float, F, K, BF16>(kernels, biases, alphas, artcnn, blocks, packed, in, out, maps, status, stream);
+    case kU8:
+        return run_typed<uint8_t, F, K, BF16>(kernels, biases, alphas, artcnn, blocks, packed, n, in, out, maps, status, stream);
+    case kU16:
+        return run_typed<uint16_t, F, K, BF16>(kernels, biases, alphas, artcnn, blocks, packed, n, in, out, maps, status, stream);
+    case kF32:
+        return run_typed<float, F, K, BF16>(kernels, biases, alphas, artcnn, blocks, packed, n, in, out, maps, status, stream);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -688,51 +720,62 @@ void pack_f3_tc_weights(const float* kernels, int F, bool artcnn, int blocks, bo
     f3tc::pack_f3_pair(up, F, true, bf16, packed.data() + layers * lb);
 }
 
-// FSRCNNX<8>'s conv5x5 1->8 head (identity) in FP32 into an 8-channel 16-bit
-// map [h][w] x 16 bytes.
-cudaError_t launch_f3_head8(const float* kernels, const float* biases, bool bf16, const Plane& in, void* feat, cudaStream_t stream)
+// FSRCNNX<8>'s conv5x5 1->8 head (identity) in FP32 into 8-channel 16-bit
+// maps [h][w] x 16 bytes, one launch over n images of one element type.
+cudaError_t launch_f3_head8(const float* kernels, const float* biases, bool bf16, int n, const Plane* in, void* const* feat,
+                            cudaStream_t stream)
 {
     using namespace f3tc;
-    if (in.w <= 0 || in.h <= 0) return cudaSuccess;
-    HeadP<5, 8> hp;
-    for (int i = 0; i < 8 * 25; i++) hp.k[i] = kernels[i];
-    for (int i = 0; i < 8; i++) hp.b[i] = biases[i];
-    const dim3 grid((in.w + 31) / 32, (in.h + 7) / 8);
-    uint4* f = static_cast<uint4*>(feat);
-    switch (in.type)
+    if (n <= 0) return cudaSuccess;
+    if (n > kMaxImg) return cudaErrorInvalidValue;
+    uint4* f[kMaxImg];
+    for (int i = 0; i < n; i++)
+    {
+        if (in[i].w <= 0 || in[i].h <= 0 || in[i].type != in[0].type) return cudaErrorInvalidValue;
+        f[i] = static_cast<uint4*>(feat[i]);
+    }
+    switch (in[0].type)
     {
     case kU8:
-        bf16 ? head_kernel<uint8_t, 5, 8, true><<<grid, 256, 0, stream>>>(hp, in, f)
-             : head_kernel<uint8_t, 5, 8, false><<<grid, 256, 0, stream>>>(hp, in, f);
-        break;
+        return bf16 ? launch_head<uint8_t, 5, 8, true>(kernels, biases, n, in, f, stream)
+                    : launch_head<uint8_t, 5, 8, false>(kernels, biases, n, in, f, stream);
     case kU16:
-        bf16 ? head_kernel<uint16_t, 5, 8, true><<<grid, 256, 0, stream>>>(hp, in, f)
-             : head_kernel<uint16_t, 5, 8, false><<<grid, 256, 0, stream>>>(hp, in, f);
-        break;
+        return bf16 ? launch_head<uint16_t, 5, 8, true>(kernels, biases, n, in, f, stream)
+                    : launch_head<uint16_t, 5, 8, false>(kernels, biases, n, in, f, stream);
     case kF32:
-        bf16 ? head_kernel<float, 5, 8, true><<<grid, 256, 0, stream>>>(hp, in, f)
-             : head_kernel<float, 5, 8, false><<<grid, 256, 0, stream>>>(hp, in, f);
-        break;
+        return bf16 ? launch_head<float, 5, 8, true>(kernels, biases, n, in, f, stream)
+                    : launch_head<float, 5, 8, false>(kernels, biases, n, in, f, stream);
     default: return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
+}
+
+cudaError_t launch_f3_tc_batch(const float* kernels, const float* biases, const float* alphas, bool artcnn, int F, int blocks,
+                               const void* packed, bool bf16, int n, const Plane* in, const Plane* out, void* const* maps,
+                               int* status, cudaStream_t stream)
+{
+    using namespace f3tc;
+    if (n <= 0) return cudaSuccess;
+    if (n > kMaxImg || !packed || !status || !maps || blocks < 2 || (F != 16 && F != 32) || (!artcnn && F != 16))
+        return cudaErrorInvalidValue;
+    for (int i = 0; i < n; i++)
+        if (in[i].w <= 0 || in[i].h <= 0 || in[i].type != in[0].type || in[i].channels != 1 || out[i].channels != 1 ||
+            out[i].w != 2 * in[i].w || out[i].h != 2 * in[i].h)
+            return cudaErrorInvalidValue;
+    if (artcnn)
+        return F == 32 ? (bf16 ? run_type<32, 3, true>(kernels, biases, alphas, true, blocks, packed, n, in, out, maps, status, stream)
+                               : run_type<32, 3, false>(kernels, biases, alphas, true, blocks, packed, n, in, out, maps, status, stream))
+                       : (bf16 ? run_type<16, 3, true>(kernels, biases, alphas, true, blocks, packed, n, in, out, maps, status, stream)
+                               : run_type<16, 3, false>(kernels, biases, alphas, true, blocks, packed, n, in, out, maps, status, stream));
+    return bf16 ? run_type<16, 5, true>(kernels, biases, alphas, false, blocks, packed, n, in, out, maps, status, stream)
+                : run_type<16, 5, false>(kernels, biases, alphas, false, blocks, packed, n, in, out, maps, status, stream);
 }
 
 cudaError_t launch_f3_tc(const float* kernels, const float* biases, const float* alphas, bool artcnn, int F, int blocks,
                          const void* packed, bool bf16, const Plane& in, const Plane& out, void* const maps[3], int* status,
                          cudaStream_t stream)
 {
-    using namespace f3tc;
     if (in.w <= 0 || in.h <= 0) return cudaSuccess;
-    if (!packed || !status || blocks < 2 || (F != 16 && F != 32)) return cudaErrorInvalidValue;
-    if (artcnn)
-        return F == 32 ? (bf16 ? run_type<32, 3, true>(kernels, biases, alphas, true, blocks, packed, in, out, maps, status, stream)
-                               : run_type<32, 3, false>(kernels, biases, alphas, true, blocks, packed, in, out, maps, status, stream))
-                       : (bf16 ? run_type<16, 3, true>(kernels, biases, alphas, true, blocks, packed, in, out, maps, status, stream)
-                               : run_type<16, 3, false>(kernels, biases, alphas, true, blocks, packed, in, out, maps, status, stream));
-    if (F != 16) return cudaErrorInvalidValue;
-    return bf16 ? run_type<16, 5, true>(kernels, biases, alphas, false, blocks, packed, in, out, maps, status, stream)
-                : run_type<16, 5, false>(kernels, biases, alphas, false, blocks, packed, in, out, maps, status, stream);
+    return launch_f3_tc_batch(kernels, biases, alphas, artcnn, F, blocks, packed, bf16, 1, &in, &out, maps, status, stream);
 }
 
 }  // namespace acgb

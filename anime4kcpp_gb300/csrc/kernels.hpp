@@ -187,9 +187,13 @@ cudaError_t launch_acnet8_tc_batch(const float* kernels, const float* biases, co
 // FSRCNNX<8> in a tensor-core form (k_arnet_tc.cu): FP32 5x5 head
 // (launch_f3_head8), the 3x3 8->8 layers as two two-layer tcgen05 launches,
 // FP32 upscale.  packed: 4 x pack_pair_conv8; maps: three w*h*16-byte arrays.
-cudaError_t launch_f3_head8(const float* kernels, const float* biases, bool bf16, const Plane& in, void* feat, cudaStream_t stream);
+cudaError_t launch_f3_head8(const float* kernels, const float* biases, bool bf16, int n, const Plane* in, void* const* feat,
+                            cudaStream_t stream);
 cudaError_t launch_fsrcnnx8_tc(const float* kernels, const float* biases, const float* alphas, const void* packed, bool bf16,
                                const Plane& in, const Plane& out, void* const maps[3], int* status, cudaStream_t stream);
+// The same over n <= 16 single-channel images (maps[3 i + j]), every layer one launch.
+cudaError_t launch_fsrcnnx8_tc_batch(const float* kernels, const float* biases, const float* alphas, const void* packed, bool bf16,
+                                     int n, const Plane* in, const Plane* out, void* const* maps, int* status, cudaStream_t stream);
 // ArtCNN<F> (F = 16, 32) and FSRCNNX<F> (F = 8, 16) x2 passes in plain FP32
 // (one kernel per layer; parameters in the reference blob layout,
 // ArtCNN.hpp:44-56, FSRCNNX.hpp:46-66); maps: three [h][w][F] float arrays.
@@ -205,6 +209,11 @@ void pack_f3_tc_weights(const float* kernels, int F, bool artcnn, int blocks, bo
 cudaError_t launch_f3_tc(const float* kernels, const float* biases, const float* alphas, bool artcnn, int F, int blocks,
                          const void* packed, bool bf16, const Plane& in, const Plane& out, void* const maps[3], int* status,
                          cudaStream_t stream);
+// The same over n <= 16 single-channel images of one element type, every
+// layer one launch over all of them; maps[3 i + j] holds image i's maps.
+cudaError_t launch_f3_tc_batch(const float* kernels, const float* biases, const float* alphas, bool artcnn, int F, int blocks,
+                               const void* packed, bool bf16, int n, const Plane* in, const Plane* out, void* const* maps,
+                               int* status, cudaStream_t stream);
 
 // Merge for chroma resampled by exactly `factor` (2 or 4) on both axes:
 // phase_weights[k*4 + t] is the Catmull-Rom weight of tap t of output phase k,

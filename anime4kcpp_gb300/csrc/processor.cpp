@@ -1055,10 +1055,13 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
     const bool acn8 = acnet8Quad();
     const bool tcBatch =
         ((spec_.family == Family::ACNetLegacy && precision_ != Precision::FP32 && tcKernel_ >= 3) || acn8) && fused_;
-    // ARNet / ACNet<8> B18 in a tensor-core form: single-channel images of one
-    // element type run every layer as one launch over all images
-    bool layered = (spec_.family == Family::ARNet || spec_.family == Family::ACNet8) && !acn8 &&
-                   precision_ != Precision::FP32 && arnetTc_ && n > 1 && (factor == 2.0 || factor == 4.0);
+    // ARNet, ACNet<8> B18, ArtCNN and FSRCNNX in a tensor-core form:
+    // single-channel images of one element type run every layer as one launch
+    // over all images
+    bool layered = (((spec_.family == Family::ARNet || spec_.family == Family::ACNet8) && !acn8 &&
+                     precision_ != Precision::FP32 && arnetTc_) ||
+                    f3Tc()) &&
+                   n > 1 && (factor == 2.0 || factor == 4.0);
     for (int i = 0; i < n && layered; i++)
         layered = src[i].c == 1 && src[i].type == src[0].type && dst[i].w == static_cast<int>(factor) * src[i].w &&
                   dst[i].h == static_cast<int>(factor) * src[i].h;
@@ -1213,7 +1216,10 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
 bool GB300Processor::layeredBatch(ThreadState& ts, int n, const DeviceImage* src, const DeviceImage* dst, double factor,
                                   cudaStream_t s)
 {
-    const int per = spec_.family == Family::ARNet ? 3 : 2;  // work maps per image
+    const int per = spec_.family == Family::ACNet8 ? 2 : 3;  // work maps per image
+    // bytes per map pixel: 8 16-bit channels, or F for ArtCNN / FSRCNNX<16>
+    const bool wide = (spec_.family == Family::ArtCNN || spec_.family == Family::FSRCNNX) && spec_.channels > 8;
+    const size_t bpp = wide ? static_cast<size_t>(spec_.channels) * 2 : 16;
     const bool bf16 = precision_ == Precision::BF16;
     const void* w = arnetWeights(bf16);
     int* status = tc_status_buffer();
@@ -1252,7 +1258,7 @@ bool GB300Processor::layeredBatch(ThreadState& ts, int n, const DeviceImage* src
                 in[j] = plane_of(a[g0 + j]);
                 out[j] = plane_of(b[g0 + j]);
                 moff[j] = mapBytes;
-                mapBytes += (static_cast<size_t>(in[j].w) * in[j].h * 16 + 255) & ~static_cast<size_t>(255);
+                mapBytes += (static_cast<size_t>(in[j].w) * in[j].h * bpp + 255) & ~static_cast<size_t>(255);
             }
             std::vector<void*> maps(static_cast<size_t>(per) * m);
             for (int k = 0; k < per; k++)
@@ -1264,12 +1270,21 @@ bool GB300Processor::layeredBatch(ThreadState& ts, int n, const DeviceImage* src
             double px = 0.0;
             for (int j = 0; j < m; j++) px += static_cast<double>(out[j].w) * out[j].h;
             const std::pair<cudaEvent_t, cudaEvent_t> ev = profileBegin(ts, s);
-            const cudaError_t err =
-                spec_.family == Family::ARNet
-                    ? launch_arnet_tc_batch(mp.kernels.data(), mp.biases.data(), mp.alphas.data(), spec_.blocks, w, bf16, m,
-                                            in.data(), out.data(), maps.data(), status, s)
-                    : launch_acnet8_tc_batch(mp.kernels.data(), mp.biases.data(), mp.alphas.data(), spec_.blocks, w, bf16, m,
-                                             in.data(), out.data(), maps.data(), status, s);
+            const float* al = mp.alphas.empty() ? nullptr : mp.alphas.data();
+            cudaError_t err;
+            if (spec_.family == Family::ARNet)
+                err = launch_arnet_tc_batch(mp.kernels.data(), mp.biases.data(), al, spec_.blocks, w, bf16, m, in.data(),
+                                            out.data(), maps.data(), status, s);
+            else if (spec_.family == Family::ACNet8)
+                err = launch_acnet8_tc_batch(mp.kernels.data(), mp.biases.data(), al, spec_.blocks, w, bf16, m, in.data(),
+                                             out.data(), maps.data(), status, s);
+            else if (!wide)
+                err = launch_fsrcnnx8_tc_batch(mp.kernels.data(), mp.biases.data(), al, w, bf16, m, in.data(), out.data(),
+                                               maps.data(), status, s);
+            else
+                err = launch_f3_tc_batch(mp.kernels.data(), mp.biases.data(), al, spec_.family == Family::ArtCNN,
+                                         spec_.channels, spec_.blocks, w, bf16, m, in.data(), out.data(), maps.data(), status,
+                                         s);
             profileEnd(ts, ev, s, px);
             if (err != cudaSuccess) return fail(ts, "batched upscale", err), false;
         }

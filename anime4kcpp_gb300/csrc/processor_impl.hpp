@@ -137,6 +137,13 @@ private:
     // quad kernel.
     const void* tcWeights(Precision p, int form);
     const void* arnetWeights(bool bf16);  // packed 8->8 layers of the ARNet / ACNet<8> tensor-core forms
+    // ArtCNN / FSRCNNX in a tensor-core form (FSRCNNX<8>: B4, the 8-channel path)
+    bool f3Tc() const
+    {
+        return (spec_.family == Family::ArtCNN ||
+                (spec_.family == Family::FSRCNNX && (spec_.channels == 16 || (spec_.channels == 8 && spec_.blocks == 4)))) &&
+               precision_ != Precision::FP32 && arnetTc_;
+    }
     // ACNet<8> B4 / B8 in a tensor-core form run the quad kernel (fused colour path, batching)
     bool acnet8Quad() const
     {
