@@ -1,6 +1,6 @@
 """CUDA path vs the oracle, through the C ABI (GPU required).
 
-Tolerances (BASELINE gate for the plain FP32 form): integer outputs within
+Tolerances (the parity gate of the plain FP32 form): integer outputs within
 +-1 LSB of the reference's CPU processor on >= 99.99 % of pixels and never
 more than 1 LSB off; f32 outputs within 1e-4 absolute.  The golden vectors
 come from the reference's own CPU processor; larger seeded cases are checked
