@@ -170,6 +170,17 @@ def output_shape(width, height, channels, factor):
     return ow.value, oh.value
 
 
+class _StaticProperty:
+    """A read-only attribute computed on each access, on the class and on its
+    instances alike (pybind11's ``def_property_readonly_static``)."""
+
+    def __init__(self, fget):
+        self.fget = fget
+
+    def __get__(self, obj, cls=None):
+        return self.fget()
+
+
 class Processor:
     """Mirror of the reference's ``pyac.core.Processor`` backed by the GB300 library."""
 
@@ -314,7 +325,7 @@ class Processor:
             raise RuntimeError(self.error())
         return ms.value, n.value, px.value
 
-    InfoList = property(lambda self: (native().ac_processor_info(0).decode(), native().ac_processor_info(2).decode()))
+    InfoList = _StaticProperty(lambda: (native().ac_processor_info(0).decode(), native().ac_processor_info(2).decode()))
 
 
 class Server:
