@@ -78,7 +78,7 @@ def test_default_processor_is_acnet8_b8_hdn(pyac):
     img = rng.integers(0, 256, (61, 83, 3), dtype=np.uint8)
     p = pyac.core.Processor()
     assert p.ok(), p.error()
-    assert "acnet" in str(p).lower()
+    assert str(p) == p.name() and str(p)  # the device's name, as Processor::name
     out = p(img)
     ref = ac.Processor("cuda", 0, "acnet-f8b8-hdn")(img, 2.0)
     assert out.shape == (122, 166, 3) and np.array_equal(out, ref)
