@@ -295,7 +295,7 @@ GB300Processor::GB300Processor(int device, const ModelSpec& spec) : spec_(spec)
     }
     if (!(prop.major == 10 && prop.minor == 3))
     {
-        initError_ = std::string("device ") + prop.name + " is not sm_103 (GB300); this build only carries sm_103a code";
+        initError_ = std::string("device ") + prop.name + " is not sm_103 (GB300); the library carries only sm_103a code";
         return;
     }
     name_ = prop.name;

@@ -86,7 +86,7 @@ def _describe(name):
             parts[1][3:], (" (" + ", ".join(extra) + " training)") if extra else "")
     if name.startswith("arnet"):
         extra = [t for t in parts[2:]]
-        return ("ARNet<8>, %s residual blocks%s (this build carries seeded parameters of the trained models' shapes: "
+        return ("ARNet<8>, %s residual blocks%s (this library carries seeded parameters of the trained models' shapes: "
                 "the trained ones are not distributed with the reference's source)." % (
                     parts[1][3:], (" (" + ", ".join(extra) + " training)") if extra else ""))
     if name.startswith("artcnn"):

@@ -1,8 +1,8 @@
 """CPU oracle for the Anime4KCPP upscaling path -- TEST INFRASTRUCTURE ONLY.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` may use this package, and only as the checker or the timed CPU
-baseline.  The product library (``anime4kcpp_gb300``) never imports it.
+``bench.py`` may use this package, and only to compare results against or as the
+timed CPU baseline.  The product library (``anime4kcpp_gb300``) never imports it.
 
 Two back ends:
 
