@@ -144,10 +144,31 @@ __device__ __forceinline__ uint4 pack8_plain(const float* v)
                           tc::pack_f16x2(v[6], v[7]));
 }
 
-// PReLU on the packed 16-bit pairs: fma(a, min(x, 0), max(x, 0)) per lane
-// of each pair (slopes rounded to 16 bits), four instructions per two values.
+// A layer's PReLU slopes as four packed 16-bit pairs (rounded to nearest),
+// converted once per layer.
 template <bool BF16>
-__device__ __forceinline__ uint4 pack8_prelu(const float* v, const float* a)
+__device__ __forceinline__ void pack_slopes(const float* a, uint32_t (&s2)[4])
+{
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+    {
+        if constexpr (BF16)
+        {
+            const __nv_bfloat162 s = __floats2bfloat162_rn(a[2 * i], a[2 * i + 1]);
+            s2[i] = *reinterpret_cast<const uint32_t*>(&s);
+        }
+        else
+        {
+            const __half2 s = __floats2half2_rn(a[2 * i], a[2 * i + 1]);
+            s2[i] = *reinterpret_cast<const uint32_t*>(&s);
+        }
+    }
+}
+
+// PReLU on the packed 16-bit pairs: fma(a, min(x, 0), max(x, 0)) per lane
+// of each pair (slopes packed by pack_slopes), four instructions per two values.
+template <bool BF16>
+__device__ __forceinline__ uint4 pack8_prelu(const float* v, const uint32_t (&s2)[4])
 {
     uint32_t r[4];
 #pragma unroll
@@ -156,7 +177,7 @@ __device__ __forceinline__ uint4 pack8_prelu(const float* v, const float* a)
         if constexpr (BF16)
         {
             const __nv_bfloat162 x = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
-            const __nv_bfloat162 s = __floats2bfloat162_rn(a[2 * i], a[2 * i + 1]);
+            const __nv_bfloat162 s = *reinterpret_cast<const __nv_bfloat162*>(&s2[i]);
             const __nv_bfloat162 z = __float2bfloat162_rn(0.0f);
             const __nv_bfloat162 y = __hfma2(s, __hmin2(x, z), __hmax2(x, z));
             r[i] = *reinterpret_cast<const uint32_t*>(&y);
@@ -164,7 +185,7 @@ __device__ __forceinline__ uint4 pack8_prelu(const float* v, const float* a)
         else
         {
             const __half2 x = __floats2half2_rn(v[2 * i], v[2 * i + 1]);
-            const __half2 s = __floats2half2_rn(a[2 * i], a[2 * i + 1]);
+            const __half2 s = *reinterpret_cast<const __half2*>(&s2[i]);
             const __half2 z = __float2half2_rn(0.0f);
             const __half2 y = __hfma2(s, __hmin2(x, z), __hmax2(x, z));
             r[i] = *reinterpret_cast<const uint32_t*>(&y);
@@ -478,6 +499,9 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
             {
                 const uint32_t parity = (layers_done + static_cast<uint32_t>(l)) & 1u;
                 const LayerRange<G> R(l, ix0, ix1, iy0, iy1);
+                uint32_t slopes[4] = {0u, 0u, 0u, 0u};
+                if constexpr (NET::ACN8)
+                    if (l < LAST) pack_slopes<BF16>(P.alpha[l], slopes);
                 float* Hs = reinterpret_cast<float*>(act);  // last layer: the activations are dead once its MMAs completed
                 if constexpr (C > 1)
                 {
@@ -541,7 +565,7 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
                                 {
                                     uint4 val;
                                     if constexpr (NET::ACN8)
-                                        val = pack8_prelu<BF16>(v + 8 * kk, P.alpha[l]);
+                                        val = pack8_prelu<BF16>(v + 8 * kk, slopes);
                                     else
                                         val = pack8<BF16>(v + 8 * kk);
                                     *slot<G>(act, p) = val;
