@@ -280,10 +280,10 @@ template <typename T, int C>
 cudaError_t launch_typed(const AcnetLegacyWeights& wts, const ColourArgs& a, dim3 grid, cudaStream_t stream)
 {
     constexpr size_t bytes = smem_bytes<T, C>();
-    // one-time set-up, thread-safe (a function-local static is initialised once)
-    static const cudaError_t setup =
-        cudaFuncSetAttribute(acnet_legacy_fp32_kernel<T, C>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+    // one-time set-up per device, thread-safe
+    const cudaError_t setup = device_once([] {
+        return cudaFuncSetAttribute(acnet_legacy_fp32_kernel<T, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+    });
     if (setup != cudaSuccess) return setup;
     acnet_legacy_fp32_kernel<T, C><<<grid, THREADS, bytes, stream>>>(wts, a);
     return cudaGetLastError();

@@ -261,10 +261,10 @@ __global__ void __launch_bounds__(THREADS, 1) acnet_tc_kernel(const __grid_const
 template <typename T, bool BF16>
 cudaError_t launch_typed(const Params& p, dim3 grid, cudaStream_t stream)
 {
-    // one-time set-up, thread-safe (a function-local static is initialised once)
-    static const cudaError_t setup =
-        cudaFuncSetAttribute(acnet_tc_kernel<T, BF16>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    // one-time set-up per device, thread-safe
+    const cudaError_t setup = device_once([] {
+        return cudaFuncSetAttribute(acnet_tc_kernel<T, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    });
     if (setup != cudaSuccess) return setup;
     acnet_tc_kernel<T, BF16><<<grid, THREADS, SMEM_BYTES, stream>>>(p);
     return cudaGetLastError();
@@ -328,23 +328,31 @@ void pack_acnet_tc_weights(const AcnetLegacyWeights& w, bool bf16, std::vector<u
 // The calling host thread's status word of the tensor-core kernels (0, or 1
 // after a timed-out wait): one per thread, as the reference keeps error state
 // per calling thread (CUDAProcessor.cpp:284), so one thread's reset never
-// clears or reports another thread's timeout.
+// clears or reports another thread's timeout; and one per device, so a thread
+// that serves processors on several GPUs hands each kernel a word in its own
+// device's memory.
 namespace {
-struct StatusWord
+struct StatusWords
 {
-    int* p = nullptr;
-    ~StatusWord()
+    int* p[kMaxDevices] = {};
+    ~StatusWords()
     {
-        if (p) cudaFree(p);
+        int cur = -1;
+        cudaGetDevice(&cur);
+        for (int d = 0; d < kMaxDevices; d++)
+            if (p[d] && cudaSetDevice(d) == cudaSuccess) cudaFree(p[d]);
+        if (cur >= 0) cudaSetDevice(cur);
     }
 };
 }  // namespace
 
 int* tc_status_buffer()
 {
-    static thread_local StatusWord w;
-    if (!w.p && cudaMalloc(&w.p, sizeof(int)) == cudaSuccess) cudaMemset(w.p, 0, sizeof(int));
-    return w.p;
+    static thread_local StatusWords w;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+    if (!w.p[dev] && cudaMalloc(&w.p[dev], sizeof(int)) == cudaSuccess) cudaMemset(w.p[dev], 0, sizeof(int));
+    return w.p[dev];
 }
 
 cudaError_t launch_acnet_legacy_tc(const AcnetLegacyWeights& wts, const void* packed, bool bf16, const Plane& in,

@@ -388,10 +388,10 @@ acnet_tc2_kernel(const __grid_constant__ CUtensorMap in_map, const __grid_consta
 template <typename T, int C, bool BF16>
 cudaError_t launch_typed(const CUtensorMap& map, const Params& p, dim3 grid, cudaStream_t stream)
 {
-    // one-time set-up, thread-safe (a function-local static is initialised once)
-    static const cudaError_t setup =
-        cudaFuncSetAttribute(acnet_tc2_kernel<T, C, BF16>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, Layout<T, C>::smem);
+    // one-time set-up per device, thread-safe
+    const cudaError_t setup = device_once([] {
+        return cudaFuncSetAttribute(acnet_tc2_kernel<T, C, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, Layout<T, C>::smem);
+    });
     if (setup != cudaSuccess) return setup;
     acnet_tc2_kernel<T, C, BF16><<<grid, THREADS, Layout<T, C>::smem, stream>>>(map, p);
     return cudaGetLastError();

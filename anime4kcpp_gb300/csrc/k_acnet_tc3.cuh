@@ -554,8 +554,8 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc3_kernel(const __grid_cons
 template <class G, typename T, int C, bool BF16>
 cudaError_t launch_typed(const Params& p, int grid, int per_sm_cap, cudaStream_t stream)
 {
-    // one-time set-up, thread-safe (a function-local static is initialised once)
-    static const LaunchSetup setup = [] {
+    // one-time set-up per device, thread-safe
+    const LaunchSetup setup = device_once([] {
         cudaError_t err = cudaFuncSetAttribute(acnet_tc3_kernel<G, T, C, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                Layout<G, T, C>::smem);
         if (err != cudaSuccess) return LaunchSetup{err, 0, 0};
@@ -581,7 +581,7 @@ cudaError_t launch_typed(const Params& p, int grid, int per_sm_cap, cudaStream_t
             std::fprintf(stderr, "tc3 <%d,%d,%d>: %d CTAs per SM, %d bytes shared, %d registers\n", static_cast<int>(sizeof(T)),
                          C, BF16 ? 1 : 0, per_sm, Layout<G, T, C>::smem, fa.numRegs);
         return LaunchSetup{cudaSuccess, per_sm, 0};
-    }();
+    });
     if (setup.err != cudaSuccess) return setup.err;
     const int per_sm = setup.per_sm;
     const int k = per_sm < per_sm_cap ? per_sm : (per_sm_cap < 1 ? 1 : per_sm_cap);

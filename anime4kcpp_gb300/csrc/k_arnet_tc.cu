@@ -577,10 +577,10 @@ __global__ void __launch_bounds__(256) up_kernel(const __grid_constant__ UpParam
 template <int MODE, bool BF16>
 cudaError_t launch_conv(const ConvParams& p, int tiles, cudaStream_t stream)
 {
-    // one-time set-up, thread-safe (a function-local static is initialised once)
-    static const cudaError_t setup =
-        cudaFuncSetAttribute(conv_kernel<MODE, BF16>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_REQ);
+    // one-time set-up per device, thread-safe
+    const cudaError_t setup = device_once([] {
+        return cudaFuncSetAttribute(conv_kernel<MODE, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_REQ);
+    });
     if (setup != cudaSuccess) return setup;
     conv_kernel<MODE, BF16><<<tiles, THREADS, SMEM_REQ, stream>>>(p);
     return cudaGetLastError();
@@ -592,10 +592,10 @@ constexpr int SMEM2_REQ = SMEM2 > 48 * 1024 ? SMEM2 : 48 * 1024;  // at most fou
 template <int MODE, bool BF16>
 cudaError_t launch_conv2(const Conv2Params& p, int tiles, cudaStream_t stream)
 {
-    // one-time set-up, thread-safe (a function-local static is initialised once)
-    static const cudaError_t setup =
-        cudaFuncSetAttribute(conv2_kernel<MODE, BF16>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_REQ);
+    // one-time set-up per device, thread-safe
+    const cudaError_t setup = device_once([] {
+        return cudaFuncSetAttribute(conv2_kernel<MODE, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_REQ);
+    });
     if (setup != cudaSuccess) return setup;
     conv2_kernel<MODE, BF16><<<tiles, THREADS, SMEM2_REQ, stream>>>(p);
     return cudaGetLastError();

@@ -556,8 +556,8 @@ template <int F, int MODE, bool BF16, typename OT = uint8_t>
 cudaError_t launch_convq(const ConvPP<F>& p, cudaStream_t stream)
 {
     using G = GeoQ<F>;
-    // one-time set-up, thread-safe (a function-local static is initialised once)
-    static const LaunchSetup setup = [] {
+    // one-time set-up per device, thread-safe
+    const LaunchSetup setup = device_once([] {
         cudaError_t err =
             cudaFuncSetAttribute(convq_kernel<F, MODE, BF16, OT>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM_REQ);
         if (err != cudaSuccess) return LaunchSetup{err, 0, 0};
@@ -570,7 +570,7 @@ cudaError_t launch_convq(const ConvPP<F>& p, cudaStream_t stream)
         if (occ < 1) return LaunchSetup{cudaErrorInvalidConfiguration, 0, 0};
         const int cap = static_cast<int>(512 / G::TMEM_COLS);
         return LaunchSetup{cudaSuccess, occ < cap ? occ : cap, sms};
-    }();
+    });
     if (setup.err != cudaSuccess) return setup.err;
     const int per_sm = setup.per_sm, sms = setup.sms;
     const int grid = p.ntiles < per_sm * sms ? p.ntiles : per_sm * sms;

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstdint>
+#include <mutex>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -25,14 +26,32 @@ struct Plane
 constexpr int kAcnetKernels = 8 * 9 + 8 * 8 * 9 * 8 + 8 * 4;
 constexpr int kAcnetBiases = 8 + 8 * 8;
 // One-time launch set-up of a kernel (function attributes, CTAs per SM, SM
-// count), computed once per process by a function-local static initialiser,
-// which C++ runs exactly once even when several host threads launch at once.
+// count), computed once per device by device_once.
 struct LaunchSetup
 {
     cudaError_t err;
     int per_sm;
     int sms;
 };
+
+// Runs f once for each device it is called on (the current device) and
+// returns that device's result afterwards.  Function attributes such as the
+// dynamic shared-memory limit are per device, so a process that launches on
+// several GPUs sets them on each.  Thread-safe (std::call_once); F is the
+// call site's lambda, so every call site and template instance has its own
+// table.
+constexpr int kMaxDevices = 64;
+template <typename F>
+auto device_once(F f) -> decltype(f())
+{
+    using R = decltype(f());
+    static std::once_flag flags[kMaxDevices];
+    static R values[kMaxDevices];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return f();
+    std::call_once(flags[dev], [&] { values[dev] = f(); });
+    return values[dev];
+}
 
 struct AcnetLegacyWeights
 {
@@ -70,7 +89,8 @@ cudaError_t launch_acnet_legacy_fp32(const AcnetLegacyWeights& wts, const Plane&
 cudaError_t launch_acnet_legacy_tc(const AcnetLegacyWeights& wts, const void* packed, bool bf16, const Plane& in,
                                    const Plane& out, cudaStream_t stream);
 void pack_acnet_tc_weights(const AcnetLegacyWeights& wts, bool bf16, std::vector<uint16_t>& packed);
-// Reads and clears the tensor-core wait-timeout flag (1 = some wait gave up).
+// Reads and clears the calling thread's tensor-core wait-timeout flag on the
+// current device (1 = some wait gave up).
 int tc_status_reset();
 
 // Pair-interleaved tensor-core form.  A 1-channel input is staged by TMA and
@@ -161,6 +181,7 @@ void pack_pair_conv8(const float* k576, bool bf16, uint16_t* out /* 1536 values 
 cudaError_t launch_arnet_tc(const float* kernels, const float* biases, const float* alphas, int blocks, const void* packed,
                             bool bf16, const Plane& in, const Plane& out, void* const maps[3], int* status,
                             cudaStream_t stream);
+// The calling thread's timeout word on the current device (device memory).
 int* tc_status_buffer();
 // The same for n single-channel images at once (1 to kArnetTcMaxImages, one
 // element type, each output 2x its input): every layer is one launch over all
