@@ -105,12 +105,28 @@ _MODEL_NAMES = (
     ["fsrcnnx-f%db4%s" % (f, t) for f in (8, 16) for t in ("", "-distort-plus")])
 
 
+# Provenance of the third-party trained models whose parameters this library
+# carries (version, author, homepage), as the reference's list states it.
+_ARTCNN = ("v1.6.2", "Artoriuz", "https://github.com/Artoriuz/ArtCNN")
+_FSRCNNX = ("v1.1", "igv", "https://github.com/igv/FSRCNN-TensorFlow")
+_FSRCNNX_DP = ("v1.3_distort_plus", "nessotrin", "https://github.com/nessotrin/FSRCNN-TensorFlow")
+
+
+def _provenance(name):
+    if name.startswith("artcnn"):
+        return _ARTCNN
+    if name.startswith("fsrcnnx"):
+        return _FSRCNNX_DP if name.endswith("distort-plus") else _FSRCNNX
+    return (None, None, None)
+
+
 def _model_list():
     out = []
     for name in _MODEL_NAMES:
         k, b, a = _model_params(name)
+        version, author, homepage = _provenance(name)
         out.append({"name": name, "description": _describe(name), "parameter_count": int(k.size + b.size + a.size),
-                    "version": None, "author": None, "homepage": None})
+                    "version": version, "author": author, "homepage": homepage})
     return tuple(out)
 
 

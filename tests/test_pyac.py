@@ -42,6 +42,9 @@ def test_model_list_matches_the_reference_listing(pyac):
     ours = pyac.specs.ModelList
     assert [m["name"] for m in ours] == [m["name"] for m in ref]
     assert [m["parameter_count"] for m in ours] == [m["parameter_count"] for m in ref]
+    # third-party models carry their version, author and homepage
+    for key in ("version", "author", "homepage"):
+        assert [m[key] for m in ours] == [m[key] for m in ref], key
     for m in ours:
         assert set(m) == {"name", "description", "parameter_count", "version", "author", "homepage"}
         assert m["description"]
