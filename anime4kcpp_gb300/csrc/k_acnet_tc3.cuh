@@ -3,10 +3,17 @@
 // queue of one or many images (template over the tile geometry; the shapes
 // are instantiated in k_acnet_tc3.cu and k_acnet_tc3_shapes.cu).
 //
-// Network, clamp semantics and the pair-interleaved GEMM formulation are
-// those of k_acnet_tc2.cu (reference layer math:
-// core/internal/AC/Core/Internal/Processor/CPU/Common.hpp:116-197,344-393);
-// the fused colour prologue/epilogue that of colour.cuh.  What changes is the
+// Network and clamp semantics: the reference's layer math
+// (core/internal/AC/Core/Internal/Processor/CPU/Common.hpp:116-197,344-393),
+// every 3x3 layer reading its input map clamped to the image edge.  GEMM
+// formulation (pair-interleaved): one GEMM row = two horizontally adjacent
+// pixels, N = 2 x 8 output channels = 16, K = 3 tap rows x 4 pixels x 8
+// channels.  Activations live as two planes (even / odd pixels), 16 bytes (8
+// FP16/BF16 channels) per pixel; a K-major shared-memory descriptor whose
+// leading byte offset is the distance between the planes reads a shifted
+// view of the window for every tap row, so no im2col copy is made: six
+// M128 x N16 x K16 MMAs per 128 pairs and layer, FP32 accumulators in tensor
+// memory.  The fused colour prologue / epilogue is that of colour.cuh.  The
 // schedule:
 //
 //  * Two CTAs per SM (one activation buffer and 256 tensor-memory columns

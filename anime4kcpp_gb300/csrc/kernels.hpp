@@ -2,6 +2,7 @@
 // pointers and sizes).  All planes live in device memory.
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <mutex>
 #include <vector>
@@ -34,23 +35,36 @@ struct LaunchSetup
     int sms;
 };
 
-// Runs f once for each device it is called on (the current device) and
-// returns that device's result afterwards.  Function attributes such as the
-// dynamic shared-memory limit are per device, so a process that launches on
-// several GPUs sets them on each.  Thread-safe (std::call_once); F is the
-// call site's lambda, so every call site and template instance has its own
-// table.
+// Runs f for each device it is called on (the current device) until it
+// succeeds once, and returns that device's successful result afterwards.
+// Function attributes such as the dynamic shared-memory limit are per device,
+// so a process that launches on several GPUs sets them on each.  A failed
+// set-up is not cached: the next call on that device runs f again, so a
+// transient error does not disable the kernel for the life of the process.
+// Thread-safe (one lock per device; f runs under it); F is the call site's
+// lambda, so every call site and template instance has its own table.
 constexpr int kMaxDevices = 64;
+inline bool setup_succeeded(cudaError_t e) { return e == cudaSuccess; }
+inline bool setup_succeeded(const LaunchSetup& s) { return s.err == cudaSuccess; }
 template <typename F>
 auto device_once(F f) -> decltype(f())
 {
     using R = decltype(f());
-    static std::once_flag flags[kMaxDevices];
+    static std::mutex locks[kMaxDevices];
+    static std::atomic<bool> done[kMaxDevices];
     static R values[kMaxDevices];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return f();
-    std::call_once(flags[dev], [&] { values[dev] = f(); });
-    return values[dev];
+    if (done[dev].load(std::memory_order_acquire)) return values[dev];
+    std::lock_guard<std::mutex> lock(locks[dev]);
+    if (done[dev].load(std::memory_order_relaxed)) return values[dev];
+    const R r = f();
+    if (setup_succeeded(r))
+    {
+        values[dev] = r;
+        done[dev].store(true, std::memory_order_release);
+    }
+    return r;
 }
 
 struct AcnetLegacyWeights
@@ -82,25 +96,16 @@ struct Phase2
 cudaError_t launch_acnet_legacy_fp32(const AcnetLegacyWeights& wts, const Plane& in, const Plane& out, const Phase2* phase2,
                                      cudaStream_t stream);
 
-// Tensor-core (tcgen05) layer-fused ACNetLegacy x2 pass.  `packed` is the
-// device copy of pack_acnet_tc_weights(); bf16 selects BF16 operands
-// (FP16 otherwise).  Layer 0, the deconvolution and all element conversions
-// stay FP32.
-cudaError_t launch_acnet_legacy_tc(const AcnetLegacyWeights& wts, const void* packed, bool bf16, const Plane& in,
-                                   const Plane& out, cudaStream_t stream);
-void pack_acnet_tc_weights(const AcnetLegacyWeights& wts, bool bf16, std::vector<uint16_t>& packed);
-// Reads and clears the calling thread's tensor-core wait-timeout flag on the
-// current device (1 = some wait gave up).
+// Timeout status word of the tensor-core kernels (tc_status.cpp): the
+// calling thread's word on the current device, 0 or 1 after a bounded wait
+// gave up.  tc_status_enqueue(s) queues its copy to a pinned host slot and
+// its reset on stream s; after s synchronised, tc_status_take() returns the
+// copied value (-1 when nothing was queued).  tc_status_reset() reads and
+// clears it synchronously.
+int* tc_status_buffer();
+cudaError_t tc_status_enqueue(cudaStream_t stream);
+int tc_status_take();
 int tc_status_reset();
-
-// Pair-interleaved tensor-core form.  A 1-channel input is staged by TMA and
-// needs a 16-byte aligned plane and pitch (acnet_tc2_supported); a 3/4-channel
-// RGB(A) input runs the fused split/merge path (phase2 required) and writes
-// RGB(A) output.
-bool acnet_tc2_supported(const Plane& in);
-cudaError_t launch_acnet_legacy_tc2(const AcnetLegacyWeights& wts, const void* packed2, bool bf16, const Plane& in,
-                                    const Plane& out, const Phase2* phase2, cudaStream_t stream);
-void pack_acnet_tc2_weights(const AcnetLegacyWeights& wts, bool bf16, std::vector<uint16_t>& packed);
 
 // Persistent warp-specialised tensor-core form over a tile queue of n images
 // (same type and channel count, every output 2x its input); packed2 is the
@@ -181,8 +186,6 @@ void pack_pair_conv8(const float* k576, bool bf16, uint16_t* out /* 1536 values 
 cudaError_t launch_arnet_tc(const float* kernels, const float* biases, const float* alphas, int blocks, const void* packed,
                             bool bf16, const Plane& in, const Plane& out, void* const maps[3], int* status,
                             cudaStream_t stream);
-// The calling thread's timeout word on the current device (device memory).
-int* tc_status_buffer();
 // The same for n single-channel images at once (1 to kArnetTcMaxImages, one
 // element type, each output 2x its input): every layer is one launch over all
 // images' tiles; maps[3 i + j] are image i's three work maps.

@@ -252,7 +252,7 @@ GB300Processor::GB300Processor(int device, const ModelSpec& spec) : spec_(spec)
     if (const char* k = std::getenv("AC_GB300_TC_KERNEL"))
     {
         const int v = std::atoi(k);
-        tcKernel_ = (v >= 1 && v <= 3) ? v : 4;
+        tcKernel_ = v == 3 ? 3 : 4;
     }
     if (const char* f = std::getenv("AC_GB300_FUSED")) fused_ = std::atoi(f) != 0;
     if (const char* n = std::getenv("AC_GB300_TC3_CTAS")) tc3Ctas_ = std::atoi(n);
@@ -261,6 +261,7 @@ GB300Processor::GB300Processor(int device, const ModelSpec& spec) : spec_(spec)
     if (const char* v = std::getenv("AC_GB300_TC3_PER_SM")) tc3PerSm_ = std::atoi(v);
     if (const char* v = std::getenv("AC_GB300_AUTOTUNE")) autotune_ = std::atoi(v) != 0;
     if (const char* v = std::getenv("AC_GB300_ARNET_TC")) arnetTc_ = std::atoi(v) != 0;
+    phase2Ok_ = phase_weights(2, &phase2_.w[0][0]);
     int n = 0;
     cudaError_t err = cudaGetDeviceCount(&n);
     if (err != cudaSuccess || n == 0)
@@ -624,9 +625,9 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
                                                   tc3PerSm_ > 0 ? tc3PerSm_ : 2);
                 }
             }
-            else if (tcKernel_ == 3)
+            else
             {
-                // persistent warp-specialised form (default)
+                // persistent pair form (AC_GB300_TC_KERNEL=3), autotuned tile shapes
                 const void* w = tcWeights(precision_, 2);
                 if (!w) err = cudaErrorMemoryAllocation;
                 else if ((err = ts.counter.ensure(256)) == cudaSuccess)
@@ -640,18 +641,6 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
                         err = launch_acnet_legacy_tc3(*acnet_, w, bf16, 1, &in, &out, ph, counter,
                                                       tc3Ctas_ > 0 ? tc3Ctas_ : smCount_, stream, plan.shape, plan.perSm);
                 }
-            }
-            else
-            {
-                // The pair-interleaved form stages 1-channel input by TMA
-                // (16-byte aligned plane) and runs the fused RGB(A) path; other
-                // 1-channel planes take the one-pixel-per-row form.
-                const bool v2 = (tcKernel_ != 1 || in.channels > 1) && acnet_tc2_supported(in);
-                const void* w = tcWeights(precision_, v2 ? 1 : 0);
-                if (!w) err = cudaErrorMemoryAllocation;
-                else if (v2) err = launch_acnet_legacy_tc2(*acnet_, w, bf16, in, out, ph, stream);
-                else if (in.channels == 1) err = launch_acnet_legacy_tc(*acnet_, w, bf16, in, out, stream);
-                else err = cudaErrorInvalidValue;
             }
         }
     }
@@ -743,8 +732,7 @@ const void* GB300Processor::tcWeights(Precision p, int form)
             pack_acnet8_tc4_weights(model_params(spec_).kernels.data(), spec_.blocks, bf16, packed);
         else if (form == 3) pack_acnet_tc4_weights(*acnet_, bf16, packed);
         else if (form == 2) pack_acnet_tc3_weights(*acnet_, bf16, packed);
-        else if (form == 1) pack_acnet_tc2_weights(*acnet_, bf16, packed);
-        else pack_acnet_tc_weights(*acnet_, bf16, packed);
+        else return nullptr;
         if (deviceWeights_[idx].ensure(packed.size() * sizeof(uint16_t)) != cudaSuccess) return nullptr;
         if (cudaMemcpy(deviceWeights_[idx].ptr, packed.data(), packed.size() * sizeof(uint16_t), cudaMemcpyHostToDevice) !=
             cudaSuccess)
@@ -857,6 +845,15 @@ bool GB300Processor::validate(ThreadState& ts, int w, int h, int c, int type, do
     return true;
 }
 
+bool GB300Processor::validStride(ThreadState& ts, const DeviceImage& d, const char* which)
+{
+    const int64_t row = static_cast<int64_t>(d.w) * d.c * (d.type & 0xff);
+    if (d.stride <= 0 || static_cast<int64_t>(d.stride) < row)
+        return fail(ts, std::string(which) + ": row stride must be positive and at least one row of pixels");
+    if (static_cast<int64_t>(d.stride) * d.h > 2147483647) return fail(ts, std::string(which) + ": image too large");
+    return true;
+}
+
 // Runs the pipeline between device images.  `dst` has the final shape.
 bool GB300Processor::run(ThreadState& ts, const DeviceImage& src, const DeviceImage& dst, double factor, cudaStream_t stream)
 {
@@ -872,8 +869,8 @@ bool GB300Processor::run(ThreadState& ts, const DeviceImage& src, const DeviceIm
     if (c > 1 && power == 1 && fxy == 1.0 && dst.w == 2 * src.w && dst.h == 2 * src.h && fused_ &&
         (spec_.family == Family::ACNetLegacy || acnet8Quad()))
     {
-        Phase2 ph;
-        if (phase_weights(2, &ph.w[0][0]))
+        const Phase2& ph = phase2_;
+        if (phase2Ok_)
         {
             bool nonzero = true;
             for (int k = 0; k < 2; k++)
@@ -1012,13 +1009,15 @@ void GB300Processor::processHost(const Image& src, Image& dst, double factor)
     err = cudaMemcpy2DAsync(dst.ptr(), dst.stride(), ddst.ptr, ddst.stride, static_cast<size_t>(ow) * dst.pixelSize(), oh,
                             cudaMemcpyDeviceToHost, stream);
     if (err != cudaSuccess) { fail(ts, "device to host copy", err); return; }
+    const bool tc = precision_ != Precision::FP32;
+    if (tc && (err = tc_status_enqueue(stream)) != cudaSuccess) { fail(ts, "status read", err); return; }
     err = cudaStreamSynchronize(stream);
     if (err != cudaSuccess)
     {
         fail(ts, "kernel execution", err);
         return;
     }
-    if (precision_ != Precision::FP32 && tc_status_reset() != 0) fail(ts, "tensor-core wait timed out");
+    if (tc && tc_status_take() != 0) fail(ts, "tensor-core wait timed out");
 }
 
 int GB300Processor::processDevice(const DeviceImage& src, const DeviceImage& dst, double factor, cudaStream_t stream, bool sync)
@@ -1027,6 +1026,7 @@ int GB300Processor::processDevice(const DeviceImage& src, const DeviceImage& dst
     if (!begin(ts)) return -1;
     if (!src.ptr || !dst.ptr) return fail(ts, "null device pointer"), -1;
     if (!validate(ts, src.w, src.h, src.c, src.type, factor)) return -1;
+    if (!validStride(ts, src, "src") || !validStride(ts, dst, "dst")) return -1;
     int ow, oh;
     output_shape(src.w, src.h, src.c, factor, ow, oh);
     if (src.c == 1 && factor / static_cast<double>(1 << (factor > 2.0 ? ceil_log2(factor) : 1)) != 1.0)
@@ -1039,9 +1039,11 @@ int GB300Processor::processDevice(const DeviceImage& src, const DeviceImage& dst
     if (!run(ts, src, dst, factor, s)) return -1;
     if (sync)
     {
-        cudaError_t err = cudaStreamSynchronize(s);
-        if (err != cudaSuccess) return fail(ts, "kernel execution", err), -1;
-        if (precision_ != Precision::FP32 && tc_status_reset() != 0) return fail(ts, "tensor-core wait timed out"), -1;
+        const bool tc = precision_ != Precision::FP32;
+        cudaError_t err = tc ? tc_status_enqueue(s) : cudaSuccess;
+        if (err != cudaSuccess) return fail(ts, "status read", err), -1;
+        if ((err = cudaStreamSynchronize(s)) != cudaSuccess) return fail(ts, "kernel execution", err), -1;
+        if (tc && tc_status_take() != 0) return fail(ts, "tensor-core wait timed out"), -1;
     }
     return 0;
 }
@@ -1103,8 +1105,8 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
         cudaError_t err = ts.counter.ensure(256);
         if (err != cudaSuccess) return fail(ts, "device allocation", err), false;
         int* counter = static_cast<int*>(ts.counter.ptr) + (ts.counterSlot++ & 63);
-        Phase2 ph;
-        if (!phase_weights(2, &ph.w[0][0])) return fail(ts, "chroma resample weights"), false;
+        if (!phase2Ok_) return fail(ts, "chroma resample weights"), false;
+        const Phase2& ph = phase2_;
         const int maxImages = std::min(quad ? acnet_tc4_max_images() : acnet_tc3_max_images(), 64);
         std::vector<int> order(n);
         for (int i = 0; i < n; i++) order[i] = i;
@@ -1303,6 +1305,7 @@ int GB300Processor::processBatchDevice(int n, const DeviceImage* src, const Devi
     {
         if (!src[i].ptr || !dst[i].ptr) return fail(ts, "null device pointer"), -1;
         if (!validate(ts, src[i].w, src[i].h, src[i].c, src[i].type, factor)) return -1;
+        if (!validStride(ts, src[i], "src") || !validStride(ts, dst[i], "dst")) return -1;
         int ow, oh;
         output_shape(src[i].w, src[i].h, src[i].c, factor, ow, oh);
         if (src[i].c == 1 && factor / static_cast<double>(1 << (factor > 2.0 ? ceil_log2(factor) : 1)) != 1.0)
@@ -1316,9 +1319,11 @@ int GB300Processor::processBatchDevice(int n, const DeviceImage* src, const Devi
     if (!batchRun(ts, n, src, dst, factor, s)) return -1;
     if (sync)
     {
-        cudaError_t err = cudaStreamSynchronize(s);
-        if (err != cudaSuccess) return fail(ts, "kernel execution", err), -1;
-        if (precision_ != Precision::FP32 && tc_status_reset() != 0) return fail(ts, "tensor-core wait timed out"), -1;
+        const bool tc = precision_ != Precision::FP32;
+        cudaError_t err = tc ? tc_status_enqueue(s) : cudaSuccess;
+        if (err != cudaSuccess) return fail(ts, "status read", err), -1;
+        if ((err = cudaStreamSynchronize(s)) != cudaSuccess) return fail(ts, "kernel execution", err), -1;
+        if (tc && tc_status_take() != 0) return fail(ts, "tensor-core wait timed out"), -1;
     }
     return 0;
 }
@@ -1341,6 +1346,7 @@ int GB300Processor::processYuvDevice(int frames, int planes, const DeviceImage* 
         if (!y.ptr || !oy.ptr) return fail(ts, "null device pointer"), -1;
         if (y.c != 1 || oy.c != 1) return fail(ts, "yuv: plane 0 (Y) must have one channel"), -1;
         if (!validate(ts, y.w, y.h, 1, y.type, factor)) return -1;
+        if (!validStride(ts, y, "src Y plane") || !validStride(ts, oy, "dst Y plane")) return -1;
         int ow, oh;
         output_shape(y.w, y.h, 1, factor, ow, oh);
         if (factor / static_cast<double>(1 << (factor > 2.0 ? ceil_log2(factor) : 1)) != 1.0)
@@ -1359,6 +1365,7 @@ int GB300Processor::processYuvDevice(int frames, int planes, const DeviceImage* 
             if (a.type != y.type || b.type != y.type || a.c != b.c || a.c < 1 || a.c > 4 || a.w <= 0 || a.h <= 0 ||
                 b.w <= 0 || b.h <= 0)
                 return fail(ts, "yuv: chroma planes need Y's element type, 1 to 4 channels and a size"), -1;
+            if (!validStride(ts, a, "src chroma plane") || !validStride(ts, b, "dst chroma plane")) return -1;
         }
         ys[f] = y;
         yd[f] = oy;
@@ -1399,8 +1406,10 @@ int GB300Processor::processYuvDevice(int frames, int planes, const DeviceImage* 
     }
     if (sync)
     {
+        const bool tc = precision_ != Precision::FP32;
+        if (tc && (err = tc_status_enqueue(s)) != cudaSuccess) return fail(ts, "status read", err), -1;
         if ((err = cudaStreamSynchronize(s)) != cudaSuccess) return fail(ts, "kernel execution", err), -1;
-        if (precision_ != Precision::FP32 && tc_status_reset() != 0) return fail(ts, "tensor-core wait timed out"), -1;
+        if (tc && tc_status_take() != 0) return fail(ts, "tensor-core wait timed out"), -1;
     }
     return 0;
 }
@@ -1441,13 +1450,16 @@ int GB300Processor::processDeviceNoAlloc(int n, const DeviceImage* src, const De
             return rejected("allocation-free call: every image needs the first image's channel count and element type");
         if (a.w <= 0 || a.h <= 0 || b.w != 2 * a.w || b.h != 2 * a.h)
             return rejected("allocation-free call: every dst must be exactly 2x its src");
-        if (a.stride < a.w * c * es || b.stride < b.w * c * es) return rejected("stride smaller than a row");
-        if (static_cast<double>(b.stride) * b.h > 2147483647.0) return rejected("output image too large");
+        if (a.stride <= 0 || b.stride <= 0 || static_cast<int64_t>(a.stride) < static_cast<int64_t>(a.w) * c * es ||
+            static_cast<int64_t>(b.stride) < static_cast<int64_t>(b.w) * c * es)
+            return rejected("stride smaller than a row");
+        if (static_cast<int64_t>(b.stride) * b.h > 2147483647 || static_cast<int64_t>(a.stride) * a.h > 2147483647)
+            return rejected("image too large");
         in[i] = plane_of(a);
         out[i] = plane_of(b);
     }
-    Phase2 ph;
-    if (c > 1 && !phase_weights(2, &ph.w[0][0])) return failed("chroma resample weights");
+    if (c > 1 && !phase2Ok_) return failed("chroma resample weights");
+    const Phase2& ph = phase2_;
     const bool bf16 = precision_ == Precision::BF16;
     const void* w = nullptr;
     {

@@ -125,6 +125,10 @@ private:
     bool begin(ThreadState& ts);
     bool fail(ThreadState& ts, const std::string& what, cudaError_t err = cudaSuccess);
     bool validate(ThreadState& ts, int w, int h, int c, int type, double factor);
+    // A caller's device image: row stride positive and at least one row of
+    // w * c elements (computed in 64 bits), the last row's end addressable
+    // in the int byte offsets the kernels use.
+    bool validStride(ThreadState& ts, const DeviceImage& d, const char* which);
     bool run(ThreadState& ts, const DeviceImage& src, const DeviceImage& dst, double factor, cudaStream_t stream);
     const ResizeAxis* axis(ThreadState& ts, int n_in, int n_out, int mode, cudaStream_t stream, cudaError_t& err);
     cudaError_t luma_pass(ThreadState& ts, const Plane& in, const Plane& out, const Phase2* ph, cudaStream_t stream);
@@ -180,6 +184,10 @@ private:
     int tc3PerSm_ = 0;               // forced CTAs per SM (AC_GB300_TC3_PER_SM), 0: autotuned
     bool autotune_ = true;           // AC_GB300_AUTOTUNE=0: default shape, two CTAs per SM
     std::map<std::tuple<int, int, int, int, int, int>, Tc3Plan> plans_;
+    // x2 Catmull-Rom phase weights of the fused chroma resample, computed
+    // once at construction (the allocation-free entry must not build them)
+    Phase2 phase2_{};
+    bool phase2Ok_ = false;
     std::mutex mutex_;
     std::unordered_map<std::thread::id, std::unique_ptr<ThreadState>> states_;
 };

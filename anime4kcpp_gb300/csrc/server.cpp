@@ -458,10 +458,12 @@ void Server::workerLoop(int w)
                     e = cudaMemcpy2DAsync(h.ptr, h.stride, j->ddst[p].ptr, j->ddst[p].stride,
                                           static_cast<size_t>(h.w) * h.c * (h.type & 0xff), h.h, cudaMemcpyDeviceToHost, st);
                 }
+        const bool tc = precision_ != Precision::FP32;
+        if (tc && e == cudaSuccess) e = tc_status_enqueue(st);
         const cudaError_t se = cudaStreamSynchronize(st);
         if (e == cudaSuccess) e = se;
         if (e != cudaSuccess && err.empty()) err = std::string("CUDA: ") + cudaGetErrorString(e);
-        if (e == cudaSuccess && rc == 0 && precision_ != Precision::FP32 && tc_status_reset() != 0)
+        if (e == cudaSuccess && rc == 0 && tc && tc_status_take() != 0)
         {
             rc = -1;
             err = "tensor-core wait timed out";

@@ -86,20 +86,79 @@ def measured_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle samples during the timed region."""
+    """SM clock, power and clock-event reasons sampled DURING the timed region.
 
+    Reads them through NVML (the driver's libnvidia-ml, read-only queries)
+    every 2 ms from a background thread, so even a region of a few tens of
+    milliseconds gets samples; falls back to `nvidia-smi -lms 100` when the
+    library cannot be loaded.  Nothing here changes a GPU setting."""
+
+    # nvmlClocksEventReasons bits (nvml.h)
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
     FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
 
-    def __init__(self, device):
+    def __init__(self, device, period_s=0.002):
         self.device = device
-        self.proc = None
+        self.period = period_s
+        self.samples = []  # (sm_mhz, max_mhz, reasons bitmask)
         self.lines = []
+        self.proc = None
+        self.stop = threading.Event()
+        self.thread = None
+        self.source = None
+        self.nvml = self._nvml()
+
+    def _nvml(self):
+        import ctypes
+        try:
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return None
+            h = ctypes.c_void_p()
+            # the CUDA device by its PCI address (NVML does not follow
+            # CUDA_VISIBLE_DEVICES), else by index
+            found = False
+            try:
+                import torch
+                pr = torch.cuda.get_device_properties(self.device)
+                bus = ("%08X:%02X:%02X.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)).encode()
+                found = lib.nvmlDeviceGetHandleByPciBusId_v2(ctypes.c_char_p(bus), ctypes.byref(h)) == 0
+            except Exception:
+                found = False
+            if not found and lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.device), ctypes.byref(h)) != 0:
+                return None
+            mx = ctypes.c_uint()
+            if lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) != 0:
+                return None
+            self.max_mhz = float(mx.value)
+            return lib, h
+        except (OSError, AttributeError):
+            return None
+
+    def _poll(self):
+        import ctypes
+        lib, h = self.nvml
+        clk, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+        get_reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        while not self.stop.is_set():
+            if lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk)) == 0 and get_reasons(h, ctypes.byref(rs)) == 0:
+                self.samples.append((float(clk.value), self.max_mhz, int(rs.value)))
+            time.sleep(self.period)
 
     def __enter__(self):
+        self.stop.clear()
+        if self.nvml:
+            self.source = "nvml every %.0f ms" % (self.period * 1e3)
+            self.thread = threading.Thread(target=self._poll, daemon=True)
+            self.thread.start()
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
                                           "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.source = "nvidia-smi every 100 ms"
             threading.Thread(target=self._read, daemon=True).start()
         except Exception:
             self.proc = None
@@ -110,6 +169,9 @@ class ClockSampler:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        self.stop.set()
+        if self.thread:
+            self.thread.join(timeout=2)
         if self.proc:
             self.proc.terminate()
             try:
@@ -119,6 +181,12 @@ class ClockSampler:
 
     def summary(self):
         sm, mx, reasons = [], [], set()
+        for clk, m, bits in self.samples:
+            sm.append(clk)
+            mx.append(m)
+            for b, n in self.REASONS.items():
+                if bits & b:
+                    reasons.add(n)
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
@@ -134,7 +202,8 @@ class ClockSampler:
                     reasons.add(n)
         if not sm:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm), "reasons": sorted(reasons)}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm), "reasons": sorted(reasons),
+                "source": self.source}
 
 
 def cpu_baseline(seconds=12.0):
@@ -383,6 +452,9 @@ def time_batch(ac, torch, args):
         res[form] = {"value": out_px * steps / (ms / 1e3) / 1e6, "unit": "Mpx/s", "ms_per_batch": ms / steps,
                      "steps": steps, "launches_per_batch": (ac.launch_count() - l0) / steps,
                      "graph_replays_per_batch": (ac.graph_replays() - r0) / steps}
+        if not args.no_error_stats:
+            res[form]["error"] = dict(error_vs_fp64(dsts[0].cpu().numpy(), imgs[0], BATCH_MODEL),
+                                      sample="image 0 (%dx%d)" % (imgs[0].shape[1], imgs[0].shape[0]))
     res["fp16_over_fp32"] = res["fp16"]["value"] / res["fp32"]["value"]
     return res
 
@@ -423,6 +495,8 @@ def time_video(ac, torch, args):
         ms = e0.elapsed_time(e1) / steps
         res[form] = {"value": 8 * 7680 * 4320 / (ms / 1e3) / 1e6, "unit": "Mpx/s", "ms_per_8_frames": ms,
                      "launches_per_step": (ac.launch_count() - l0) / steps}
+        if not args.no_error_stats:
+            res[form]["error"] = video_error(outs[0][0].cpu().numpy(), frames[0][0].cpu().numpy(), "arnet-b8")
     res["fp16_over_fp32"] = res["fp16"]["value"] / res["fp32"]["value"]
     return res
 
@@ -461,6 +535,8 @@ def time_families(ac, torch, args):
                 raise RuntimeError(p.error())
             ms = e0.elapsed_time(e1) / steps
             rec[form] = {"ms_per_frame": round(ms, 4), "value": OW * OH / (ms / 1e3) / 1e6, "unit": "Mpx/s"}
+            if not args.no_error_stats:
+                rec[form]["error"] = error_vs_fp64(dst.cpu().numpy(), x, model)
         if has_tc:
             rec["fp16_over_fp32"] = rec["fp16"]["value"] / rec["fp32"]["value"]
         out[model] = rec
@@ -504,6 +580,8 @@ def time_cli_default(ac, torch, args):
             raise RuntimeError(p.error())
         ms = e0.elapsed_time(e1) / steps
         out[form] = {"ms_per_step": round(ms, 4), "value": 8 * OW * OH / (ms / 1e3) / 1e6, "unit": "Mpx/s"}
+        if not args.no_error_stats:
+            out[form]["error"] = dict(error_vs_fp64(dsts[0].cpu().numpy(), frames[0], CLI_MODEL), sample="frame 0")
     out["fp16_over_fp32"] = out["fp16"]["value"] / out["fp32"]["value"]
     return out
 
@@ -673,6 +751,81 @@ def time_serve_saturation(ac, torch, args):
             "failed": int(sum(1 for x in lats if x[2] != 0))}
 
 
+def error_vs_fp64(got, img, model):
+    """Error statistics of one result against the FP64 oracle of the same
+    path (the luma network in FP64, every other step at the reference's
+    rounding points): max_abs, psnr_db, max_lsb, frac_within_1lsb.  Checker
+    use of the oracle, outside every timed region."""
+    import oracle
+    exact, quant = oracle.pipeline_f64(img, model)
+    st = oracle.error_stats(got, exact, quant)
+    return {k: (round(v, 7) if isinstance(v, float) else v) for k, v in st.items()}
+
+
+def video_error(got10, y10, model, shift=6):
+    """Error of one x4 video frame's Y plane (10-bit content in u16) against
+    the FP64 oracle at the reference CLI's rounding points: Y << shift, two
+    FP64 x2 passes with the intermediate quantised to u16 (fromFloat), the
+    result through fromFloat and >> shift.  In 10-bit LSB: max_lsb and
+    frac_within_1lsb against that quantised output; psnr_db on the 10-bit
+    grid (peak 1023) against it."""
+    import oracle
+    y16 = (y10.astype(np.uint32) << shift).astype(np.uint16)
+    p1 = oracle.process_f64(y16, model)
+    p2 = oracle.process_f64(oracle.from_float_np(p1, np.uint16), model)
+    q10 = (oracle.from_float_np(p2, np.uint16) >> shift).astype(np.int64)
+    d = got10.astype(np.int64) - q10
+    mse = float(np.mean((d / 1023.0) ** 2))
+    exact10 = np.clip(p2, 0.0, 1.0) * 65535.0 / (1 << shift)
+    return {"max_abs": round(float(np.abs(got10 + 0.5 - exact10).max() / 1023.0), 7),
+            "psnr_db": 99.0 if mse == 0 else round(10 * np.log10(1.0 / mse), 3),
+            "max_lsb": int(np.abs(d).max()), "frac_within_1lsb": round(float((np.abs(d) <= 1).mean()), 7),
+            "samples": int(d.size), "sample": "frame 0 Y plane, 10-bit LSB; psnr against the quantised FP64 oracle"}
+
+
+PREC_MODEL = "acnet-legacy-hdn3"
+
+
+def time_precision(ac, torch, args):
+    """The precision workload: one 3840x2160 RGB u8 frame (256 Voronoi cells)
+    x2 to 7680x4320 with ACNetLegacy HDN3 in the FP16, BF16 and FP32 forms,
+    and one 1920x1080 f32 luma plane (uniform [0, 1] cell values plus the
+    outline structure) x2 with HDN3; each timed (inputs resident in HBM, one
+    launch per frame, CUDA events on the launching stream) and checked
+    against the FP64 oracle."""
+    from anime4kcpp_gb300 import synthetic
+    out = {"workload": "3840x2160 RGB u8 (256 cells) -> 7680x4320 and 1920x1080 f32 luma -> 3840x2160, "
+                       "ACNetLegacy HDN3 x2, FP16 / BF16 / FP32"}
+    stream = torch.cuda.Stream()
+    h = stream.cuda_stream
+    cases = [("rgb_4k_u8", synthetic.rgb_u8(2160, 3840, cells=256, seed=2160), (4320, 7680, 3), torch.uint8),
+             ("luma_1080p_f32", synthetic.f32_luma_uniform(1080, 1920, seed=1081), (2160, 3840), torch.float32)]
+    for name, img, oshape, odt in cases:
+        src = torch.from_numpy(img).cuda()
+        dst = torch.empty(oshape, dtype=odt, device="cuda")
+        rec = {}
+        for form in ("fp16", "bf16", "fp32"):
+            p = ac.Processor("cuda", 0, PREC_MODEL, precision=form)
+            for _ in range(2):
+                p.process_device(src, dst, 2.0, stream=h, sync=False)
+            torch.cuda.synchronize()
+            steps = max(3, args.precision_steps)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                p.process_device(src, dst, 2.0, stream=h, sync=False)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if not p.ok():
+                raise RuntimeError(p.error())
+            ms = e0.elapsed_time(e1) / steps
+            rec[form] = {"ms_per_frame": round(ms, 4), "value": oshape[0] * oshape[1] / (ms / 1e3) / 1e6,
+                         "unit": "Mpx/s", "error": error_vs_fp64(dst.cpu().numpy(), img, PREC_MODEL)}
+        rec["fp16_over_fp32"] = rec["fp16"]["value"] / rec["fp32"]["value"]
+        out[name] = rec
+    return out
+
+
 def run_gb300(args, rank, world, local_rank):
     import torch
 
@@ -713,6 +866,9 @@ def run_gb300(args, rank, world, local_rank):
             psteps = max(3, steps // 2)
             rec["per_frame_launch"] = {"value": OW * OH * frames * psteps / (pms / 1e3) / 1e6, "ms_per_step": pms / psteps,
                                        "launches": plaunches, "kernel_ms_per_launch": pprof[0] / max(pprof[1], 1)}
+        if not args.no_error_stats:
+            torch.cuda.synchronize()
+            rec["error"] = error_vs_fp64(dsts[0].cpu().numpy(), host[0], MODEL)
         forms[form] = rec
         if is_head:
             headline = (form, proc, rec, sampler)
@@ -762,6 +918,10 @@ def run_gb300(args, rank, world, local_rank):
         "vs_baseline": None, "dtype": "f32" if form == "fp32" else ("f16" if form == "fp16" else "bf16"),
         "data": DATA,
         "config": {"workload": WORKLOAD, "frames_per_step": frames, "form": form, "launch": rec["launch"],
+                   "value_is": ("the %d frames of a step as ONE persistent launch (batch entry point); one launch per "
+                                "frame is value_per_frame_launch" % frames) if "per_frame_launch" in rec else
+                               "one launch per frame",
+                   "value_per_frame_launch": rec.get("per_frame_launch", {}).get("value"),
                    "l2": "inputs larger than L2: 2 alternating batches of 8 distinct frames (50 MB in, 200 MB out per step)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_value, "unit": "Mpx/s", "h2d_bytes_per_step": H * W * 3 * frames,
@@ -774,8 +934,13 @@ def run_gb300(args, rank, world, local_rank):
         for tc in ("fp16", "bf16"):
             if tc in forms and "value" in forms[tc]:
                 out["%s_over_fp32" % tc] = forms[tc]["value"] / forms["fp32"]["value"]
+    if "error" in rec:
+        out["error"] = dict(rec["error"], oracle="FP64 network, reference rounding points (oracle.pipeline_f64)",
+                            sample="frame 0 of the step, 1920x1080 RGB u8 x2")
     clocks = sampler.summary() if sampler else None
     out["clocks"] = clocks
+    if rank == 0 and world == 1 and args.precision_steps > 0:
+        out["precision"] = time_precision(ac, torch, args)
     if rank == 0 and world == 1 and not args.no_batch:
         out["batch"] = time_batch(ac, torch, args)
     if rank == 0 and world == 1 and args.video_steps > 0:
@@ -805,6 +970,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-image batching workload")
+    ap.add_argument("--no-error-stats", action="store_true", help="skip the FP64-oracle error statistics")
+    ap.add_argument("--precision-steps", type=int, default=5, help="frames per form of the precision workload (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=12)
     ap.add_argument("--video-steps", type=int, default=4, help="8-frame steps of the video workload (0: skip)")
     ap.add_argument("--family-steps", type=int, default=10, help="frames per family and form in the families workload (0: skip)")

@@ -103,7 +103,9 @@ AC_C_API int ac_gb300_process_yuv_device(ACProcessor* processor, int frames, int
  * capture.  Calls that overlap in time on one device share the scratch and
  * race: serialise them (one stream, or events).  `stream` NULL is the legacy
  * default stream.  With sync != 0 the call waits and reports a timed-out
- * tensor-core wait as AC_ERROR(AC_EPROCESSOR). */
+ * tensor-core wait as AC_ERROR(AC_EPROCESSOR).  With sync == 0 a timeout is
+ * not reported: the status word lives in the shared scratch and the next
+ * call clears it, so a caller that needs the outcome passes sync != 0. */
 AC_C_API int ac_gb300_process_device_noalloc(ACProcessor* processor, int count, const ACGB300DeviceImage* src,
                                              const ACGB300DeviceImage* dst, void* stream, int sync);
 

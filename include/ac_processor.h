@@ -10,11 +10,16 @@
  * ac_processor_ok() is AC_ERROR(AC_EPROCESSOR) and whose ac_processor_error()
  * says why.
  *
- * Models: "acnet-legacy-gan", "acnet-legacy-hdn0".."-hdn3" (trained
- * parameters of the reference) and "arnet-[hdn-][box-]b8|b16|b32|b64"
- * (ARNet<8> topology with seeded synthetic parameters; the reference's trained
- * ARNet parameters are not available).  Model strings are parsed like
- * core/src/processor/Processor.cpp:26-187.
+ * Models (the reference's model strings, parsed like
+ * core/src/processor/Processor.cpp:26-187):
+ *   "acnet-legacy-gan", "acnet-legacy-hdn0".."-hdn3"      ACNetLegacy
+ *   "acnet-f8b4|b8|b18[-hdn][-box][-box-hdn]"             ACNet<8>
+ *   "artcnn-c4f16|c4f32[-dn|-ds]"                         ArtCNN<16/32>
+ *   "fsrcnnx-f8|f16[-dp]"                                 FSRCNNX<8/16>
+ *   "arnet-[hdn-][box-]b8|b16|b32|b64"                    ARNet<8>
+ * ACNetLegacy, ACNet<8>, ArtCNN and FSRCNNX run the reference's trained
+ * parameters; ARNet runs its exact topology with seeded synthetic parameters
+ * (the reference's trained ARNet parameters are not in its source tree).
  */
 #ifndef AC_GB300_PROCESSOR_H
 #define AC_GB300_PROCESSOR_H

@@ -62,6 +62,7 @@ def lib():
             L.orc_arnet_x2_f64.argtypes = [vp, i, i, i, i, dp, fp, fp, fp, i, i]
             L.orc_acnet8_x2.argtypes = [vp, i, i, i, i, vp, i, fp, fp, fp, i, i]
             L.orc_acnet8_x2_f64.argtypes = [vp, i, i, i, i, dp, fp, fp, fp, i, i]
+            L.orc_f3_x2_f64.argtypes = [vp, i, i, i, i, dp, fp, fp, fp, i, i, i, i]
             L.orc_artcnn_x2.argtypes = [vp, i, i, i, i, vp, i, fp, fp, i, i, i]
             L.orc_fsrcnnx_x2.argtypes = [vp, i, i, i, i, vp, i, fp, fp, fp, i, i, i]
             L.orc_rgb2yuv.argtypes = [vp, i, i, i, i, i, vp, i, vp, i]
@@ -71,7 +72,7 @@ def lib():
             L.orc_resize_coeffs.argtypes = [i, i, i, vp, vp, i]
             L.orc_arnet_synth.argtypes = [i, ctypes.c_uint64, fp, fp, fp]
             for fn in ("orc_acnet_legacy_x2", "orc_acnet_legacy_x2_f64", "orc_arnet_x2", "orc_arnet_x2_f64",
-                       "orc_acnet8_x2", "orc_acnet8_x2_f64", "orc_artcnn_x2", "orc_fsrcnnx_x2",
+                       "orc_acnet8_x2", "orc_acnet8_x2_f64", "orc_f3_x2_f64", "orc_artcnn_x2", "orc_fsrcnnx_x2",
                        "orc_rgb2yuv", "orc_yuv2rgb", "orc_resize", "orc_resize_mt", "orc_resize_coeffs", "orc_arnet_synth"):
                 getattr(L, fn).restype = ctypes.c_int
             _lib = L
@@ -238,6 +239,10 @@ def luma_x2(y, model, threads=0, f64=False):
         elif fam == "acnet8":
             k, b, a = acnet8_weights(*var)
             rc = lib().orc_acnet8_x2_f64(_p(y), w, h, y.strides[0], t, _p(out), _p(k), _p(b), _p(a), var[0], threads)
+        elif fam in ("artcnn", "fsrcnnx"):
+            k, b, a = f3_weights(fam, *var)
+            rc = lib().orc_f3_x2_f64(_p(y), w, h, y.strides[0], t, _p(out), _p(k), _p(b), _p(a),
+                                     1 if fam == "artcnn" else 2, var[0], 4, threads)
         else:
             k, b, a = arnet_weights(*var)
             rc = lib().orc_arnet_x2_f64(_p(y), w, h, y.strides[0], t, _p(out), _p(k), _p(b), _p(a), var[0], threads)
@@ -345,6 +350,80 @@ def process_f64(img, model, threads=0):
     """One x2 pass of the network in FP64 over a luma plane; returns the
     unquantised, unsaturated (2H, 2W) float64 output."""
     return luma_x2(img, model, threads, f64=True)
+
+
+_MAXV = {np.dtype(np.uint8): 255.0, np.dtype(np.uint16): 65535.0, np.dtype(np.float32): 1.0}
+
+
+def from_float_np(v, dtype):
+    """fromFloat<T> (Util.hpp:64-78) in numpy: saturate to [0, 1]; integer
+    types scale by their maximum, add 0.5 and truncate; f32 is only
+    saturated."""
+    dtype = np.dtype(dtype)
+    s = np.clip(v, 0.0, 1.0)
+    if dtype == np.float32:
+        return s.astype(np.float32)
+    return np.floor(s * _MAXV[dtype] + 0.5).astype(dtype)
+
+
+def pipeline_f64(img, model, threads=0):
+    """The x2 path of Processor::process (Processor.cpp:199-276) with the luma
+    network evaluated in FP64 (process_f64) and every other step as the
+    reference does it: rgb2yuv quantised to the source type, chroma resized
+    by the Catmull-Rom restatement, yuv2rgb.
+
+    Returns (exact, quantised):
+      exact      float64 output in units of the type's full scale (u8: /255),
+                 the network's value saturated like fromFloat but not rounded,
+                 the colour merge computed in FP64 on it, saturated;
+      quantised  the output the reference's own path would give if its
+                 network arithmetic were exact: the FP64 luma through fromFloat
+                 to the source type, then yuv2rgb (the reference's rounding
+                 points)."""
+    img = _plane(img)
+    if img.ndim == 3 and img.shape[2] == 1:
+        img = img[:, :, 0]
+    maxv = _MAXV[img.dtype]
+    if img.ndim == 2:
+        y64 = process_f64(img, model, threads)
+        return np.clip(y64, 0.0, 1.0), from_float_np(y64, img.dtype)
+    h, w, c = img.shape
+    y, uv = rgb2yuv(img)
+    y64 = process_f64(y, model, threads)
+    uv2 = resize(uv, 2 * w, 2 * h, threads=threads)
+    quant = yuv2rgb(from_float_np(y64, img.dtype), uv2)
+    yy = np.clip(y64, 0.0, 1.0)
+    u = uv2[:, :, 0].astype(np.float64) / maxv - 0.5
+    v = uv2[:, :, 1].astype(np.float64) / maxv - 0.5
+    rgb = np.stack([yy + 1.403 * v, yy - 0.344 * u - 0.714 * v, yy + 1.773 * u], axis=-1)
+    if c == 4:
+        a = uv2[:, :, 2].astype(np.float64) / maxv
+        safe = np.where(a > 1e-6, a, 1.0)
+        rgb = np.where((a > 1e-6)[:, :, None], rgb / safe[:, :, None], 0.0)
+        rgb = np.concatenate([rgb, a[:, :, None]], axis=-1)
+    return np.clip(rgb, 0.0, 1.0), quant
+
+
+def error_stats(got, exact, quantised):
+    """Error of a result against the FP64 oracle (pipeline_f64):
+
+      max_abs           largest |result - exact| in full-scale units
+      psnr_db           10 log10(1 / mean squared error), peak 1.0
+      max_lsb           largest |result - quantised| in the type's LSB
+                        (integer types; for f32 the same in units of 1e-4)
+      frac_within_1lsb  share of samples with |result - quantised| <= 1 LSB
+                        (f32: <= 1e-4)"""
+    got = np.asarray(got)
+    if got.dtype == np.float32:
+        g = got.astype(np.float64)
+        dq = np.abs(g - quantised.astype(np.float64)) / 1e-4
+    else:
+        g = got.astype(np.float64) / _MAXV[got.dtype]
+        dq = np.abs(got.astype(np.int64) - quantised.astype(np.int64)).astype(np.float64)
+    e = g - exact
+    mse = float(np.mean(e * e))
+    return {"max_abs": float(np.abs(e).max()), "psnr_db": 99.0 if mse == 0 else float(10 * np.log10(1.0 / mse)),
+            "max_lsb": float(dq.max()), "frac_within_1lsb": float((dq <= 1.0).mean()), "samples": int(got.size)}
 
 
 # ----------------------------------------------------- the reference itself

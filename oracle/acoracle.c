@@ -906,6 +906,165 @@ int orc_acnet8_x2_f64(const void* src, int w, int h, int sstride, int type,
     return 0;
 }
 
+/* ----------------------------- FP64 twins of ArtCNN<F> and FSRCNNX<F> */
+
+/* Same layer sequence as orc_artcnn_x2 / orc_fsrcnnx_x2, every map and sum in
+ * double; dst receives the (2h) x (2w) unquantised, unsaturated output. */
+typedef struct {
+    const void* src; int w, h, sstride, type;
+    const double* in; double* out; int cin, cout, K;
+    const float* k; const float* b; int act; const float* alphas;
+    const double* id;                  /* residual: out = act(conv) + id */
+    const float* k2; const float* b2; const float* a2; const double* feat;  /* FSRCNNX tail */
+    double* dst;
+} gd_ctx;
+static void gd_head_rows(void* p, int y0, int y1)
+{
+    gd_ctx* c = (gd_ctx*)p;
+    const int K = c->K, R = K / 2;
+    for (int y = y0; y < y1; y++)
+        for (int x = 0; x < c->w; x++)
+        {
+            double r[25];
+            for (int i = 0; i < K; i++)
+            {
+                int yy = y + i - R;
+                yy = yy < 0 ? 0 : (yy > c->h - 1 ? c->h - 1 : yy);
+                for (int j = 0; j < K; j++)
+                {
+                    int xx = x + j - R;
+                    xx = xx < 0 ? 0 : (xx > c->w - 1 ? c->w - 1 : xx);
+                    r[i * K + j] = to_double(rowp(c->src, c->sstride, yy), (size_t)xx, c->type);
+                }
+            }
+            double* o = c->out + ((size_t)y * c->w + x) * c->cout;
+            for (int n = 0; n < c->cout; n++)
+            {
+                double s = 0.0;
+                for (int t = 0; t < K * K; t++) s += r[t] * (double)c->k[n * K * K + t];
+                o[n] = act_d(s + (double)c->b[n], c->act, c->alphas, n);
+            }
+        }
+}
+static void gd_conv_sum(const gd_ctx* c, int x, int y, double* s)
+{
+    int xs[3], ys[3];
+    taps3x3(x, y, c->w, c->h, xs, ys);
+    for (int n = 0; n < c->cout; n++)
+    {
+        double acc = 0.0;
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++)
+            {
+                const double* rp = c->in + ((size_t)ys[i] * c->w + xs[j]) * c->cin;
+                const float* kp = c->k + (size_t)n * c->cin * 9 + (size_t)(i * 3 + j) * c->cin;
+                for (int ch = 0; ch < c->cin; ch++) acc += rp[ch] * (double)kp[ch];
+            }
+        s[n] = acc + (double)c->b[n];
+    }
+}
+static void gd_conv_rows(void* p, int y0, int y1)
+{
+    gd_ctx* c = (gd_ctx*)p;
+    double s[32];
+    for (int y = y0; y < y1; y++)
+        for (int x = 0; x < c->w; x++)
+        {
+            gd_conv_sum(c, x, y, s);
+            size_t off = ((size_t)y * c->w + x) * c->cout;
+            for (int n = 0; n < c->cout; n++)
+            {
+                double v = act_d(s[n], c->act, c->alphas, n);
+                if (c->id) v += c->id[off + n];
+                c->out[off + n] = v;
+            }
+        }
+}
+static void gd_tail_rows(void* p, int y0, int y1)
+{
+    gd_ctx* c = (gd_ctx*)p;
+    double s[32];
+    for (int y = y0; y < y1; y++)
+        for (int x = 0; x < c->w; x++)
+        {
+            gd_conv_sum(c, x, y, s);
+            for (int n = 0; n < c->cout; n++) s[n] = act_d(s[n], ACT_PRELU, c->alphas, n);
+            size_t off = ((size_t)y * c->w + x) * c->cout;
+            for (int n = 0; n < c->cout; n++)
+            {
+                double acc = 0.0;
+                for (int i = 0; i < c->cout; i++) acc += s[i] * (double)c->k2[n * c->cout + i];
+                acc += (double)c->b2[n] + c->feat[off + n];
+                c->out[off + n] = act_d(acc, ACT_PRELU, c->a2, n);
+            }
+        }
+}
+static void gd_shuffle_rows(void* p, int y0, int y1)
+{
+    gd_ctx* c = (gd_ctx*)p;
+    double s[4];
+    for (int y = y0; y < y1; y++)
+        for (int x = 0; x < c->w; x++)
+        {
+            gd_conv_sum(c, x, y, s);
+            for (int n = 0; n < 4; n++) c->dst[(size_t)(2 * y + (n >> 1)) * (2 * c->w) + 2 * x + (n & 1)] = s[n];
+        }
+}
+
+/* family 1: ArtCNN<F> (orc_artcnn_x2's order), 2: FSRCNNX<F> (orc_fsrcnnx_x2's). */
+int orc_f3_x2_f64(const void* src, int w, int h, int sstride, int type, double* dst, const float* kernels,
+                  const float* biases, const float* alphas, int family, int F, int blocks, int threads)
+{
+    if (!src || !dst || w <= 0 || h <= 0 || F < 1 || F > 32 || (family != 1 && family != 2)) return -22;
+    if (family == 1 ? blocks < 1 : blocks < 2) return -22;
+    size_t n = (size_t)w * h * F;
+    double* feat = (double*)malloc(n * sizeof(double));
+    double* a = (double*)malloc(n * sizeof(double));
+    double* b = (double*)malloc(n * sizeof(double));
+    if (!feat || !a || !b) { free(feat); free(a); free(b); return -12; }
+    const int K = family == 1 ? 3 : 5;
+    gd_ctx c;
+    memset(&c, 0, sizeof(c));
+    c.src = src; c.w = w; c.h = h; c.sstride = sstride; c.type = type; c.dst = dst;
+    c.out = feat; c.cout = F; c.K = K; c.k = kernels; c.b = biases; c.act = ACT_IDENTITY;
+    parallel_rows(gd_head_rows, &c, h, threads);
+    const double* in = feat;
+    const float* kl = kernels + F * K * K;
+    int l = 1;
+    c.cin = F; c.cout = F;
+    if (family == 1)
+    {
+        for (int i = 0; i < blocks; i++, l++)
+        {
+            c.in = in; c.out = a; c.k = kl + (size_t)F * F * 9 * (l - 1); c.b = biases + F * l; c.act = ACT_RELU; c.id = NULL;
+            parallel_rows(gd_conv_rows, &c, h, threads);
+            in = a; double* t = a; a = b; b = t;
+        }
+        c.in = in; c.out = a; c.k = kl + (size_t)F * F * 9 * (l - 1); c.b = biases + F * l; c.act = ACT_IDENTITY; c.id = feat;
+        parallel_rows(gd_conv_rows, &c, h, threads);
+        in = a; l++;
+        c.in = in; c.cout = 4; c.k = kl + (size_t)F * F * 9 * (l - 1); c.b = biases + F * l;
+    }
+    else
+    {
+        for (; l < blocks; l++)
+        {
+            c.in = in; c.out = a; c.k = kl + (size_t)F * F * 9 * (l - 1); c.b = biases + F * l; c.act = ACT_PRELU;
+            c.alphas = alphas + F * (l - 1); c.id = NULL;
+            parallel_rows(gd_conv_rows, &c, h, threads);
+            in = a; double* t = a; a = b; b = t;
+        }
+        c.in = in; c.out = a; c.k = kl + (size_t)F * F * 9 * (l - 1); c.b = biases + F * l; c.alphas = alphas + F * (l - 1);
+        c.k2 = kl + (size_t)F * F * 9 * blocks; c.b2 = biases + F * (l + 1); c.a2 = alphas + F * l; c.feat = feat;
+        parallel_rows(gd_tail_rows, &c, h, threads);
+        in = a; l += 2;
+        c.in = in; c.cout = 4; c.k = kl + (size_t)F * F * 9 * blocks + F * F; c.b = biases + F * l;
+    }
+    parallel_rows(gd_shuffle_rows, &c, h, threads);
+    free(feat); free(a); free(b);
+    return 0;
+}
+
 /* ------------------------------------------------------ colour conversion */
 
 /* rgb2yuv (ImageProcess.cpp:39-61) / rgba2yuva (:114-138): interleaved

@@ -4,7 +4,8 @@ includes the header, supplies its own ``cudaGetDevice`` (a thread-local
 device index) and calls one set-up site from many threads on several
 "devices".  Each device's set-up must run exactly once and every caller on
 that device must get that device's result; an index beyond the table runs
-the set-up on every call."""
+the set-up on every call; a set-up that fails is not cached (device 5's
+first two attempts fail, the third succeeds and is kept)."""
 import os
 import shutil
 import subprocess
@@ -35,8 +36,9 @@ static std::atomic<int> runs[128];
 static acgb::LaunchSetup site()
 {
     return acgb::device_once([] {
-        runs[tls_dev]++;
+        const int n = ++runs[tls_dev];
         std::this_thread::yield();
+        if (tls_dev == 5 && n <= 2) return acgb::LaunchSetup{cudaErrorInvalidValue, 0, 0};
         return acgb::LaunchSetup{cudaSuccess, 10 * tls_dev + 1, tls_dev};
     });
 }
@@ -59,8 +61,17 @@ int main()
     tls_dev = 100;
     for (int i = 0; i < 3; i++)
         if (site().sms != 100) bad++;
-    std::printf("%d %d %d %d %d %d\n", bad.load(), runs[0].load(), runs[1].load(), runs[2].load(), runs[3].load(),
-                runs[100].load());
+    // a failing set-up is retried on the next call, a success then kept
+    tls_dev = 5;
+    int fails = 0;
+    for (int i = 0; i < 6; i++)
+    {
+        const acgb::LaunchSetup s = site();
+        if (s.err != cudaSuccess) fails++;
+        else if (s.per_sm != 51) bad++;
+    }
+    std::printf("%d %d %d %d %d %d %d %d\n", bad.load(), runs[0].load(), runs[1].load(), runs[2].load(), runs[3].load(),
+                runs[100].load(), runs[5].load(), fails);
     return 0;
 }
 """
@@ -74,7 +85,8 @@ def test_device_once_runs_once_per_device(tmp_path):
     src.write_text(PROGRAM)
     subprocess.check_call(["g++", "-std=c++17", "-O1", "-pthread", "-I" + CSRC, "-I" + CUDA_INC, str(src), "-o", str(exe)])
     out = subprocess.check_output([str(exe)], text=True).split()
-    bad, r0, r1, r2, r3, r100 = map(int, out)
+    bad, r0, r1, r2, r3, r100, r5, fails5 = map(int, out)
     assert bad == 0
     assert (r0, r1, r2, r3) == (1, 1, 1, 1)
     assert r100 == 3
+    assert (r5, fails5) == (3, 2)

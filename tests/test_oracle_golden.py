@@ -57,3 +57,25 @@ def test_catmull_rom_x2_weights_are_exact():
     assert np.allclose(even, [-0.0234375, 0.2265625, 0.8671875, -0.0703125], atol=0)
     assert np.allclose(odd, [-0.0703125, 0.8671875, 0.2265625, -0.0234375], atol=0)
     assert first[4] == 0 and first[5] == 1
+
+
+X2_CASES = [c for c in META if c["factor"] == 2.0]
+
+
+@pytest.mark.parametrize("case", X2_CASES, ids=[c["name"] for c in X2_CASES])
+def test_fp64_oracle_agrees_with_reference(case):
+    """The FP64 twin of every network (oracle.pipeline_f64, the error
+    statistics' reference) quantised at the reference's rounding points is
+    within the reference's own ISA spread of the reference's output: 1 LSB
+    on integer outputs, 1e-4 on f32."""
+    x = GOLD[case["name"] + "/in"]
+    want = GOLD[case["name"] + "/generic"]
+    exact, quant = oracle.pipeline_f64(x, case["model"], threads=2)
+    assert quant.shape == want.shape
+    d = np.abs(quant.astype(np.float64) - want.astype(np.float64))
+    if case["dtype"] == "float32":
+        assert d.max() <= 1e-4
+    else:
+        assert d.max() <= 1
+    st = oracle.error_stats(want, exact, quant)
+    assert st["frac_within_1lsb"] == 1.0
