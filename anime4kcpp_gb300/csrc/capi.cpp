@@ -285,7 +285,7 @@ const char* ac_processor_info(int processor_type)
     {
     case AC_PROCESSOR_CPU:
     case AC_PROCESSOR_OPENCL:
-    case AC_PROCESSOR_CUDA: return acgb::Processor::info(processor_type);
+    case AC_PROCESSOR_CUDA: return acgb::processor_info(processor_type);
     default: return "unsupported processor";
     }
 }

@@ -133,3 +133,33 @@ int acgb_image_op(int op, const acgb::Image& src, acgb::Image& dst, double fx, d
     dst = out;
     return AC_SUCCESS;
 }
+
+// ------------------------------------------- ac::core image operations
+
+namespace ac::core {
+
+void rgb2yuv(const Image& rgb, Image& yuv) { acgb_image_op(1, rgb, yuv, 0.0, 0.0, 0); }
+void rgba2yuva(const Image& rgba, Image& yuva) { acgb_image_op(2, rgba, yuva, 0.0, 0.0, 0); }
+void yuv2rgb(const Image& yuv, Image& rgb) { acgb_image_op(3, yuv, rgb, 0.0, 0.0, 0); }
+void yuva2rgba(const Image& yuva, Image& rgba) { acgb_image_op(4, yuva, rgba, 0.0, 0.0, 0); }
+
+void resize(const Image& src, Image& dst, double fx, double fy, int mode) noexcept
+{
+    try
+    {
+        acgb_image_op(0, src, dst, fx, fy, mode);
+    }
+    catch (...)
+    {
+    }
+}
+
+Image resize(const Image& src, double fx, double fy, int mode) noexcept
+{
+    if (!(fx > 0.0) || !(fy > 0.0)) return src;
+    Image dst;
+    resize(src, dst, fx, fy, mode);
+    return dst;
+}
+
+}  // namespace ac::core

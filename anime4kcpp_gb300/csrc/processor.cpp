@@ -162,15 +162,30 @@ void DeviceBuffer::release()
 
 // ------------------------------------------------------------ Processor
 
+}  // namespace acgb
+
+// ---------------------------------------------------- ac::core::Processor
+
+namespace ac::core {
+
+Processor::Processor() noexcept = default;
+Processor::~Processor() = default;
+
 Image Processor::process(const Image& src, double factor)
 {
     Image dst{};
-    process(src, dst, factor);
+    processPath(src, dst, factor);
     return dst;
 }
 
-void Processor::process(const Image& src, Image& dst, double factor) { processHost(src, dst, factor); }
+void Processor::process(const Image& src, Image& dst, double factor) { processPath(src, dst, factor); }
 
+bool Processor::ok() noexcept { return true; }
+const char* Processor::error() noexcept { return "NO ERROR"; }
+
+}  // namespace ac::core
+
+namespace acgb {
 namespace {
 
 class UnavailableProcessor final : public Processor
@@ -187,7 +202,7 @@ public:
     }
 
 protected:
-    void processHost(const Image&, Image&, double) override {}
+    void processPath(const Image&, Image&, double) override {}
 
 private:
     int type_;
@@ -208,22 +223,9 @@ int find_processor_type(const char* type)
 
 }  // namespace
 
-std::shared_ptr<Processor> Processor::create(const char* type, int device, const char* model)
+const char* processor_info(int type)
 {
-    int t = find_processor_type(type);
-    if (t == CPU)
-        return std::make_shared<UnavailableProcessor>(CPU, "the GB300 backend provides no CPU processor; use type \"cuda\"");
-    if (t == OpenCL)
-        return std::make_shared<UnavailableProcessor>(OpenCL, "the GB300 backend provides no OpenCL processor; use type \"cuda\"");
-    ModelSpec spec;
-    std::string err;
-    if (!parse_model(model, spec, err)) return std::make_shared<UnavailableProcessor>(CUDA, err);
-    return std::make_shared<GB300Processor>(t == -1 ? -1 : device, spec);
-}
-
-const char* Processor::info(int type)
-{
-    if (type != CUDA) return "not provided by the GB300 backend\n";
+    if (type != Processor::CUDA) return "not provided by the GB300 backend\n";
     static std::string text = []() {
         std::ostringstream os;
         int n = 0;
@@ -242,7 +244,84 @@ const char* Processor::info(int type)
     return text.c_str();
 }
 
-const char* Processor::listInfo() { return info(CUDA); }
+}  // namespace acgb
+
+namespace ac::core {
+
+std::shared_ptr<Processor> Processor::create(const char* type, int device, const char* model)
+{
+    using acgb::UnavailableProcessor;
+    const int t = acgb::find_processor_type(type);
+    if (t == CPU)
+        return std::make_shared<UnavailableProcessor>(CPU, "the GB300 backend provides no CPU processor; use type \"cuda\"");
+    if (t == OpenCL)
+        return std::make_shared<UnavailableProcessor>(OpenCL, "the GB300 backend provides no OpenCL processor; use type \"cuda\"");
+    acgb::ModelSpec spec;
+    std::string err;
+    if (!acgb::parse_model(model, spec, err)) return std::make_shared<UnavailableProcessor>(CUDA, err);
+    return std::make_shared<acgb::GB300Processor>(t == -1 ? -1 : device, spec);
+}
+
+const char* Processor::listInfo() { return acgb::processor_info(CUDA); }
+
+// The per-model factory hook: each model descriptor names the model string
+// the reference's parser maps to the same network (Processor.cpp:26-187).
+namespace {
+std::shared_ptr<Processor> create_cuda(int idx, const std::string& model)
+{
+    return Processor::create("cuda", idx, model.c_str());
+}
+const char* const kKinds[4] = {"", "-hdn", "-box", "-box-hdn"};
+}  // namespace
+
+template<>
+std::shared_ptr<Processor> Processor::create<Processor::CUDA, model::ACNetLegacy>(int idx, const model::ACNetLegacy& m)
+{
+    const int v = static_cast<int>(m.variant());
+    return create_cuda(idx, v == 0 ? std::string("acnet-legacy-gan") : "acnet-legacy-hdn" + std::to_string(v - 1));
+}
+template<>
+std::shared_ptr<Processor> Processor::create<Processor::CUDA, model::ACNet<8>>(int idx, const model::ACNet<8>& m)
+{
+    return create_cuda(idx, "acnet-f8b" + std::to_string(m.blocks()) + kKinds[static_cast<int>(m.variant()) % 4]);
+}
+template<>
+std::shared_ptr<Processor> Processor::create<Processor::CUDA, model::ARNet<8>>(int idx, const model::ARNet<8>& m)
+{
+    const int k = static_cast<int>(m.variant()) % 4;
+    return create_cuda(idx, std::string("arnet") + (k & 1 ? "-hdn" : "") + (k & 2 ? "-box" : "") + "-b" +
+                                std::to_string(m.blocks()));
+}
+template<>
+std::shared_ptr<Processor> Processor::create<Processor::CUDA, model::ArtCNN<16>>(int idx, const model::ArtCNN<16>& m)
+{
+    const char* tail[3] = {"", "-dn", "-ds"};
+    return create_cuda(idx, std::string("artcnn-c4f16") + tail[static_cast<int>(m.variant())]);
+}
+template<>
+std::shared_ptr<Processor> Processor::create<Processor::CUDA, model::ArtCNN<32>>(int idx, const model::ArtCNN<32>& m)
+{
+    const char* tail[3] = {"", "-dn", "-ds"};
+    return create_cuda(idx, std::string("artcnn-c4f32") + tail[static_cast<int>(m.variant())]);
+}
+template<>
+std::shared_ptr<Processor> Processor::create<Processor::CUDA, model::FSRCNNX<8>>(int idx, const model::FSRCNNX<8>& m)
+{
+    return create_cuda(idx, m.variant() == model::FSRCNNX<8>::Variant::B4_DISTORT_PLUS ? "fsrcnnx-f8-dp" : "fsrcnnx-f8");
+}
+template<>
+std::shared_ptr<Processor> Processor::create<Processor::CUDA, model::FSRCNNX<16>>(int idx, const model::FSRCNNX<16>& m)
+{
+    return create_cuda(idx, m.variant() == model::FSRCNNX<16>::Variant::B4_DISTORT_PLUS ? "fsrcnnx-f16-dp" : "fsrcnnx-f16");
+}
+
+template<> const char* Processor::info<Processor::CPU>() { return acgb::processor_info(CPU); }
+template<> const char* Processor::info<Processor::OpenCL>() { return acgb::processor_info(OpenCL); }
+template<> const char* Processor::info<Processor::CUDA>() { return acgb::processor_info(CUDA); }
+
+}  // namespace ac::core
+
+namespace acgb {
 
 // --------------------------------------------------------- GB300Processor
 
@@ -950,7 +1029,7 @@ bool GB300Processor::run(ThreadState& ts, const DeviceImage& src, const DeviceIm
     return true;
 }
 
-void GB300Processor::processHost(const Image& src, Image& dst, double factor)
+void GB300Processor::processPath(const Image& src, Image& dst, double factor)
 {
     ThreadState& ts = state();
     if (!begin(ts)) return;

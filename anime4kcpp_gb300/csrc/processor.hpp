@@ -1,8 +1,7 @@
-// Processor interface of the GB300 backend, mirroring the reference's
-// ac::core::Processor (core/include/AC/Core/Processor.hpp:15-48): create()
-// never returns null and reports failure through ok()/error(); process()
-// follows core/src/processor/Processor.cpp:199-276; ok()/error() describe
-// the calling thread's most recent call.
+// Internal view of the GB300 backend's processor: the public
+// ac::core::Processor (reference interface core/include/AC/Core/
+// Processor.hpp:15-48), the arithmetic forms, device-resident images and
+// the output-shape rule of core/src/processor/Processor.cpp:199-276.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -10,6 +9,7 @@
 #include <memory>
 #include <string>
 
+#include "AC/Core/Processor.hpp"
 #include "image.hpp"
 #include "kernels.hpp"
 #include "models.hpp"
@@ -31,33 +31,11 @@ struct DeviceImage
     int w = 0, h = 0, c = 0, stride = 0, type = Image::UInt8;
 };
 
-class Processor
-{
-public:
-    static constexpr int CPU = 0;
-    static constexpr int OpenCL = 1;
-    static constexpr int CUDA = 2;
-
-    virtual ~Processor() = default;
-
-    Image process(const Image& src, double factor);
-    // A non-empty dst is taken as preallocated with the shape the reference
-    // would produce (Processor.hpp:27-29).
-    void process(const Image& src, Image& dst, double factor);
-
-    virtual bool ok() noexcept = 0;
-    virtual const char* error() noexcept = 0;
-    virtual const char* name() const noexcept = 0;
-    virtual int type() const noexcept { return CUDA; }
-    virtual const char* typeName() const noexcept { return "CUDA"; }
-
-    static std::shared_ptr<Processor> create(const char* type, int device, const char* model);
-    static const char* listInfo();
-    static const char* info(int type);
-
-protected:
-    virtual void processHost(const Image& src, Image& dst, double factor) = 0;
-};
+// The backend's processor interface is the public ac::core::Processor
+// (include/AC/Core/Processor.hpp).
+using Processor = ac::core::Processor;
+// Device list of a processor type (Processor::info<type>()).
+const char* processor_info(int type);
 
 // The GPU processor.  Exposed for the extension entry points.
 class GB300Processor;

@@ -40,6 +40,8 @@ public:
     bool ok() noexcept override;
     const char* error() noexcept override;
     const char* name() const noexcept override;
+    int type() const noexcept override { return CUDA; }
+    const char* typeName() const noexcept override { return "CUDA"; }
 
     // Device-pointer entry: src/dst already in HBM; work is queued on
     // `stream` (the calling thread's own stream when null).  Returns 0 or -1
@@ -80,7 +82,7 @@ public:
     const ModelSpec& spec() const { return spec_; }
 
 protected:
-    void processHost(const Image& src, Image& dst, double factor) override;
+    void processPath(const Image& src, Image& dst, double factor) override;
 
 private:
     struct AxisTable

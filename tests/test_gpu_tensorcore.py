@@ -4,8 +4,9 @@
 The FP16/BF16 forms round the 8-channel activations and the 8->8 weights to
 16 bits; they are held to the precision targets of the headline workload:
 PSNR >= 50 dB against the FP64 oracle on u8 outputs and agreement with the
-reference CPU processor within +-1 LSB on >= 99 % of u8 pixels (FP16), never
-more than a few LSB anywhere.
+reference CPU processor within +-1 LSB on >= 99.99 % of u8 pixels (FP16;
+measured at 1080p RGB: all of them), BF16 within +-1 LSB on >= 99.5 %.
+tests/test_gpu_precision.py holds the headline configuration itself.
 """
 import json
 import os
@@ -104,10 +105,11 @@ def test_tc_rgb_full_hd(form, kernel, monkeypatch):
     assert p.ok(), p.error()
     d = np.abs(got.astype(int) - ref32.astype(int))
     if form == "fp16":
-        assert (d <= 1).mean() >= 0.99
-        assert d.max() <= 6
+        # measured on this configuration: every sample within 1 LSB
+        assert (d <= 1).mean() >= 0.9999
+        assert d.max() <= 2
     else:
-        assert (d <= 2).mean() >= 0.95
+        assert (d <= 1).mean() >= 0.995 and d.max() <= 8
 
 
 @pytest.mark.parametrize("kernel", ["3", "4"])
