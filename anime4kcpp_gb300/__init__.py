@@ -65,7 +65,8 @@ class ACGB300ServeResult(ctypes.Structure):
 
 class ACGB300ServeStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "completed", "failed", "batches", "batched_jobs")] + \
-               [(n, ctypes.c_double) for n in ("budget_bytes", "in_use_bytes", "peak_bytes", "pool_bytes")]
+               [(n, ctypes.c_double) for n in ("budget_bytes", "in_use_bytes", "peak_bytes", "pool_bytes")] + \
+               [("device_allocs", ctypes.c_uint64)]
 
 
 # Every symbol of include/ac_image.h, include/ac_processor.h and include/ac_gb300.h.

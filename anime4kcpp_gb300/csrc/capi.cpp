@@ -510,6 +510,7 @@ int ac_gb300_server_stats(ACGB300Server* server, ACGB300ServeStats* stats)
     stats->in_use_bytes = s.inUseBytes;
     stats->peak_bytes = s.peakBytes;
     stats->pool_bytes = s.poolBytes;
+    stats->device_allocs = s.deviceAllocs;
     return AC_SUCCESS;
 }
 

@@ -139,23 +139,48 @@ bool phase_weights(int F, float* w)
 cudaError_t DeviceBuffer::ensure(size_t bytes)
 {
     if (bytes <= cap) return cudaSuccess;
-    if (ptr) cudaFree(ptr);
-    ptr = nullptr;
-    cap = 0;
-    size_t want = (bytes + (2u << 20) - 1) & ~static_cast<size_t>((2u << 20) - 1);
-    cudaError_t err = cudaMalloc(&ptr, want);
+    // Grow by at least half the current capacity (few growth events), in
+    // 2 MB steps.  The outgrown block is not freed here: cudaFree waits for
+    // the whole device, which would stall every other stream's work (the
+    // serving loop's latency); it is kept until release().
+    const size_t step = 2u << 20;
+    const size_t grown = cap + cap / 2;
+    const size_t want = (std::max(bytes, grown) + step - 1) & ~(step - 1);
+    void* fresh = nullptr;
+    cudaError_t err = cudaMalloc(&fresh, want);
     if (err != cudaSuccess)
     {
-        ptr = nullptr;
+        cudaGetLastError();  // the failed allocation is reported here, not left for a later check
         return err;
     }
+    device_alloc_count().fetch_add(1, std::memory_order_relaxed);
+    if (ptr)
+    {
+        try
+        {
+            retired.push_back(ptr);
+        }
+        catch (...)
+        {
+            cudaFree(ptr);
+        }
+    }
+    ptr = fresh;
     cap = want;
     return cudaSuccess;
+}
+
+std::atomic<uint64_t>& device_alloc_count()
+{
+    static std::atomic<uint64_t> n{0};
+    return n;
 }
 
 void DeviceBuffer::release()
 {
     if (ptr) cudaFree(ptr);
+    for (void* r : retired) cudaFree(r);
+    retired.clear();
     ptr = nullptr;
     cap = 0;
 }

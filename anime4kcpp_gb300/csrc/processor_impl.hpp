@@ -2,6 +2,7 @@
 // C ABI translation unit).
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <map>
 #include <memory>
@@ -22,14 +23,19 @@ bool phase_weights(int F, float* w);
 // CUDA graphs of batched launches replayed in this process so far.
 uint64_t graph_replays();
 
-// Grow-only device allocation.
+// Grow-only device allocation.  Outgrown blocks are kept (not freed while
+// work may run) until release().
 struct DeviceBuffer
 {
     void* ptr = nullptr;
     size_t cap = 0;
+    std::vector<void*> retired;
     cudaError_t ensure(size_t bytes);
     void release();
 };
+// Device allocations made by DeviceBuffer::ensure and the serving pool in
+// this process (diagnostics of the serving loop).
+std::atomic<uint64_t>& device_alloc_count();
 
 class GB300Processor final : public Processor
 {

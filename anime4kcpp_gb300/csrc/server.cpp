@@ -196,6 +196,7 @@ Server::Block Server::poolGet(size_t bytes, cudaError_t& err)
     }
     void* p = nullptr;
     if ((err = cudaMalloc(&p, r)) != cudaSuccess) return Block{};
+    device_alloc_count().fetch_add(1, std::memory_order_relaxed);
     poolBytes_ += r;
     return Block{p, r};
 }
@@ -290,6 +291,7 @@ ServeStats Server::stats()
     }
     std::lock_guard<std::mutex> lock(poolMutex_);
     s.poolBytes = static_cast<double>(poolBytes_);
+    s.deviceAllocs = device_alloc_count().load(std::memory_order_relaxed);
     return s;
 }
 

@@ -54,6 +54,7 @@ struct ServeStats
 {
     uint64_t submitted = 0, completed = 0, failed = 0, batches = 0, batchedJobs = 0;
     double budgetBytes = 0.0, inUseBytes = 0.0, peakBytes = 0.0, poolBytes = 0.0;
+    uint64_t deviceAllocs = 0;  // device allocations of this process so far (pool and work buffers)
 };
 
 class Server

@@ -594,14 +594,15 @@ SERVE_MODELS = ["acnet-legacy-hdn0", "acnet-legacy-hdn1", "acnet-legacy-hdn2", "
 def time_serve(ac, torch, args, forms=("fp16", "fp32")):
     """The serving workload: an open-loop Poisson stream of upscale jobs at
     `args.serve_rate` jobs/s for `args.serve_seconds` s through the serving
-    loop (ac.Server, 80 GB HBM budget, 4 worker streams).  Sizes 854x480,
+    loop (ac.Server, 80 GB HBM budget, 6 worker streams).  Sizes 854x480,
     1280x720, 1920x1080, 3840x2160 in ratio 1:2:2:1; factor 2 or 4 in ratio
     3:1; models ACNetLegacy HDN0-3 and ARNet B8 chosen uniformly; formats RGB
     u8 or 10-bit YUV 4:2:0 u16 (planar, shift 6) in ratio 4:1.  Latency =
-    submit -> result in the caller's pinned host buffer."""
+    submit -> result in the caller's pinned host buffer.  Then the FP16 form
+    at higher offered rates (`args.serve_load_rates`, `args.serve_load_seconds`
+    each): where continuous batching engages."""
     import queue
     from anime4kcpp_gb300 import synthetic
-    rng = np.random.default_rng(7)
     canvas = synthetic.rgb_u8(2160, 3840, cells=256, seed=70)
     luma = synthetic.luma(2160, 3840, np.uint16, cells=256, seed=71, noise=4.0, bits=10)
     chroma = [synthetic.luma(1080, 1920, np.uint16, cells=256, seed=72 + k, noise=4.0, bits=10) for k in range(2)]
@@ -626,27 +627,30 @@ def time_serve(ac, torch, args, forms=("fp16", "fp32")):
         for i in range(len(v)):
             free[k].put(i)
 
-    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, size=int(args.serve_rate * args.serve_seconds * 1.5) + 10))
-    arrivals = arrivals[arrivals < args.serve_seconds]
-    picks = [(int(rng.choice(4, p=np.array(SERVE_RES_W) / 6.0)), 2 if rng.random() < 0.75 else 4,
-              SERVE_MODELS[int(rng.integers(0, 5))], "rgb" if rng.random() < 0.8 else "yuv") for _ in arrivals]
-    out = {"workload": "Poisson %.0f jobs/s for %.0f s; 480p:720p:1080p:2160p = 1:2:2:1; x2:x4 = 3:1; "
-                       "ACNetLegacy HDN0-3 / ARNet-B8 uniform; RGB u8 : 10-bit YUV420 u16 = 4:1; 80 GB budget, "
-                       "4 worker streams" % (args.serve_rate, args.serve_seconds),
-           "jobs": len(arrivals)}
-    for form in forms:
-        srv = ac.Server(0, form, hbm_budget_gb=80.0, workers=4)
-        # warm-up: every model, format and factor once (processors, weights)
-        warm = []
-        for m in SERVE_MODELS:
-            for fmt in ("rgb", "yuv"):
-                for f in (2, 4):
-                    slot = free[(0, f, fmt)].get()
-                    warm.append((srv.submit(inputs[(0, fmt)], rings[(0, f, fmt)][slot], m, float(f), 6 if fmt == "yuv" else 0),
-                                 (0, f, fmt), slot))
-        for t, key, slot in warm:
-            srv.wait(t)
-            free[key].put(slot)
+    def stream_of(rate, seconds, seed):
+        rng = np.random.default_rng(seed)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * seconds * 1.5) + 10))
+        arrivals = arrivals[arrivals < seconds]
+        picks = [(int(rng.choice(4, p=np.array(SERVE_RES_W) / 6.0)), 2 if rng.random() < 0.75 else 4,
+                  SERVE_MODELS[int(rng.integers(0, 5))], "rgb" if rng.random() < 0.8 else "yuv") for _ in arrivals]
+        return arrivals, picks
+
+    def warm(srv):
+        # every model, format, factor and size once (processors, weights,
+        # work buffers and pool blocks of every size class)
+        for ri in range(len(SERVE_RES)):
+            tickets = []
+            for m in SERVE_MODELS:
+                for fmt in ("rgb", "yuv"):
+                    for f in (2, 4):
+                        slot = free[(ri, f, fmt)].get()
+                        tickets.append((srv.submit(inputs[(ri, fmt)], rings[(ri, f, fmt)][slot], m, float(f),
+                                                   6 if fmt == "yuv" else 0), (ri, f, fmt), slot))
+            for t, key, slot in tickets:
+                srv.wait(t, timeout=600.0)
+                free[key].put(slot)
+
+    def run(srv, arrivals, picks):
         done = queue.Queue()
         tickets = queue.Queue()
         stalls = [0]
@@ -663,6 +667,7 @@ def time_serve(ac, torch, args, forms=("fp16", "fp32")):
 
         collectors = [threading.Thread(target=collect, daemon=True) for _ in range(8)]
         [c.start() for c in collectors]
+        st0 = srv.stats()
         t0 = time.perf_counter()
         for at, (ri, f, m, fmt) in zip(arrivals, picks):
             delay = t0 + at - time.perf_counter()
@@ -681,23 +686,51 @@ def time_serve(ac, torch, args, forms=("fp16", "fp32")):
             tickets.put(None)
         [c.join() for c in collectors]
         wall = time.perf_counter() - t0
+        st1 = srv.stats()
         res = [done.get() for _ in range(done.qsize())]
+
+        def pct(vals, q):
+            return float(np.percentile(vals, q)) if len(vals) else None
+
         lat = np.array([r["latency_ms"] for r, _ in res])
         ok = [r for r, _ in res if r["status"] == 0]
-        lat1080 = np.array([r["latency_ms"] for r, m in res if m[0] == 2])
+        r1080 = [r for r, m in res if m[0] == 2]
+        lat1080 = np.array([r["latency_ms"] for r in r1080])
         lat1080x2 = np.array([r["latency_ms"] for r, m in res if m[0] == 2 and m[1] == 2 and m[3] == "rgb" and "acnet" in m[2]])
-        st = srv.stats()
-        srv.close()
-        out[form] = {
-            "completed": len(ok), "failed": len(res) - len(ok),
+        return {
+            "completed": len(ok), "failed": len(res) - len(ok), "jobs": len(res),
             "out_mpx_per_s": sum(m[4] for r, m in res if r["status"] == 0) / wall / 1e6,
-            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "p50_ms_1080p": float(np.percentile(lat1080, 50)) if len(lat1080) else None,
-            "p99_ms_1080p": float(np.percentile(lat1080, 99)) if len(lat1080) else None,
-            "p99_ms_1080p_acnet_x2_rgb": float(np.percentile(lat1080x2, 99)) if len(lat1080x2) else None,
-            "mean_queue_ms": float(np.mean([r["queue_ms"] for r, _ in res])),
-            "batched_jobs": int(st["batched_jobs"]), "batches": int(st["batches"]),
-            "peak_admitted_gb": st["peak_bytes"] / 1e9, "wall_s": wall, "generator_stalls": stalls[0]}
+            "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
+            "p50_ms_1080p": pct(lat1080, 50), "p99_ms_1080p": pct(lat1080, 99),
+            "p99_ms_1080p_acnet_x2_rgb": pct(lat1080x2, 99),
+            # the 1080p p99 split: admission queue, waiting for a worker, on the device (copies included)
+            "p99_ms_1080p_parts": {"admission": pct([r["queue_ms"] for r in r1080], 99),
+                                   "worker_wait": pct([r["latency_ms"] - r["queue_ms"] - r["device_ms"] for r in r1080], 99),
+                                   "device": pct([r["device_ms"] for r in r1080], 99)},
+            "mean_queue_ms": float(np.mean([r["queue_ms"] for r, _ in res])) if res else None,
+            "batched_jobs": int(st1["batched_jobs"] - st0["batched_jobs"]), "batches": int(st1["batches"] - st0["batches"]),
+            "mean_jobs_per_launch_when_batched": (st1["batched_jobs"] - st0["batched_jobs"]) /
+            max(1, st1["batches"] - st0["batches"]),
+            "device_allocs_during_run": int(st1["device_allocs"] - st0["device_allocs"]),
+            "peak_admitted_gb": st1["peak_bytes"] / 1e9, "wall_s": wall, "generator_stalls": stalls[0]}
+
+    out = {"workload": "Poisson %.0f jobs/s for %.0f s; 480p:720p:1080p:2160p = 1:2:2:1; x2:x4 = 3:1; "
+                       "ACNetLegacy HDN0-3 / ARNet-B8 uniform; RGB u8 : 10-bit YUV420 u16 = 4:1; 80 GB budget, "
+                       "%d worker streams" % (args.serve_rate, args.serve_seconds, args.serve_workers)}
+    arrivals, picks = stream_of(args.serve_rate, args.serve_seconds, 7)
+    out["jobs"] = len(arrivals)
+    for form in forms:
+        srv = ac.Server(0, form, hbm_budget_gb=80.0, workers=args.serve_workers)
+        warm(srv)
+        out[form] = run(srv, arrivals, picks)
+        if form == "fp16" and args.serve_load_seconds > 0:
+            loads = []
+            for k, rate in enumerate(args.serve_load_rates):
+                a, p = stream_of(rate, args.serve_load_seconds, 100 + k)
+                rec = run(srv, a, p)
+                loads.append(dict(rec, offered_jobs_per_s=rate, seconds=args.serve_load_seconds))
+            out["fp16_load_points"] = loads
+        srv.close()
     return out
 
 
@@ -976,11 +1009,15 @@ def main():
     ap.add_argument("--video-steps", type=int, default=4, help="8-frame steps of the video workload (0: skip)")
     ap.add_argument("--family-steps", type=int, default=10, help="frames per family and form in the families workload (0: skip)")
     ap.add_argument("--cli-steps", type=int, default=10, help="steps of the CLI-default-model workload (0: skip)")
-    ap.add_argument("--serve-seconds", type=float, default=10.0, help="serving workload length per form (0: skip)")
+    ap.add_argument("--serve-seconds", type=float, default=60.0, help="serving workload length per form (0: skip)")
+    ap.add_argument("--serve-workers", type=int, default=6, help="worker streams of the serving loop")
+    ap.add_argument("--serve-load-seconds", type=float, default=8.0, help="length of each higher-rate FP16 serving run (0: skip)")
+    ap.add_argument("--serve-load-rates", default="600,1000", help="offered rates of the higher-rate FP16 serving runs, jobs/s")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="serving workload arrival rate, jobs/s")
     ap.add_argument("--saturation-rate", type=float, default=4000.0, help="offered rate of the saturation run, jobs/s")
     args = ap.parse_args()
     args.forms = [f for f in args.forms.split(",") if f]
+    args.serve_load_rates = [float(r) for r in args.serve_load_rates.split(",") if r]
     args.warmup = max(args.warmup, 3)
 
     rank, world, local_rank = env_int("RANK", 0), env_int("WORLD_SIZE", 1), env_int("LOCAL_RANK", 0)

@@ -184,6 +184,7 @@ typedef struct ACGB300ServeStats
 {
     uint64_t submitted, completed, failed, batches, batched_jobs;
     double budget_bytes, in_use_bytes, peak_bytes, pool_bytes;
+    uint64_t device_allocs; /* device allocations of the process so far (serving pool and work buffers) */
 } ACGB300ServeStats;
 
 typedef struct ACGB300Server ACGB300Server;
