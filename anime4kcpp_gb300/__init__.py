@@ -80,7 +80,7 @@ EXPORTS = (
     "ac_gb300_set_precision", "ac_gb300_get_precision", "ac_gb300_output_shape", "ac_gb300_process_device",
     "ac_gb300_launch_count", "ac_gb300_model_params", "ac_gb300_profile_enable", "ac_gb300_profile_collect",
     "ac_gb300_tc_selftest", "ac_gb300_wait_selftest", "ac_gb300_process_device_noalloc", "ac_gb300_process_batch_device",
-    "ac_gb300_graph_replays", "ac_gb300_process_yuv_device",
+    "ac_gb300_graph_replays", "ac_gb300_last_plan", "ac_gb300_debug_fail_alloc", "ac_gb300_process_yuv_device",
     "ac_gb300_server_create", "ac_gb300_server_error", "ac_gb300_server_submit", "ac_gb300_server_wait",
     "ac_gb300_server_stats", "ac_gb300_server_destroy",
 )
@@ -120,6 +120,8 @@ def native():
             "ac_gb300_process_device_noalloc": (I, [pproc, I, P(ACGB300DeviceImage), P(ACGB300DeviceImage), V, I]),
             "ac_gb300_process_batch_device": (I, [pproc, I, P(ACGB300DeviceImage), P(ACGB300DeviceImage), D, V, I]),
             "ac_gb300_graph_replays": (ctypes.c_uint64, []),
+            "ac_gb300_last_plan": (I, [pproc, P(I), P(I), P(I), P(I)]),
+            "ac_gb300_debug_fail_alloc": (None, [I]),
             "ac_gb300_process_yuv_device": (I, [pproc, I, I, P(ACGB300DeviceImage), P(ACGB300DeviceImage), D, I, V, I]),
             "ac_gb300_server_create": (V, [I, I, D, I, I]),
             "ac_gb300_server_error": (ctypes.c_char_p, [V]),
@@ -316,6 +318,17 @@ class Processor:
         return native().ac_gb300_process_device_noalloc(ctypes.byref(self._p), n, s, d, ctypes.c_void_p(stream or 0),
                                                         1 if sync else 0)
 
+    def last_plan(self):
+        """The persistent tensor-core launch plan of this thread's most
+        recent call (``ac_gb300_last_plan``): kernel ("quad", "pair",
+        "quad-acnet8" or None), tile (w, h) and CTAs per SM."""
+        k, tw, th, ps = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        if native().ac_gb300_last_plan(ctypes.byref(self._p), ctypes.byref(k), ctypes.byref(tw), ctypes.byref(th),
+                                       ctypes.byref(ps)) != AC_SUCCESS:
+            raise RuntimeError("no GPU processor")
+        return {"kernel": {4: "quad", 3: "pair", 5: "quad-acnet8"}.get(k.value), "tile": (tw.value, th.value),
+                "ctas_per_sm": ps.value}
+
     def profile(self, enable=True):
         native().ac_gb300_profile_enable(ctypes.byref(self._p), 1 if enable else 0)
 
@@ -405,6 +418,11 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def debug_fail_alloc(nth):
+    """Arm the nth next device allocation of the library to fail (0 disarms)."""
+    native().ac_gb300_debug_fail_alloc(int(nth))
 
 
 def graph_replays():

@@ -67,10 +67,11 @@ void pack_quad_layer0(const float* k, bool bf16, uint16_t* out)
 
 int acnet_tc4_max_images() { return tcv4::kMaxImages; }
 
-void acnet_tc4_shape(int* tw, int* th)
+void acnet_tc4_shape(int shape, int* tw, int* th)
 {
-    *tw = tcv4::Geo0::TW;
-    *th = tcv4::Geo0::TH;
+    using namespace tcv4;
+    *tw = shape == 1 ? GeoQ1::TW : (shape == 2 ? GeoQ2::TW : Geo0::TW);
+    *th = shape == 1 ? GeoQ1::TH : (shape == 2 ? GeoQ2::TH : Geo0::TH);
 }
 
 // Layer 0 as an 8-channel layer over the input slots (y_hi, y_lo, y_hi) with
@@ -91,11 +92,12 @@ void pack_acnet_tc4_weights(const AcnetLegacyWeights& w, bool bf16, std::vector<
 // `ctas` SMs' worth of CTAs drain the queue.
 cudaError_t launch_acnet_legacy_tc4_core(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n, const Plane* in,
                                          const Plane* out, const Phase2* phase2, int* counter, int* status, int ctas,
-                                         cudaStream_t stream, int per_sm_cap)
+                                         cudaStream_t stream, int per_sm_cap, int shape)
 {
     using namespace tcv4;
     if (n <= 0) return cudaSuccess;
-    if (n > kMaxImages || !packed4 || !counter || !status || ctas <= 0) return cudaErrorInvalidValue;
+    if (n > kMaxImages || !packed4 || !counter || !status || ctas <= 0 || shape < 0 || shape >= kTc4Shapes)
+        return cudaErrorInvalidValue;
     const int c = in[0].channels, type = in[0].type;
     if (c > 1 && !phase2) return cudaErrorInvalidValue;
     Params p;
@@ -105,7 +107,8 @@ cudaError_t launch_acnet_legacy_tc4_core(const AcnetLegacyWeights& wts, const vo
     for (int l = 0; l < NetLegacy::NL; l++)
         for (int k = 0; k < 8; k++) p.bias[l][k] = wts.b[8 * l + k];
     if (phase2) p.ph = *phase2;
-    constexpr int TW = Geo0::TW, TH = Geo0::TH;
+    int TW = 0, TH = 0;
+    acnet_tc4_shape(shape, &TW, &TH);
     int tiles = 0;
     for (int i = 0; i < n; i++)
     {
@@ -123,18 +126,24 @@ cudaError_t launch_acnet_legacy_tc4_core(const AcnetLegacyWeights& wts, const vo
     cudaError_t err = cudaMemsetAsync(counter, 0, sizeof(int), stream);
     if (err != cudaSuccess) return err;
     const int grid = tiles < ctas ? tiles : ctas;
-    err = launch_shape<Geo0, NetLegacy>(type, c, bf16, p, grid, per_sm_cap, stream);
+    switch (shape)
+    {
+    case 1: err = launch_shape<GeoQ1, NetLegacy>(type, c, bf16, p, grid, per_sm_cap, stream); break;
+    case 2: err = launch_shape<GeoQ2, NetLegacy>(type, c, bf16, p, grid, per_sm_cap, stream); break;
+    default: err = launch_shape<Geo0, NetLegacy>(type, c, bf16, p, grid, per_sm_cap, stream); break;
+    }
     if (err == cudaSuccess) count_launch();
     return err;
 }
 
 cudaError_t launch_acnet_legacy_tc4(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n, const Plane* in,
                                     const Plane* out, const Phase2* phase2, int* counter, int ctas, cudaStream_t stream,
-                                    int per_sm_cap)
+                                    int per_sm_cap, int shape)
 {
     int* status = tc_status_buffer();
     if (!status) return cudaErrorMemoryAllocation;
-    return launch_acnet_legacy_tc4_core(wts, packed4, bf16, n, in, out, phase2, counter, status, ctas, stream, per_sm_cap);
+    return launch_acnet_legacy_tc4_core(wts, packed4, bf16, n, in, out, phase2, counter, status, ctas, stream, per_sm_cap,
+                                        shape);
 }
 
 }  // namespace acgb

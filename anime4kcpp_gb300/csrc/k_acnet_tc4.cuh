@@ -734,7 +734,12 @@ cudaError_t launch_shape(int type, int c, bool bf16, const Params& p, int grid, 
     }
 }
 
-using Geo0 = Geo<46, 46, 9>;     // ACNetLegacy: 64 x 64 window
+using Geo0 = Geo<46, 46, 9>;     // ACNetLegacy: 64 x 64 window (shape 0, the default)
+using GeoQ1 = Geo<62, 33, 9>;    // ACNetLegacy shape 1: 80 x 51 window (wide tiles)
+using GeoQ2 = Geo<30, 67, 9>;    // ACNetLegacy shape 2: 48 x 85 window (tall tiles)
+// Shapes 1 and 2 are instantiated in k_acnet_tc4_shapes.cu (built in parallel).
+extern template cudaError_t launch_shape<GeoQ1, NetLegacy>(int, int, bool, const Params&, int, int, cudaStream_t);
+extern template cudaError_t launch_shape<GeoQ2, NetLegacy>(int, int, bool, const Params&, int, int, cudaStream_t);
 using GeoA8B4 = Geo<52, 48, 6>;  // ACNet<8> B4: 64 x 60 window (chroma sums of a 52 x 52 tile would not fit)
 using GeoA8B8 = Geo<44, 44, 10>; // ACNet<8> B8
 

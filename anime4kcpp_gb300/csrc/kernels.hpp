@@ -129,21 +129,25 @@ cudaError_t launch_acnet_legacy_tc3_noalloc(const AcnetLegacyWeights& wts, const
                                             cudaStream_t stream);
 cudaError_t acnet_tc3_noalloc_status(int* value);
 
-// Quad form of the persistent kernel: four pixels per GEMM row (N = 32), one
-// 46x46 tile shape, B matrices streamed per layer; `packed4` is the device
-// copy of pack_acnet_tc4_weights().  Same arguments and output bytes
-// contract as launch_acnet_legacy_tc3 (results agree within the FP16/BF16
-// tolerance; the MMA accumulation order differs).
+// Quad form of the persistent kernel: four pixels per GEMM row (N = 32),
+// B matrices streamed per layer; `packed4` is the device copy of
+// pack_acnet_tc4_weights().  Three tile shapes (`shape` 0: 46x46 in a 64x64
+// window, the default; 1: 62x33 in 80x51; 2: 30x67 in 48x85), every one
+// computing each output pixel from the same window with the same arithmetic
+// (identical bytes).  Same arguments and output contract as
+// launch_acnet_legacy_tc3 (results agree within the FP16/BF16 tolerance; the
+// MMA accumulation order differs).
+constexpr int kTc4Shapes = 3;
 int acnet_tc4_max_images();
-void acnet_tc4_shape(int* tw, int* th);
+void acnet_tc4_shape(int shape, int* tw, int* th);
 void pack_acnet_tc4_weights(const AcnetLegacyWeights& wts, bool bf16, std::vector<uint16_t>& packed);
 cudaError_t launch_acnet_legacy_tc4(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n, const Plane* in,
                                     const Plane* out, const Phase2* phase2, int* counter, int ctas, cudaStream_t stream,
-                                    int per_sm_cap = 2);
+                                    int per_sm_cap = 2, int shape = 0);
 // The same with the caller's status word (`status`, 0 or 1 after a timed-out wait).
 cudaError_t launch_acnet_legacy_tc4_core(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n, const Plane* in,
                                          const Plane* out, const Phase2* phase2, int* counter, int* status, int ctas,
-                                         cudaStream_t stream, int per_sm_cap);
+                                         cudaStream_t stream, int per_sm_cap, int shape = 0);
 // ACNet<8> with 4 or 8 blocks in the quad kernel (PReLU layers, conv3x3
 // 8 -> 4 pixel-shuffle tail with the nearest-source add; fused colour path as
 // for ACNetLegacy).  `packed4` is the device copy of pack_acnet8_tc4_weights();

@@ -146,6 +146,7 @@ cudaError_t DeviceBuffer::ensure(size_t bytes)
     const size_t step = 2u << 20;
     const size_t grown = cap + cap / 2;
     const size_t want = (std::max(bytes, grown) + step - 1) & ~(step - 1);
+    if (injected_alloc_failure()) return cudaErrorMemoryAllocation;
     void* fresh = nullptr;
     cudaError_t err = cudaMalloc(&fresh, want);
     if (err != cudaSuccess)
@@ -174,6 +175,23 @@ std::atomic<uint64_t>& device_alloc_count()
 {
     static std::atomic<uint64_t> n{0};
     return n;
+}
+
+// Host-side fault injection: while armed with n > 0, the n-th next device
+// allocation of DeviceBuffer::ensure or the serving pool fails as if the
+// device were out of memory (no cudaMalloc is made for it).
+namespace {
+std::atomic<int> g_fail_alloc_countdown{0};
+}
+
+void arm_alloc_failure(int nth) { g_fail_alloc_countdown.store(nth > 0 ? nth : 0); }
+
+bool injected_alloc_failure()
+{
+    int v = g_fail_alloc_countdown.load();
+    while (v > 0)
+        if (g_fail_alloc_countdown.compare_exchange_weak(v, v - 1)) return v == 1;
+    return false;
 }
 
 void DeviceBuffer::release()
@@ -724,9 +742,12 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
                 else if ((err = ts.counter.ensure(256)) == cudaSuccess)
                 {
                     int* counter = static_cast<int*>(ts.counter.ptr) + (ts.counterSlot++ & 63);
-                    err = launch_acnet_legacy_tc4(*acnet_, w, bf16, 1, &in, &out, ph, counter,
-                                                  tc3Ctas_ > 0 ? tc3Ctas_ : smCount_, stream,
-                                                  tc3PerSm_ > 0 ? tc3PerSm_ : 2);
+                    bool ran = false;
+                    const Tc3Plan plan = tc3Plan(1, &in, &out, ph, w, bf16, counter, stream, ran, err, true);
+                    ts.lastPlan = LastPlan{4, plan.shape, plan.perSm};
+                    if (err == cudaSuccess && !ran)
+                        err = launch_acnet_legacy_tc4(*acnet_, w, bf16, 1, &in, &out, ph, counter,
+                                                      tc3Ctas_ > 0 ? tc3Ctas_ : smCount_, stream, plan.perSm, plan.shape);
                 }
             }
             else
@@ -741,6 +762,7 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
                     int* counter = static_cast<int*>(ts.counter.ptr) + (ts.counterSlot++ & 63);
                     bool ran = false;
                     const Tc3Plan plan = tc3Plan(1, &in, &out, ph, w, bf16, counter, stream, ran, err);
+                    ts.lastPlan = LastPlan{3, plan.shape, plan.perSm};
                     if (err == cudaSuccess && !ran)
                         err = launch_acnet_legacy_tc3(*acnet_, w, bf16, 1, &in, &out, ph, counter,
                                                       tc3Ctas_ > 0 ? tc3Ctas_ : smCount_, stream, plan.shape, plan.perSm);
@@ -753,6 +775,8 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
 }
 
 void GB300Processor::setProfiling(bool on) { profiling_ = on; }
+
+GB300Processor::LastPlan GB300Processor::lastPlan() { return state().lastPlan; }
 
 int GB300Processor::collectProfile(double& ms, int& launches, double& outPixels)
 {
@@ -859,7 +883,8 @@ static int ilog2(double v)
 }
 
 GB300Processor::Tc3Plan GB300Processor::tc3Plan(int n, const Plane* in, const Plane* out, const Phase2* ph, const void* w,
-                                                bool bf16, int* counter, cudaStream_t stream, bool& ran, cudaError_t& err)
+                                                bool bf16, int* counter, cudaStream_t stream, bool& ran, cudaError_t& err,
+                                                bool quad)
 {
     ran = false;
     err = cudaSuccess;
@@ -876,7 +901,8 @@ GB300Processor::Tc3Plan GB300Processor::tc3Plan(int n, const Plane* in, const Pl
         sw += in[i].w;
         sh += in[i].h;
     }
-    const auto key = std::make_tuple(in[0].type, in[0].channels, bf16 ? 1 : 0, ilog2(total), ilog2(sw / n), ilog2(sh / n));
+    const auto key = std::make_tuple(in[0].type, in[0].channels, (bf16 ? 1 : 0) + (quad ? 2 : 0), ilog2(total), ilog2(sw / n),
+                                     ilog2(sh / n));
     {
         std::lock_guard<std::mutex> lock(mutex_);
         auto it = plans_.find(key);
@@ -895,13 +921,17 @@ GB300Processor::Tc3Plan GB300Processor::tc3Plan(int n, const Plane* in, const Pl
     const int ctas = tc3Ctas_ > 0 ? tc3Ctas_ : smCount_;
     float best = 1e30f;
     Tc3Plan bestPlan = plan;
-    for (int shape = 0; shape < kTc3Shapes && err == cudaSuccess; shape++)
+    auto launch = [&](int shape, int perSm) {
+        return quad ? launch_acnet_legacy_tc4(*acnet_, w, bf16, n, in, out, ph, counter, ctas, stream, perSm, shape)
+                    : launch_acnet_legacy_tc3(*acnet_, w, bf16, n, in, out, ph, counter, ctas, stream, shape, perSm);
+    };
+    const int shapes = quad ? kTc4Shapes : kTc3Shapes;
+    for (int shape = 0; shape < shapes && err == cudaSuccess; shape++)
         for (int perSm = 2; perSm >= 1 && err == cudaSuccess; perSm--)
         {
-            err = launch_acnet_legacy_tc3(*acnet_, w, bf16, n, in, out, ph, counter, ctas, stream, shape, perSm);
+            err = launch(shape, perSm);
             if (err == cudaSuccess) err = cudaEventRecord(e0, stream);
-            for (int r = 0; r < 2 && err == cudaSuccess; r++)
-                err = launch_acnet_legacy_tc3(*acnet_, w, bf16, n, in, out, ph, counter, ctas, stream, shape, perSm);
+            for (int r = 0; r < 2 && err == cudaSuccess; r++) err = launch(shape, perSm);
             if (err == cudaSuccess) err = cudaEventRecord(e1, stream);
             if (err == cudaSuccess) err = cudaEventSynchronize(e1);
             float ms = 0.0f;
@@ -1248,9 +1278,10 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
             const Phase2* php = in[0].channels > 1 ? &ph : nullptr;
             bool ran = false;
             Tc3Plan plan;
-            if (quad) plan.perSm = tc3PerSm_ > 0 ? tc3PerSm_ : 2;
-            else plan = tc3Plan(m, in, out, php, w, bf16, counter, s, ran, err);
+            if (acn8) plan.perSm = tc3PerSm_ > 0 ? tc3PerSm_ : 2;  // one tile shape per ACNet<8> depth
+            else plan = tc3Plan(m, in, out, php, w, bf16, counter, s, ran, err, quad);
             if (err != cudaSuccess) return fail(ts, "batched upscale", err), false;
+            ts.lastPlan = LastPlan{acn8 ? 5 : (quad ? 4 : 3), plan.shape, plan.perSm};
             mix(static_cast<uint64_t>(plan.shape * 4 + plan.perSm));
             mix(static_cast<uint64_t>(quad));
             const int ctas = tc3Ctas_ > 0 ? tc3Ctas_ : smCount_;
@@ -1261,7 +1292,8 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
                     return launch_acnet8_tc4(mp.biases.data(), mp.alphas.data(), spec_.blocks, w, bf16, m, in, out, php,
                                              counter, ctas, s, plan.perSm);
                 }
-                return quad ? launch_acnet_legacy_tc4(*acnet_, w, bf16, m, in, out, php, counter, ctas, s, plan.perSm)
+                return quad ? launch_acnet_legacy_tc4(*acnet_, w, bf16, m, in, out, php, counter, ctas, s, plan.perSm,
+                                                      plan.shape)
                             : launch_acnet_legacy_tc3(*acnet_, w, bf16, m, in, out, php, counter, ctas, s, plan.shape,
                                                       plan.perSm);
             };

@@ -36,6 +36,10 @@ struct DeviceBuffer
 // Device allocations made by DeviceBuffer::ensure and the serving pool in
 // this process (diagnostics of the serving loop).
 std::atomic<uint64_t>& device_alloc_count();
+// Fault injection: make the nth next device allocation fail (0 disarms);
+// injected_alloc_failure() is asked before every such allocation.
+void arm_alloc_failure(int nth);
+bool injected_alloc_failure();
 
 class GB300Processor final : public Processor
 {
@@ -109,8 +113,20 @@ private:
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
     };
+public:
+    // The persistent launch plan of the calling thread's most recent
+    // tensor-core call: kernel 4 quad (ACNetLegacy), 3 pair, 5 quad
+    // (ACNet<8>), 0 none; tile shape index; CTAs per SM.
+    struct LastPlan
+    {
+        int kernel = 0, shape = 0, perSm = 0;
+    };
+    LastPlan lastPlan();
+
+private:
     struct ThreadState
     {
+        LastPlan lastPlan;
         cudaStream_t stream = nullptr;
         DeviceBuffer src, y, uv, la, lb, out;
         DeviceBuffer maps[4];  // ARNet feature maps
@@ -162,17 +178,18 @@ private:
         return spec_.family == Family::ACNet8 && precision_ != Precision::FP32 && arnetTc_ && tcKernel_ == 4 &&
                acnet8_tc4_supported(spec_.blocks);
     }
-    // Tile shape and CTAs per SM for a persistent launch over these images:
-    // forced by AC_GB300_TC3_SHAPE / AC_GB300_TC3_PER_SM, else measured once
-    // per batch class (element type, channels, form, log2 of the total and
-    // mean image sizes) over every shape x {2, 1} CTAs per SM.  When it
-    // measured, the launches already produced the output (`ran`).
     bool batchRun(ThreadState& ts, int n, const DeviceImage* src, const DeviceImage* dst, double factor, cudaStream_t s);
     // ARNet / ACNet<8> tensor-core forms over n single-channel images, x2 or
     // x4: each layer one launch over every image (up to kArnetTcMaxImages).
     bool layeredBatch(ThreadState& ts, int n, const DeviceImage* src, const DeviceImage* dst, double factor, cudaStream_t s);
+    // Tile shape and CTAs per SM for a persistent launch of the pair kernel
+    // or (quad) the quad kernel over these images: forced by
+    // AC_GB300_TC3_SHAPE / AC_GB300_TC3_PER_SM, else measured once per batch
+    // class (kernel, element type, channels, form, log2 of the total and mean
+    // image sizes) over every tile shape x {2, 1} CTAs per SM.  When it
+    // measured, the launches already produced the output (`ran`).
     Tc3Plan tc3Plan(int n, const Plane* in, const Plane* out, const Phase2* ph, const void* w, bool bf16, int* counter,
-                    cudaStream_t stream, bool& ran, cudaError_t& err);
+                    cudaStream_t stream, bool& ran, cudaError_t& err, bool quad = false);
 
     int device_ = -1;
     int smCount_ = 0;

@@ -195,6 +195,11 @@ Server::Block Server::poolGet(size_t bytes, cudaError_t& err)
         free_.erase(big);
     }
     void* p = nullptr;
+    if (injected_alloc_failure())
+    {
+        err = cudaErrorMemoryAllocation;
+        return Block{};
+    }
     if ((err = cudaMalloc(&p, r)) != cudaSuccess) return Block{};
     device_alloc_count().fetch_add(1, std::memory_order_relaxed);
     poolBytes_ += r;

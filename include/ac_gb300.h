@@ -63,6 +63,25 @@ AC_C_API int ac_gb300_process_device(ACProcessor* processor, const ACGB300Device
 AC_C_API int ac_gb300_process_batch_device(ACProcessor* processor, int count, const ACGB300DeviceImage* src,
                                            const ACGB300DeviceImage* dst, double factor, void* stream, int sync);
 
+/* The persistent tensor-core launch plan of the calling thread's most recent
+ * call on this processor: *kernel 4 (the quad kernel, ACNetLegacy), 3 (the
+ * pair kernel), 5 (the quad kernel, ACNet<8>) or 0 (no such launch yet);
+ * *tile_w x *tile_h its tile shape; *ctas_per_sm the CTAs-per-SM cap.  The
+ * plan is the autotuner's choice for the call's batch class, measured the
+ * first time the class was seen, or the one the environment forced
+ * (AC_GB300_TC3_SHAPE, AC_GB300_TC3_PER_SM).  Returns AC_SUCCESS or
+ * AC_ERROR(AC_EINVAL). */
+AC_C_API int ac_gb300_last_plan(ACProcessor* processor, int* kernel, int* tile_w, int* tile_h, int* ctas_per_sm);
+
+/* Host-side fault injection for tests of the failure paths: arms the
+ * nth next device allocation of the library's work buffers or serving pool
+ * (counted over the whole process) to fail as if the device were out of
+ * memory; no allocation is attempted for it.  0 disarms.  The failing call
+ * reports AC_ERROR(AC_EPROCESSOR) with a "device allocation" message (a
+ * serving job: status -1) and later calls succeed.  No reference
+ * counterpart. */
+AC_C_API void ac_gb300_debug_fail_alloc(int nth);
+
 /* Number of batched launches this process has run as CUDA graph replays. */
 AC_C_API uint64_t ac_gb300_graph_replays(void);
 

@@ -67,21 +67,19 @@ def test_batch_matches_per_image_and_replays_graphs(form, kernel, monkeypatch):
         for d, w in zip(dsts, want):
             assert np.array_equal(d.cpu().numpy(), w)
         replays = ac.graph_replays() - before
-        # pair kernel: call 0 measures the plan, call 1 launches directly,
-        # calls 2 and 3 capture once and replay the graph; the quad kernel has
-        # one plan, so its capture comes one call earlier
-        first = 2 if kernel == "3" else 1
-        assert replays == (groups if call >= first else 0)
+        # call 0 measures the plan (autotuner), call 1 launches directly,
+        # calls 2 and 3 capture once and replay the graph
+        assert replays == (groups if call >= 2 else 0)
     ref = oracle.process(frames[0], 2.0, "acnet-legacy-hdn1").astype(int)
     d = np.abs(want[0].astype(int) - ref)
     assert (d <= 1).mean() >= 0.99
 
 
+@pytest.mark.parametrize("kernel", ["3", "4"])
 @pytest.mark.parametrize("c", [1, 3, 4])
-def test_tile_shapes_and_cta_caps_give_identical_bytes(c, monkeypatch):
-    """The pair kernel's three tile shapes and CTA caps (the quad kernel has
-    one shape; its CTA counts are covered in test_gpu_tensorcore.py)."""
-    monkeypatch.setenv("AC_GB300_TC_KERNEL", "3")
+def test_tile_shapes_and_cta_caps_give_identical_bytes(c, kernel, monkeypatch):
+    """Each persistent kernel's three tile shapes and CTA caps."""
+    monkeypatch.setenv("AC_GB300_TC_KERNEL", kernel)
     if c == 1:
         x = synthetic.luma(131, 150, np.uint16, seed=9)
     else:
@@ -96,23 +94,40 @@ def test_tile_shapes_and_cta_caps_give_identical_bytes(c, monkeypatch):
             d = _out_like(src)
             p.process_device(src, d, 2.0)
             outs.append(d.cpu().numpy())
+            plan = p.last_plan()
+            assert plan["kernel"] == ("quad" if kernel == "4" else "pair")
+            assert plan["ctas_per_sm"] == int(per_sm)
     for o in outs[1:]:
         assert np.array_equal(o, outs[0])
 
 
-def test_autotuned_equals_untuned(monkeypatch):
-    """The pair kernel's autotuner picks a plan without changing the bytes."""
-    monkeypatch.setenv("AC_GB300_TC_KERNEL", "3")
-    x = synthetic.rgb_u8(300, 500, seed=21)
-    src = torch.from_numpy(x).cuda()
-    outs = []
+@pytest.mark.parametrize("kernel", ["3", "4"])
+@pytest.mark.parametrize("batch", [False, True])
+def test_autotuned_equals_untuned(kernel, batch, monkeypatch):
+    """The autotuner of each persistent kernel (the quad kernel is the
+    default) picks a plan -- tile shape and CTAs per SM, measured once per
+    batch class -- without changing the bytes."""
+    monkeypatch.setenv("AC_GB300_TC_KERNEL", kernel)
+    imgs = [synthetic.rgb_u8(300, 500, seed=21)] + ([synthetic.rgb_u8(h, w, seed=h) for h, w in
+                                                     [(257, 1031), (700, 333), (64, 64)]] if batch else [])
+    srcs = [torch.from_numpy(x).cuda() for x in imgs]
+    outs, plans = [], []
     for tune in ("1", "0"):
         monkeypatch.setenv("AC_GB300_AUTOTUNE", tune)
         p = ac.Processor("cuda", 0, "acnet-legacy-hdn0", precision="fp16")
-        d = _out_like(src)
-        p.process_device(src, d, 2.0)
-        outs.append(d.cpu().numpy())
-    assert np.array_equal(outs[0], outs[1])
+        dsts = [_out_like(s) for s in srcs]
+        for _ in range(2):  # the measuring call, then the tuned plan's own launch
+            if batch:
+                p.process_batch_device(srcs, dsts, 2.0)
+            else:
+                p.process_device(srcs[0], dsts[0], 2.0)
+        outs.append([d.cpu().numpy() for d in dsts])
+        plans.append(p.last_plan())
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
+    assert plans[0]["kernel"] == plans[1]["kernel"] == ("quad" if kernel == "4" else "pair")
+    assert plans[0]["tile"][0] > 0 and plans[0]["ctas_per_sm"] in (1, 2)
+    assert plans[1]["ctas_per_sm"] == 2  # untuned: the default plan
 
 
 @pytest.mark.parametrize("form,factor", [("fp32", 2.0), ("fp16", 4.0)])
