@@ -90,6 +90,8 @@ cudaError_t launch_acnet8_tc4(const float* biases, const float* alphas, int bloc
     cudaError_t err = cudaMemsetAsync(counter, 0, sizeof(int), stream);
     if (err != cudaSuccess) return err;
     const int grid = tiles < ctas ? tiles : ctas;
+    if (blocks == 4) stage_maps<GeoA8B4>(p, n, in);
+    else stage_maps<GeoA8B8>(p, n, in);
     err = blocks == 4 ? launch_acnet8_b4(type, c, bf16, p, grid, per_sm_cap, stream)
                       : launch_acnet8_b8(type, c, bf16, p, grid, per_sm_cap, stream);
     if (err == cudaSuccess) count_launch();

@@ -128,6 +128,12 @@ cudaError_t launch_acnet_legacy_tc4_core(const AcnetLegacyWeights& wts, const vo
     const int grid = tiles < ctas ? tiles : ctas;
     switch (shape)
     {
+    case 1: stage_maps<GeoQ1>(p, n, in); break;
+    case 2: stage_maps<GeoQ2>(p, n, in); break;
+    default: stage_maps<Geo0>(p, n, in); break;
+    }
+    switch (shape)
+    {
     case 1: err = launch_shape<GeoQ1, NetLegacy>(type, c, bf16, p, grid, per_sm_cap, stream); break;
     case 2: err = launch_shape<GeoQ2, NetLegacy>(type, c, bf16, p, grid, per_sm_cap, stream); break;
     default: err = launch_shape<Geo0, NetLegacy>(type, c, bf16, p, grid, per_sm_cap, stream); break;

@@ -36,6 +36,7 @@
 // pixel-shuffled and added to the source pixel (nearest) instead of
 // ACNetLegacy's 2x2 transposed conv.  The halo is the number of 3x3
 // layers: 9 (ACNetLegacy), 6 (ACNet<8> B4), 10 (B8).
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -47,6 +48,7 @@
 #include "device_common.cuh"
 #include "kernels.hpp"
 #include "tc_ptx.cuh"
+#include "tma_host.hpp"
 
 namespace acgb {
 namespace tcv4 {
@@ -96,6 +98,11 @@ struct Geo
     static_assert(WW * WH <= NBLK * 512, "window must fit the quad blocks");
     static_assert(UVH * 2 * TW * 3 * 4 <= ACT_BYTES, "chroma sums must fit the activation buffer");
     static_assert(PADQ >= QPR + 1, "taps of the first and last rows stay inside the planes");
+    // Bytes per row of the TMA-staged input window of a C-channel u8 image:
+    // the window's WW * C bytes plus up to 15 bytes in front of them (the
+    // box starts on a 16-byte boundary), rounded up to 16.
+    template <int C>
+    static constexpr int stage_bx() { return (WW * C + 15 + 15) / 16 * 16; }
 };
 
 template <class G, typename T, int C>
@@ -108,7 +115,15 @@ struct Layout
     static constexpr int uv_bytes = C == 1 ? 0 : (UVW * UVH * (C - 1) * static_cast<int>(sizeof(T)) + 15) / 16 * 16;
     static constexpr int lut_off = uv_off + uv_bytes;
     static constexpr int lut_bytes = sizeof(T) == 1 ? 1024 : 0;
-    static constexpr int misc_off = lut_off + lut_bytes;
+    // TMA-staged input window (u8 images of 1 or 3 channels: the box of a
+    // window row fits one 256-byte TMA box row, and two CTAs still share an
+    // SM); 4-channel and 16/32-bit images load the window directly.
+    static constexpr bool STAGE = sizeof(T) == 1 && C != 4;
+    static constexpr int BX = STAGE ? G::template stage_bx<C>() : 0;
+    static_assert(BX <= 256, "a staged window row must fit one TMA box row");
+    static constexpr int stage_off = (lut_off + lut_bytes + 127) / 128 * 128;
+    static constexpr int stage_bytes = STAGE ? G::WH * BX : 0;
+    static constexpr int misc_off = stage_off + stage_bytes;
     static constexpr int smem = misc_off + 256;
 };
 
@@ -117,6 +132,7 @@ struct Image4
     Plane in, out;
     int tiles_x;
     int tile0;
+    int staged;  // the input window is TMA-staged through tmap[image] (u8, 1 or 3 channels)
 };
 
 struct Params
@@ -131,7 +147,11 @@ struct Params
     int* tile_counter;
     int* status;
     Image4 img[kMaxImages];
+    // 2-D tensor maps over the input images as rows of bytes (w * channels
+    // by h, the image's pitch), box Layout::BX x WH; used where img[i].staged.
+    alignas(64) CUtensorMap tmap[kMaxImages];
 };
+static_assert(sizeof(Params) <= 32764, "kernel parameters must fit the 32 KB parameter space");
 
 template <bool BF16>
 __device__ __forceinline__ uint4 pack8_plain(const float* v)
@@ -295,8 +315,11 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
     volatile int* tile_slot = reinterpret_cast<volatile int*>(smem + L::misc_off + 124);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + L::misc_off + 128);
     uint32_t* gbar = reinterpret_cast<uint32_t*>(smem + L::misc_off + 132);
+    uint64_t* tbar = reinterpret_cast<uint64_t*>(smem + L::misc_off + 136);  // staging load of a window
+    volatile int* next_slot = reinterpret_cast<volatile int*>(smem + L::misc_off + 144);
     unsigned char* act = smem + L::ACT_OFF;
     unsigned char* bring = smem + L::B_OFF;
+    unsigned char* stage = smem + L::stage_off;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const bool mma_warp = warp >= NEPI;
@@ -309,6 +332,7 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
         // two blocks x four lane-quarter warps arrive per round and layer
         for (int r = 0; r < NROUND; r++) tc::mbar_init(&round_bar[r], 8);
         for (int i = 0; i < NBUF; i++) tc::mbar_init(&bbar[i], 1);
+        tc::mbar_init(tbar, 1);
         tc::fence_mbar_init();
         *abort_flag = 0;
         *gbar = 0;
@@ -343,9 +367,39 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
 
     uint32_t layers_done = 0;  // layers completed by this CTA over all its tiles
     uint32_t gbar_gen = 0;
+    uint32_t stage_waits = 0;   // staging loads waited on (every thread alike)
+    uint32_t stage_issued = 0;  // staging loads issued (thread 0)
+    // Thread 0 takes the CTA's next tile from the queue (the first one here,
+    // each following one during the last layer of the current tile); when
+    // the tile's image is staged it starts the TMA load of the tile's input
+    // window (rows gy0 .. gy0 + WH - 1, bytes from the 16-byte boundary at or
+    // before column gx0; outside the image the box reads zeros, which the
+    // prologue never uses) into the staging buffer, so the load overlaps the
+    // current tile's last layer.
+    auto take_tile = [&](volatile int* slot) {
+        const int t = *abort_flag ? P.ntiles : atomicAdd(P.tile_counter, 1);
+        *slot = t;
+        if constexpr (L::STAGE)
+        {
+            if (t < P.ntiles)
+            {
+                int j = 0;
+                while (j + 1 < P.nimg && P.img[j + 1].tile0 <= t) j++;
+                const Image4& J = P.img[j];
+                if (J.staged)
+                {
+                    const int loc = t - J.tile0;
+                    const int sx = ((loc % J.tiles_x) * TW - HALO) * C, sy = (loc / J.tiles_x) * TH - HALO;
+                    tc::mbar_arrive_expect_tx(tbar, static_cast<uint32_t>(WH * L::BX));
+                    tc::tma_load_2d(stage, &P.tmap[j], sx & ~15, sy, tbar);
+                    stage_issued++;
+                }
+            }
+        }
+    };
+    if (tid == 0) take_tile(tile_slot);
     for (;;)
     {
-        if (tid == 0) *tile_slot = *abort_flag ? P.ntiles : atomicAdd(P.tile_counter, 1);
         __syncthreads();
         const int tile = *tile_slot;
         if (tile >= P.ntiles) break;
@@ -362,6 +416,19 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
                            (store_px2_align<T, C>() - 1)) == 0;
 
         // ---- prologue (all warps): window luma as layer-0 input slots (+ chroma region) ----
+        // A staged window is read from shared memory once its TMA load
+        // completed (bounded wait); otherwise straight from the image.
+        bool staged = false;
+        if constexpr (L::STAGE)
+        {
+            if (I.staged)
+            {
+                staged = true;
+                wait_bar(tbar, stage_waits & 1u, abort_flag);
+                stage_waits++;
+            }
+        }
+        const int sx0 = (gx0 * C) & ~15;  // first byte column of the staged box
         constexpr int PER = (WW * WH + THREADS - 1) / THREADS;
         for (int k0 = 0; k0 < PER; k0 += 4)
         {
@@ -374,7 +441,12 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
                 {
                     const int wy = i / WW, wx = i - wy * WW;
                     const int gx = clampi(gx0 + wx, 0, W - 1), gy = clampi(gy0 + wy, 0, H - 1);
-                    const T* src = row_ptr<T>(I.in.ptr, I.in.pitch, gy) + gx * C;
+                    const T* src;
+                    if constexpr (L::STAGE)
+                        src = staged ? reinterpret_cast<const T*>(stage + (gy - gy0) * L::BX + gx * C - sx0)
+                                     : row_ptr<T>(I.in.ptr, I.in.pitch, gy) + gx * C;
+                    else
+                        src = row_ptr<T>(I.in.ptr, I.in.pitch, gy) + gx * C;
 #pragma unroll
                     for (int c = 0; c < C; c++) px[k][c] = src[c];
                 }
@@ -497,6 +569,12 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
             const int q = warp & 3, g = warp >> 2;
             for (int l = 0; l < NL; l++)
             {
+                // Near the end of the tile (the prologue read the staging
+                // buffer long before): take the next tile and start its
+                // window's load, late enough not to hold a tile another CTA
+                // could start sooner.
+                if (l == LAST && tid == 0) take_tile(next_slot);
+                __syncwarp();
                 const uint32_t parity = (layers_done + static_cast<uint32_t>(l)) & 1u;
                 const LayerRange<G> R(l, ix0, ix1, iy0, iy1);
                 uint32_t slopes[4] = {0u, 0u, 0u, 0u};
@@ -656,16 +734,36 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
+        if (tid == 0) *tile_slot = *next_slot;
     }
     // B loads still in flight (issued ahead for tiles that did not come) must
     // land before the CTA exits; bounded by time, not cut short by an abort.
     if (loader)
         for (uint32_t g2 = layers_done; g2 < issued; g2++)
             if (!tc::mbar_wait_ns(&bbar[g2 % NBUF], (g2 / NBUF) & 1u, kWaitNs)) *abort_flag = 1;
+    // likewise a staging load whose tile was not processed (after an abort)
+    if (tid == 0 && stage_issued > stage_waits && !tc::mbar_wait_ns(tbar, stage_waits & 1u, kWaitNs)) *abort_flag = 1;
     if (tid == 0 && *abort_flag) atomicExch(P.status, 1);
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, TMEM_COLS);
+}
+
+// Host: the tensor maps of the images whose input windows the kernel stages
+// by TMA (u8 with 1 or 3 channels, 16-byte aligned base and pitch; the
+// others keep img[i].staged = 0 and are loaded directly).
+// AC_GB300_TMA_IN=0 turns staging off (a check that both paths agree).
+template <class G>
+inline void stage_maps(Params& p, int n, const Plane* in)
+{
+    for (int i = 0; i < n; i++) p.img[i].staged = 0;
+    const int c = in[0].channels;
+    if (n <= 0 || in[0].type != kU8 || c == 4) return;
+    if (const char* e = std::getenv("AC_GB300_TMA_IN"))
+        if (std::atoi(e) == 0) return;
+    const int bx = c == 1 ? G::template stage_bx<1>() : G::template stage_bx<3>();
+    for (int i = 0; i < n; i++)
+        if (encode_tmap_2d(&p.tmap[i], in[i].ptr, 1, in[i].w * c, in[i].h, in[i].pitch, bx, G::WH)) p.img[i].staged = 1;
 }
 
 template <class G, class NET, typename T, int C, bool BF16>

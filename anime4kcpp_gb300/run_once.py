@@ -1,10 +1,13 @@
 """Run one upscale of a seeded synthetic frame through the device-pointer
 entry point, a fixed number of times (used for kernel profiling); with
 --batch N, N such frames per call through the batch entry point (one
-persistent launch per call in the tensor-core forms).
+persistent launch per call in the tensor-core forms); with --yuv, one planar
+10-bit YUV 4:2:0 frame in u16 through the planar entry point (Y shifted by
+6 bits around the network, chroma resized).
 
     python -m anime4kcpp_gb300.run_once --form fp16 --size 1920x1080 --channels 3 --repeat 2
     python -m anime4kcpp_gb300.run_once --form fp16 --size 1920x1080 --channels 3 --batch 8 --repeat 2
+    python -m anime4kcpp_gb300.run_once --form fp16 --model arnet-b8 --size 1920x1080 --yuv --factor 4 --repeat 2
 """
 import argparse
 
@@ -20,6 +23,7 @@ def main():
     ap.add_argument("--factor", type=float, default=2.0)
     ap.add_argument("--repeat", type=int, default=2)
     ap.add_argument("--batch", type=int, default=0, help="frames per call through the batch entry point (0: single)")
+    ap.add_argument("--yuv", action="store_true", help="one planar 10-bit YUV 4:2:0 u16 frame (shift 6)")
     a = ap.parse_args()
     import torch
 
@@ -27,6 +31,18 @@ def main():
     from anime4kcpp_gb300 import build, synthetic
     build.build()
     w, h = (int(v) for v in a.size.split("x"))
+    if a.yuv:
+        f = int(a.factor)
+        planes = [synthetic.luma(h, w, np.uint16, seed=1, bits=10)] + \
+                 [synthetic.luma(h // 2, w // 2, np.uint16, seed=2 + k, bits=10) for k in range(2)]
+        frame = [torch.from_numpy(pl).cuda() for pl in planes]
+        out = [torch.empty((f * pl.shape[0], f * pl.shape[1]), dtype=torch.uint16, device="cuda") for pl in planes]
+        p = ac.Processor("cuda", 0, a.model, precision=a.form)
+        for _ in range(a.repeat):
+            p.process_yuv_device([frame], [out], a.factor, 6)
+        torch.cuda.synchronize()
+        print("ok yuv", a.form, a.size, "launches", ac.launch_count())
+        return
     if a.channels == 1:
         x = synthetic.luma(h, w, np.uint8, seed=1)
     else:

@@ -640,18 +640,19 @@ def time_serve(ac, torch, args, forms=("fp16", "fp32")):
 
     def warm(srv):
         # every model, format, factor and size once (processors, weights,
-        # work buffers and pool blocks of every size class)
+        # work buffers and pool blocks of every size class), one job at a
+        # time: each output slot goes back to its ring before the next job
         for ri in range(len(SERVE_RES)):
-            tickets = []
             for m in SERVE_MODELS:
                 for fmt in ("rgb", "yuv"):
                     for f in (2, 4):
-                        slot = free[(ri, f, fmt)].get()
-                        tickets.append((srv.submit(inputs[(ri, fmt)], rings[(ri, f, fmt)][slot], m, float(f),
-                                                   6 if fmt == "yuv" else 0), (ri, f, fmt), slot))
-            for t, key, slot in tickets:
-                srv.wait(t, timeout=600.0)
-                free[key].put(slot)
+                        key = (ri, f, fmt)
+                        slot = free[key].get_nowait()
+                        try:
+                            srv.wait(srv.submit(inputs[(ri, fmt)], rings[key][slot], m, float(f), 6 if fmt == "yuv" else 0),
+                                     timeout=600.0)
+                        finally:
+                            free[key].put(slot)
 
     def run(srv, arrivals, picks):
         done = queue.Queue()
