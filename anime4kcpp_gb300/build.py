@@ -124,7 +124,11 @@ def build(force=False, jobs=None, verbose=False):
     newest_obj = max(os.path.getmtime(o) for o in objs)
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest_obj:
         tmp = LIB + ".tmp"
-        cmd = [NVCC] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs + ["-lpthread", "-ldl", "-lrt"]
+        # -Bsymbolic: the library's own calls bind to its own definitions, so it
+        # can be loaded (RTLD_LOCAL) next to another library that exports the
+        # ac::core C++ symbols (the reference core with this library as backend)
+        cmd = [NVCC] + ARCH + ["-shared", "-cudart", "static", "-Xlinker", "-Bsymbolic", "-o", tmp] + objs + \
+            ["-lpthread", "-ldl", "-lrt"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), res.stdout + res.stderr))
