@@ -206,24 +206,39 @@ class ClockSampler:
                 "source": self.source}
 
 
-def cpu_baseline(seconds=12.0):
-    """The reference CPU path on this host's cores over a bounded sample of the
-    workload: whole 1080p frames until ~`seconds` of work."""
+def reference_cpu_path():
+    """The reference's CPU path as it runs on this host: the reference's own
+    processor where it was compiled here (oracle/_ref), else the oracle's
+    restatement of it in the operation order of the backend the reference
+    selects on this host (aarch64: its NEON backend, as 4-lane vectors;
+    x86-64: the same 4-lane order).  Returns (run(frame), kind, backend)."""
+    import platform
+
     import oracle
-    frame = make_frames(1, seed=100)[0]
     cores = os.cpu_count() or 1
-    use_ref = False
     if oracle.ref_available():
         try:
             oracle.ref()
-            use_ref = True
+            name = oracle.ref().acref_name(MODEL.encode(), 0)
+            return (lambda f: oracle.ref_process(f, FACTOR, MODEL, arch=0)), "reference", \
+                (name.decode() if name else "reference CPU processor")
         except OSError:
-            use_ref = False
+            pass
+    backend = "restated %s backend order (4-lane vectors), %s, %d threads" % (
+        "NEON" if platform.machine() in ("aarch64", "arm64") else "NEON-order", platform.machine(), cores)
+    return (lambda f: oracle.process(f, FACTOR, MODEL, threads=cores, order="neon")), "port", backend
+
+
+def cpu_baseline(seconds=12.0):
+    """The reference CPU path on this host's cores over a bounded sample of the
+    workload: whole 1080p frames until ~`seconds` of work."""
+    frame = make_frames(1, seed=100)[0]
+    cores = os.cpu_count() or 1
+    run, kind, backend = reference_cpu_path()
+    use_ref = kind == "reference"
 
     def one():
-        if use_ref:
-            return oracle.ref_process(frame, FACTOR, MODEL, arch=0)
-        return oracle.process(frame, FACTOR, MODEL, threads=cores)
+        return run(frame)
 
     one()  # warm-up
     n, t0 = 0, time.perf_counter()
@@ -234,25 +249,20 @@ def cpu_baseline(seconds=12.0):
         if el >= seconds or n >= 20:
             break
     return {"value": OW * OH * n / el / 1e6, "unit": "Mpx/s", "cores": cores,
-            "kind": "reference" if use_ref else "port",
+            "kind": "reference" if use_ref else "port", "backend": backend,
             "sample": "%d full 1920x1080 RGB u8 frames x2 (%.1f s)" % (n, el)}
 
 
 def run_reference(args, rank):
     if rank != 0:
         return None
-    import oracle
     frame = make_frames(1, seed=100)[0]
     cores = os.cpu_count() or 1
-    use_ref = False
-    if oracle.ref_available():
-        try:
-            oracle.ref()
-            use_ref = True
-        except OSError:
-            use_ref = False
-    fn = (lambda: oracle.ref_process(frame, FACTOR, MODEL, arch=0)) if use_ref else \
-         (lambda: oracle.process(frame, FACTOR, MODEL, threads=cores))
+    run, kind, backend = reference_cpu_path()
+    use_ref = kind == "reference"
+
+    def fn():
+        return run(frame)
     for _ in range(args.warmup):
         fn()
     t0 = time.perf_counter()
@@ -266,7 +276,7 @@ def run_reference(args, rank):
         "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": DATA, "impl": "reference",
         "config": {"workload": WORKLOAD, "frames_per_step": 1, "note": "bounded sample: one frame per step on host cores"},
-        "cpu_baseline": {"value": value, "unit": "Mpx/s", "cores": cores, "kind": kind,
+        "cpu_baseline": {"value": value, "unit": "Mpx/s", "cores": cores, "kind": kind, "backend": backend,
                          "sample": "%d steps of one 1920x1080 RGB u8 frame x2" % args.steps},
         "e2e": {"value": value, "unit": "Mpx/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

@@ -57,6 +57,7 @@ def lib():
             L = ctypes.CDLL(so)
             vp, i, f, d, fp, dp = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p
             L.orc_acnet_legacy_x2.argtypes = [vp, i, i, i, i, vp, i, fp, fp, i]
+            L.orc_acnet_legacy_x2_simd4.argtypes = [vp, i, i, i, i, vp, i, fp, fp, i]
             L.orc_acnet_legacy_x2_f64.argtypes = [vp, i, i, i, i, dp, fp, fp, i]
             L.orc_arnet_x2.argtypes = [vp, i, i, i, i, vp, i, fp, fp, fp, i, i]
             L.orc_arnet_x2_f64.argtypes = [vp, i, i, i, i, dp, fp, fp, fp, i, i]
@@ -71,7 +72,7 @@ def lib():
             L.orc_resize_mt.argtypes = [vp, i, i, i, i, i, vp, i, i, i, i, i]
             L.orc_resize_coeffs.argtypes = [i, i, i, vp, vp, i]
             L.orc_arnet_synth.argtypes = [i, ctypes.c_uint64, fp, fp, fp]
-            for fn in ("orc_acnet_legacy_x2", "orc_acnet_legacy_x2_f64", "orc_arnet_x2", "orc_arnet_x2_f64",
+            for fn in ("orc_acnet_legacy_x2", "orc_acnet_legacy_x2_simd4", "orc_acnet_legacy_x2_f64", "orc_arnet_x2", "orc_arnet_x2_f64",
                        "orc_acnet8_x2", "orc_acnet8_x2_f64", "orc_f3_x2_f64", "orc_artcnn_x2", "orc_fsrcnnx_x2",
                        "orc_rgb2yuv", "orc_yuv2rgb", "orc_resize", "orc_resize_mt", "orc_resize_coeffs", "orc_arnet_synth"):
                 getattr(L, fn).restype = ctypes.c_int
@@ -224,8 +225,10 @@ def f3_weights(family, F, kind):
 
 # --------------------------------------------------------------- primitives
 
-def luma_x2(y, model, threads=0, f64=False):
-    """One x2 luma pass of ``model`` over a 2-D plane (u8/u16/f32)."""
+def luma_x2(y, model, threads=0, f64=False, order="generic"):
+    """One x2 luma pass of ``model`` over a 2-D plane (u8/u16/f32).  ``order``
+    "neon" runs ACNetLegacy in the operation order of the reference's NEON
+    backend (4-lane partial sums; the CPU baseline on aarch64 hosts)."""
     y = _plane(y)
     h, w = y.shape
     t = _TYPE_OF[y.dtype]
@@ -250,7 +253,8 @@ def luma_x2(y, model, threads=0, f64=False):
         out = np.empty((2 * h, 2 * w), y.dtype)
         if fam == "acnet_legacy":
             k, b = acnet_legacy_weights(var)
-            rc = lib().orc_acnet_legacy_x2(_p(y), w, h, y.strides[0], t, _p(out), out.strides[0], _p(k), _p(b), threads)
+            fn = lib().orc_acnet_legacy_x2_simd4 if order == "neon" else lib().orc_acnet_legacy_x2
+            rc = fn(_p(y), w, h, y.strides[0], t, _p(out), out.strides[0], _p(k), _p(b), threads)
         elif fam == "acnet8":
             k, b, a = acnet8_weights(*var)
             rc = lib().orc_acnet8_x2(_p(y), w, h, y.strides[0], t, _p(out), out.strides[0], _p(k), _p(b), _p(a), var[0],
@@ -319,10 +323,11 @@ def _ceil_log2(v):
 
 # ----------------------------------------------------------------- pipeline
 
-def process(img, factor, model, threads=0):
+def process(img, factor, model, threads=0, order="generic"):
     """Restatement of Processor::process (Processor.cpp:199-276) with an empty
     dst: luma passes, luma resize by the residual factor, chroma resize by the
-    full factor, colour merge.  ``img`` is (H, W) or (H, W, 3|4)."""
+    full factor, colour merge.  ``img`` is (H, W) or (H, W, 3|4).  ``order``
+    as for luma_x2."""
     img = _plane(img)
     power = _ceil_log2(factor) if factor > 2.0 else 1
     fxy = factor / float(1 << power)
@@ -331,14 +336,14 @@ def process(img, factor, model, threads=0):
     if img.ndim == 2:
         out = img
         for _ in range(power):
-            out = luma_x2(out, model, threads)
+            out = luma_x2(out, model, threads, order=order)
         if fxy != 1.0:
             out = resize(out, int(out.shape[1] * fxy), int(out.shape[0] * fxy))
         return out
     y, uv = rgb2yuv(img)
     out = y
     for _ in range(power):
-        out = luma_x2(out, model, threads)
+        out = luma_x2(out, model, threads, order=order)
     if fxy != 1.0:
         out = resize(out, int(out.shape[1] * fxy), int(out.shape[0] * fxy))
     h, w = img.shape[:2]

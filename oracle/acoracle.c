@@ -357,6 +357,156 @@ int orc_acnet_legacy_x2(const void* src, int w, int h, int sstride, int type,
     return 0;
 }
 
+/* ------------------------- 4-lane form of the reference's NEON backend */
+
+/* ACNetLegacy x2 in the operation order of the reference's NEON backend
+ * (core/internal/AC/Core/Internal/Processor/CPU/ARM/NEON.hpp, the backend
+ * its CPU processor selects on aarch64), written with portable 4-lane
+ * vectors (GCC vector extensions: NEON on aarch64, SSE on x86_64):
+ *
+ *   conv_cin1 (layer 0, 9 taps): s = r[0..3]*k[0..3] + r[4..7]*k[4..7] in 4
+ *     lanes, sum = hsum(s) + r[8]*k[8], out = sum + bias;
+ *   conv 8 -> 8 (conv_kernel with 4-lane groups): s[n] accumulates
+ *     r_p[4i..4i+3] * k[n][p][4i..4i+3] over taps p = 0..8 and i = 0, 1;
+ *     out[n] = bias[n] + hsum(s[n]);
+ *   dot<8> (the 2x2 transposed conv): hsum(s[0..3]*k[0..3] + s[4..7]*k[4..7]);
+ *   hsum(v) = (v0 + v1) + (v2 + v3) (pairwise adds).
+ *
+ * Multiply and add are separate roundings (vmlaq_f32's definition; this
+ * file is compiled without contraction).  Used as the timed CPU baseline of
+ * the reference's path on the GPU host; pinned to the reference's Generic
+ * output within its own ISA spread (1 LSB). */
+typedef float v4f __attribute__((vector_size(16)));
+
+static inline v4f v4_load(const float* p)
+{
+    v4f v;
+    memcpy(&v, p, sizeof(v));
+    return v;
+}
+static inline float v4_hsum(v4f v) { return (v[0] + v[1]) + (v[2] + v[3]); }
+
+typedef struct {
+    const void* src; int w, h, sstride, type;
+    const float* in; float* out;
+    void* dst; int dstride;
+    const float* k; const float* b; const float* k2;
+} s4_ctx;
+
+static void s4_l0_rows(void* p, int y0, int y1)
+{
+    s4_ctx* c = (s4_ctx*)p;
+    for (int y = y0; y < y1; y++)
+        for (int x = 0; x < c->w; x++)
+        {
+            int xs[3], ys[3];
+            taps3x3(x, y, c->w, c->h, xs, ys);
+            float r[9];
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++)
+                    r[i * 3 + j] = to_float(rowp(c->src, c->sstride, ys[i]), (size_t)xs[j], c->type);
+            const v4f r0 = v4_load(r), r1 = v4_load(r + 4);
+            float* out = c->out + ((size_t)y * c->w + x) * 8;
+            for (int n = 0; n < 8; n++)
+            {
+                const float* kp = c->k + n * 9;
+                v4f acc = r0 * v4_load(kp);
+                acc = acc + r1 * v4_load(kp + 4);
+                float sum = v4_hsum(acc);
+                float m = r[8] * kp[8];
+                sum = sum + m;
+                out[n] = std_max0(sum + c->b[n]);
+            }
+        }
+}
+
+static inline void s4_conv8(const float* const* rp, const float* k, const float* b, float* out)
+{
+    v4f acc[8];
+    for (int n = 0; n < 8; n++) acc[n] = (v4f){0.0f, 0.0f, 0.0f, 0.0f};
+    for (int t = 0; t < 9; t++)
+        for (int i = 0; i < 2; i++)
+        {
+            const v4f r = v4_load(rp[t] + 4 * i);
+            for (int n = 0; n < 8; n++) acc[n] = acc[n] + r * v4_load(k + n * 72 + t * 8 + 4 * i);
+        }
+    for (int n = 0; n < 8; n++) out[n] = b[n] + v4_hsum(acc[n]);
+}
+
+static void s4_l8_rows(void* p, int y0, int y1)
+{
+    s4_ctx* c = (s4_ctx*)p;
+    for (int y = y0; y < y1; y++)
+        for (int x = 0; x < c->w; x++)
+        {
+            int xs[3], ys[3];
+            taps3x3(x, y, c->w, c->h, xs, ys);
+            const float* rp[9];
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++)
+                    rp[i * 3 + j] = c->in + ((size_t)ys[i] * c->w + xs[j]) * 8;
+            float* out = c->out + ((size_t)y * c->w + x) * 8;
+            s4_conv8(rp, c->k, c->b, out);
+            for (int n = 0; n < 8; n++) out[n] = std_max0(out[n]);
+        }
+}
+
+static void s4_last_rows(void* p, int y0, int y1)
+{
+    s4_ctx* c = (s4_ctx*)p;
+    for (int y = y0; y < y1; y++)
+        for (int x = 0; x < c->w; x++)
+        {
+            int xs[3], ys[3];
+            taps3x3(x, y, c->w, c->h, xs, ys);
+            const float* rp[9];
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++)
+                    rp[i * 3 + j] = c->in + ((size_t)ys[i] * c->w + xs[j]) * 8;
+            float s[8];
+            s4_conv8(rp, c->k, c->b, s);
+            for (int n = 0; n < 8; n++) s[n] = std_max0(s[n]);
+            const v4f s0 = v4_load(s), s1 = v4_load(s + 4);
+            for (int dy = 0; dy < 2; dy++)
+            {
+                void* row = rowpw(c->dst, c->dstride, 2 * y + dy);
+                for (int dx = 0; dx < 2; dx++)
+                {
+                    const float* k2 = c->k2 + 8 * (dy * 2 + dx);
+                    v4f acc = s0 * v4_load(k2);
+                    acc = acc + s1 * v4_load(k2 + 4);
+                    from_float(row, (size_t)(2 * x + dx), c->type, v4_hsum(acc));
+                }
+            }
+        }
+}
+
+int orc_acnet_legacy_x2_simd4(const void* src, int w, int h, int sstride, int type,
+                              void* dst, int dstride, const float* kernels, const float* biases, int threads)
+{
+    if (!src || !dst || w <= 0 || h <= 0) return -22;
+    size_t n = (size_t)w * h * 8;
+    float* a = (float*)malloc(n * sizeof(float));
+    float* b = (float*)malloc(n * sizeof(float));
+    if (!a || !b) { free(a); free(b); return -12; }
+    s4_ctx c;
+    memset(&c, 0, sizeof(c));
+    c.src = src; c.w = w; c.h = h; c.sstride = sstride; c.type = type; c.dst = dst; c.dstride = dstride;
+    c.out = a; c.k = kernels; c.b = biases;
+    parallel_rows(s4_l0_rows, &c, h, threads);
+    for (int l = 1; l < 8; l++)
+    {
+        c.in = a; c.out = b; c.k = kernels + 72 + 576 * (l - 1); c.b = biases + 8 * l;
+        parallel_rows(s4_l8_rows, &c, h, threads);
+        float* t = a; a = b; b = t;
+    }
+    c.in = a; c.k = kernels + 72 + 576 * 7; c.b = biases + 64; c.k2 = kernels + 72 + 576 * 8;
+    parallel_rows(s4_last_rows, &c, h, threads);
+    free(a);
+    free(b);
+    return 0;
+}
+
 /* ARNet<8> x2 pass, CPUProcessor.cpp:1464-1491; weight offsets ARNet.hpp:26-70. */
 int orc_arnet_x2(const void* src, int w, int h, int sstride, int type,
                  void* dst, int dstride, const float* kernels, const float* biases, const float* alphas,

@@ -79,3 +79,20 @@ def test_fp64_oracle_agrees_with_reference(case):
         assert d.max() <= 1
     st = oracle.error_stats(want, exact, quant)
     assert st["frac_within_1lsb"] == 1.0
+
+
+LEGACY_CASES = [c for c in META if "legacy" in c["model"]]
+
+
+@pytest.mark.parametrize("case", LEGACY_CASES, ids=[c["name"] for c in LEGACY_CASES])
+def test_neon_order_port_within_reference_isa_spread(case):
+    """The 4-lane restatement of the reference's NEON backend (the timed CPU
+    baseline on the aarch64 GPU host) differs from the reference's Generic
+    output by at most what the reference's own SIMD backend does."""
+    x = GOLD[case["name"] + "/in"]
+    want = GOLD[case["name"] + "/generic"].astype(np.float64)
+    got = oracle.process(x, case["factor"], case["model"], threads=2, order="neon").astype(np.float64)
+    if case["dtype"] == "float32":
+        assert np.abs(got - want).max() <= 1e-4
+    else:
+        assert np.abs(got - want).max() <= 1
