@@ -954,10 +954,12 @@ def run_gb300(args, rank, world, local_rank):
                     "frac": achieved / fp32_peak, "traffic": traffic,
                     "peak_source": "computed 2 x 128 FP32 lanes x %d SMs x %.0f MHz (not in MEASURED_PEAKS)" % (props.multi_processor_count, sm_max)}
     else:
-        peak = float(peaks.get("bf16_tflops_sustained", 1700.0))
+        # the kernel is timed alone over a short region (tens of ms): the
+        # measured burst peak applies
+        peak = float(peaks.get("bf16_tflops", 1900.0))
         roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                    "traffic": traffic, "peak_source": "of measured (MEASURED_PEAKS.json bf16_tflops_sustained)"
-                    if "bf16_tflops_sustained" in peaks else "of fallback"}
+                    "traffic": traffic, "peak_source": "of measured (MEASURED_PEAKS.json bf16_tflops, burst)"
+                    if "bf16_tflops" in peaks else "of fallback (1.9 PFLOP/s burst)"}
 
     out = {
         "metric": METRIC, "value": rec["value"], "unit": "Mpx/s", "n_gpus": world, "steps": rec["steps"],
