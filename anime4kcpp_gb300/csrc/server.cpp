@@ -10,10 +10,11 @@
 // channel count and element type), copies the inputs in, runs one launch for
 // the batch, copies the results out and synchronises its stream.  Several
 // workers keep several jobs' copies and kernels in flight at once.  Half of
-// the workers ("express") serve only small jobs (up to a 1080p x2 ACNetLegacy
-// job's output) on high-priority streams, so a small job's blocks are
-// scheduled ahead of the pending blocks of large jobs; the other workers take
-// large jobs first and small ones when no large job waits.
+// the workers ("express") serve only small jobs (an input of at most
+// 1920x1080) on high-priority streams, so a small job's blocks are scheduled
+// ahead of the pending blocks of large jobs; the other workers take large
+// jobs first and small ones when no large job waits.  Copies go out in pieces
+// of at most 16 MB, so a small job's copy is not queued behind a large one.
 #include "server.hpp"
 
 #include <algorithm>
@@ -37,6 +38,25 @@ size_t round_block(size_t bytes)
 {
     const size_t mb = size_t(1) << 20, g = bytes <= (size_t(64) << 20) ? mb : (size_t(16) << 20);
     return std::max(mb, (bytes + g - 1) / g * g);
+}
+
+// A pitched copy issued as pieces of at most 16 MB: a copy engine serves
+// the streams' copies piece by piece, so a small job's copy is not queued
+// behind all of a large job's (a 7680x4320 x4 RGB result is 400 MB).
+cudaError_t copy_rows(void* dst, size_t dpitch, const void* src, size_t spitch, size_t row, int rows, cudaMemcpyKind kind,
+                      cudaStream_t st)
+{
+    const size_t piece = 16u << 20;
+    const int step = static_cast<int>(std::max<size_t>(1, piece / std::max<size_t>(row, 1)));
+    for (int y = 0; y < rows; y += step)
+    {
+        const int n = std::min(step, rows - y);
+        const cudaError_t e = cudaMemcpy2DAsync(static_cast<char*>(dst) + static_cast<size_t>(y) * dpitch, dpitch,
+                                                static_cast<const char*>(src) + static_cast<size_t>(y) * spitch, spitch, row, n,
+                                                kind, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 }  // namespace
@@ -168,8 +188,11 @@ bool Server::check(Job& j, std::string& err)
     }
     j.bytes = io + static_cast<size_t>(ws);
     j.batchable = fused && precision_ != Precision::FP32;
-    const double outPx = static_cast<double>(s.dst[0].w) * s.dst[0].h;  // the (luma) frame
-    j.express = spec.family == Family::ACNetLegacy ? outPx <= 1.3 * 3840.0 * 2160.0 : outPx <= 1.3 * 1708.0 * 960.0;
+    // Small jobs -- an input of at most 1920x1080 (any model, factor and
+    // format) -- are served by the express workers on high-priority streams,
+    // so their kernels are scheduled ahead of pending blocks of large jobs.
+    const double inPx = static_cast<double>(y.w) * y.h;
+    j.express = inPx <= 1920.0 * 1080.0;
     j.batchKey = s.model + "/" + std::to_string(y.c) + "/" + std::to_string(y.type);
     return true;
 }
@@ -434,8 +457,8 @@ void Server::workerLoop(int w)
             for (int p = 0; p < j->job.planes && e == cudaSuccess; p++)
             {
                 const HostPlane& h = j->job.src[p];
-                e = cudaMemcpy2DAsync(j->dsrc[p].ptr, j->dsrc[p].stride, h.ptr, h.stride,
-                                      static_cast<size_t>(h.w) * h.c * (h.type & 0xff), h.h, cudaMemcpyHostToDevice, st);
+                e = copy_rows(j->dsrc[p].ptr, j->dsrc[p].stride, h.ptr, h.stride,
+                              static_cast<size_t>(h.w) * h.c * (h.type & 0xff), h.h, cudaMemcpyHostToDevice, st);
             }
         int rc = proc ? 0 : -1;
         if (proc && e == cudaSuccess)
@@ -462,8 +485,8 @@ void Server::workerLoop(int w)
                 for (int p = 0; p < j->job.planes && e == cudaSuccess; p++)
                 {
                     const HostPlane& h = j->job.dst[p];
-                    e = cudaMemcpy2DAsync(h.ptr, h.stride, j->ddst[p].ptr, j->ddst[p].stride,
-                                          static_cast<size_t>(h.w) * h.c * (h.type & 0xff), h.h, cudaMemcpyDeviceToHost, st);
+                    e = copy_rows(h.ptr, h.stride, j->ddst[p].ptr, j->ddst[p].stride,
+                                  static_cast<size_t>(h.w) * h.c * (h.type & 0xff), h.h, cudaMemcpyDeviceToHost, st);
                 }
         const bool tc = precision_ != Precision::FP32;
         if (tc && e == cudaSuccess) e = tc_status_enqueue(st);

@@ -659,20 +659,24 @@ def time_serve(ac, torch, args, forms=("fp16", "fp32")):
         return arrivals, picks
 
     def warm(srv):
-        # every model, format, factor and size once (processors, weights,
-        # work buffers and pool blocks of every size class), one job at a
-        # time: each output slot goes back to its ring before the next job
-        for ri in range(len(SERVE_RES)):
+        # every model, format, factor and size (processors, weights, work
+        # buffers and pool blocks of every size class), largest first, as
+        # many concurrent jobs of each kind as there are workers (each worker
+        # thread keeps its own work buffers) as far as the output rings allow
+        for ri in reversed(range(len(SERVE_RES))):
             for m in SERVE_MODELS:
                 for fmt in ("rgb", "yuv"):
-                    for f in (2, 4):
+                    for f in (4, 2):
                         key = (ri, f, fmt)
-                        slot = free[key].get_nowait()
+                        held = [free[key].get_nowait() for _ in range(min(args.serve_workers, free[key].qsize()))]
                         try:
-                            srv.wait(srv.submit(inputs[(ri, fmt)], rings[key][slot], m, float(f), 6 if fmt == "yuv" else 0),
-                                     timeout=600.0)
+                            ts = [srv.submit(inputs[(ri, fmt)], rings[key][slot], m, float(f), 6 if fmt == "yuv" else 0)
+                                  for slot in held]
+                            for t in ts:
+                                srv.wait(t, timeout=600.0)
                         finally:
-                            free[key].put(slot)
+                            for slot in held:
+                                free[key].put(slot)
 
     def run(srv, arrivals, picks):
         done = queue.Queue()
@@ -1036,9 +1040,9 @@ def main():
     ap.add_argument("--family-steps", type=int, default=10, help="frames per family and form in the families workload (0: skip)")
     ap.add_argument("--cli-steps", type=int, default=10, help="steps of the CLI-default-model workload (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="serving workload length per form (0: skip)")
-    ap.add_argument("--serve-workers", type=int, default=6, help="worker streams of the serving loop")
+    ap.add_argument("--serve-workers", type=int, default=8, help="worker streams of the serving loop")
     ap.add_argument("--serve-load-seconds", type=float, default=8.0, help="length of each higher-rate FP16 serving run (0: skip)")
-    ap.add_argument("--serve-load-rates", default="600,1000", help="offered rates of the higher-rate FP16 serving runs, jobs/s")
+    ap.add_argument("--serve-load-rates", default="400,600,1000", help="offered rates of the higher-rate FP16 serving runs, jobs/s")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="serving workload arrival rate, jobs/s")
     ap.add_argument("--saturation-rate", type=float, default=4000.0, help="offered rate of the saturation run, jobs/s")
     args = ap.parse_args()
