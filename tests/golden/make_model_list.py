@@ -12,7 +12,9 @@ import re
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRC = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+SRC = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("AC_REFERENCE_ROOT", "")
+if not SRC:
+    sys.exit("usage: %s REFERENCE_ROOT (or set AC_REFERENCE_ROOT)" % sys.argv[0])
 
 text = open(os.path.join(SRC, "core", "include", "AC", "Specs.hpp")).read()
 models = []
