@@ -87,6 +87,10 @@ public:
     // one the first time a batch class is seen (no measurement launches in a
     // latency-sensitive request path).
     void setAutotune(bool on) { autotune_ = on; }
+    // Caps the CTAs per SM of this processor's persistent launches (0: the
+    // plan's own); the serving loop runs large jobs at one per SM, so a
+    // small job's blocks always find room on every SM.
+    void setCtasPerSm(int n) { tc3PerSm_ = n > 0 ? n : 0; }
     Precision precision() const { return precision_; }
     int device() const { return device_; }
     const ModelSpec& spec() const { return spec_; }

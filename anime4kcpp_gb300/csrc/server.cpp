@@ -111,10 +111,11 @@ Server::~Server()
     for (cudaStream_t s : streams_) cudaStreamDestroy(s);
 }
 
-GB300Processor* Server::processorFor(const std::string& model, std::string& err)
+GB300Processor* Server::processorFor(const std::string& model, bool express, std::string& err)
 {
     std::lock_guard<std::mutex> lock(procMutex_);
-    auto it = procs_.find(model);
+    const std::string key = (express ? "s/" : "l/") + model;
+    auto it = procs_.find(key);
     if (it == procs_.end())
     {
         std::shared_ptr<Processor> p = Processor::create("cuda", device_, model.c_str());
@@ -126,7 +127,11 @@ GB300Processor* Server::processorFor(const std::string& model, std::string& err)
         }
         g->setPrecision(precision_);
         g->setAutotune(false);  // the default tile plan: no measurement launches in the request path
-        it = procs_.emplace(model, p).first;
+        // A large job's persistent launch would hold both CTA slots of every
+        // SM until its tile queue drains; at one per SM a small job's blocks
+        // start at once beside it.
+        if (!express) g->setCtasPerSm(1);
+        it = procs_.emplace(key, p).first;
     }
     return static_cast<GB300Processor*>(it->second.get());
 }
@@ -193,7 +198,9 @@ bool Server::check(Job& j, std::string& err)
     // so their kernels are scheduled ahead of pending blocks of large jobs.
     const double inPx = static_cast<double>(y.w) * y.h;
     j.express = inPx <= 1920.0 * 1080.0;
-    j.batchKey = s.model + "/" + std::to_string(y.c) + "/" + std::to_string(y.type);
+    // jobs batch with jobs of their own class (a large job would slow an
+    // express batch down)
+    j.batchKey = std::string(j.express ? "s/" : "l/") + s.model + "/" + std::to_string(y.c) + "/" + std::to_string(y.type);
     return true;
 }
 
@@ -452,7 +459,7 @@ void Server::workerLoop(int w)
         }
         std::string err;
         cudaError_t e = cudaSuccess;
-        GB300Processor* proc = processorFor(batch[0]->job.model, err);
+        GB300Processor* proc = processorFor(batch[0]->job.model, batch[0]->express, err);
         for (auto& j : batch)
             for (int p = 0; p < j->job.planes && e == cudaSuccess; p++)
             {

@@ -94,7 +94,9 @@ private:
 
     void admitLoop();
     void workerLoop(int w);
-    GB300Processor* processorFor(const std::string& model, std::string& err);
+    // The processor of a model for small (express) or large jobs; large
+    // jobs' persistent launches run one CTA per SM.
+    GB300Processor* processorFor(const std::string& model, bool express, std::string& err);
     bool check(Job& j, std::string& err);
     bool allocate(Job& j, std::string& err);
     void release(Job& j);

@@ -725,6 +725,10 @@ def time_serve(ac, torch, args, forms=("fp16", "fp32")):
         r1080 = [r for r, m in res if m[0] == 2]
         lat1080 = np.array([r["latency_ms"] for r in r1080])
         lat1080x2 = np.array([r["latency_ms"] for r, m in res if m[0] == 2 and m[1] == 2 and m[3] == "rgb" and "acnet" in m[2]])
+        by_class = {}
+        for r, m in res:
+            if m[0] == 2:
+                by_class.setdefault((m[1], "arnet" if "arnet" in m[2] else "acnet", m[3]), []).append(r["device_ms"])
         return {
             "completed": len(ok), "failed": len(res) - len(ok), "jobs": len(res),
             "out_mpx_per_s": sum(m[4] for r, m in res if r["status"] == 0) / wall / 1e6,
@@ -735,6 +739,10 @@ def time_serve(ac, torch, args, forms=("fp16", "fp32")):
             "p99_ms_1080p_parts": {"admission": pct([r["queue_ms"] for r in r1080], 99),
                                    "worker_wait": pct([r["latency_ms"] - r["queue_ms"] - r["device_ms"] for r in r1080], 99),
                                    "device": pct([r["device_ms"] for r in r1080], 99)},
+            # 1080p classes (factor, family, format): jobs and p99 device ms
+            "p99_device_ms_1080p_by_class": {
+                "x%d/%s/%s" % (f, fam, fmt): {"jobs": len(v), "p99": pct(v, 99)}
+                for (f, fam, fmt), v in sorted(by_class.items())},
             "mean_queue_ms": float(np.mean([r["queue_ms"] for r, _ in res])) if res else None,
             "batched_jobs": int(st1["batched_jobs"] - st0["batched_jobs"]), "batches": int(st1["batches"] - st0["batches"]),
             "mean_jobs_per_launch_when_batched": (st1["batched_jobs"] - st0["batched_jobs"]) /
@@ -946,9 +954,11 @@ def run_gb300(args, rank, world, local_rank):
     # end to end through the C ABI with pinned host buffers
     pin_src = [torch.from_numpy(f).pin_memory() for f in host]
     pin_dst = [torch.empty((OH, OW, 3), dtype=torch.uint8).pin_memory() for _ in host]
-    e2e_steps = max(2, args.steps // 2)
+    # at least 40 steps (320 frames, ~60 ms): long enough that the host
+    # threads' start and drain do not weigh on the figure
+    e2e_steps = max(2 * args.steps, 40)
     el = time_e2e(ac, torch, proc, [p.numpy() for p in pin_src], [p.numpy() for p in pin_dst], frames, e2e_steps,
-                  max(1, args.warmup // 2), args.e2e_threads)
+                  max(2, args.warmup), args.e2e_threads)
     e2e_value = replica_mpx(OW * OH * frames * e2e_steps, max_over_ranks(el), world)
 
     peaks = measured_peaks()
@@ -988,7 +998,8 @@ def run_gb300(args, rank, world, local_rank):
                    "l2": "inputs larger than L2: 2 alternating batches of 8 distinct frames (50 MB in, 200 MB out per step)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_value, "unit": "Mpx/s", "h2d_bytes_per_step": H * W * 3 * frames,
-                "d2h_bytes_per_step": OH * OW * 3 * frames, "host_threads": args.e2e_threads},
+                "d2h_bytes_per_step": OH * OW * 3 * frames, "host_threads": args.e2e_threads, "steps": e2e_steps,
+                "call": "ac_processor_process per frame (C ABI, pinned host buffers, copies in the timed region)"},
         "gpu_launches": rec["launches"],
         "roofline": roofline,
         "forms": {k: ({kk: round(vv, 4) if isinstance(vv, float) else vv for kk, vv in v.items()}) for k, v in forms.items()},
