@@ -9,11 +9,12 @@
 // (ACNetLegacy x2 of interleaved images in a tensor-core form, same model,
 // channel count and element type), copies the inputs in, runs one launch for
 // the batch, copies the results out and synchronises its stream.  Several
-// workers keep several jobs' copies and kernels in flight at once.  Half of
-// the workers ("express") serve only small jobs (an input of at most
-// 1920x1080) on high-priority streams, so a small job's blocks are scheduled
-// ahead of the pending blocks of large jobs; the other workers take large
-// jobs first and small ones when no large job waits.  Copies go out in pieces
+// workers keep several jobs' copies and kernels in flight at once.  All but
+// one in eight of the workers ("express") serve only small jobs (an input of
+// at most 1920x1080) on high-priority streams, so a small job's blocks are
+// scheduled ahead of the pending blocks of large jobs; the others take large
+// jobs first (one or two large jobs on the device at a time) and small ones
+// when no large job waits.  Copies go out in pieces
 // of at most 16 MB, so a small job's copy is not queued behind a large one.
 #include "server.hpp"
 
@@ -71,7 +72,10 @@ Server::Server(int device, Precision precision, size_t budget, int workers, int 
         return;
     }
     workers = std::max(1, std::min(workers, 16));
-    express_ = workers / 2;
+    // One large-job worker per eight workers (at least one): large jobs run
+    // one or two at a time, so at most that much of the device is theirs
+    // when a small job arrives; the rest serve small jobs.
+    express_ = workers - std::max(1, workers / 8);
     int least = 0, greatest = 0;
     if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) least = greatest = 0;
     for (int w = 0; w < workers; w++)

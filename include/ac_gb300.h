@@ -167,8 +167,11 @@ AC_C_API int ac_gb300_model_params(const char* model, float* kernels, int kernel
  * and frame buffers resident on the device, batches compatible jobs as they
  * arrive (ACNetLegacy x2 of interleaved images in a tensor-core form: one
  * persistent launch) and overlaps the work of different jobs through
- * `workers` streams.  A job's result is the same as ac_processor_process
- * gives for it alone. */
+ * `workers` streams.  Jobs with an input of at most 1920x1080 are served on
+ * high-priority streams by all but one in eight of the workers; larger jobs
+ * run on the others, one or two at a time, their persistent launches at one
+ * CTA per SM, so a small job's work finds room on the device at once.  A
+ * job's result is the same as ac_processor_process gives for it alone. */
 typedef struct ACGB300HostPlane
 {
     void* ptr; /* host memory; pinned memory lets the copies overlap */
