@@ -120,7 +120,7 @@ def native():
             "ac_gb300_process_device_noalloc": (I, [pproc, I, P(ACGB300DeviceImage), P(ACGB300DeviceImage), V, I]),
             "ac_gb300_process_batch_device": (I, [pproc, I, P(ACGB300DeviceImage), P(ACGB300DeviceImage), D, V, I]),
             "ac_gb300_graph_replays": (ctypes.c_uint64, []),
-            "ac_gb300_last_plan": (I, [pproc, P(I), P(I), P(I), P(I)]),
+            "ac_gb300_last_plan": (I, [pproc, P(I), P(I), P(I), P(I), P(I)]),
             "ac_gb300_debug_fail_alloc": (None, [I]),
             "ac_gb300_process_yuv_device": (I, [pproc, I, I, P(ACGB300DeviceImage), P(ACGB300DeviceImage), D, I, V, I]),
             "ac_gb300_server_create": (V, [I, I, D, I, I]),
@@ -321,13 +321,15 @@ class Processor:
     def last_plan(self):
         """The persistent tensor-core launch plan of this thread's most
         recent call (``ac_gb300_last_plan``): kernel ("quad", "pair",
-        "quad-acnet8" or None), tile (w, h) and CTAs per SM."""
-        k, tw, th, ps = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        "quad-acnet8" or None), tile (w, h), CTAs per SM and fusion depth (9:
+        the whole network in one launch; 5: split in two launches, the tile
+        being the second launch's)."""
+        k, tw, th, ps, fd = (ctypes.c_int() for _ in range(5))
         if native().ac_gb300_last_plan(ctypes.byref(self._p), ctypes.byref(k), ctypes.byref(tw), ctypes.byref(th),
-                                       ctypes.byref(ps)) != AC_SUCCESS:
+                                       ctypes.byref(ps), ctypes.byref(fd)) != AC_SUCCESS:
             raise RuntimeError("no GPU processor")
         return {"kernel": {4: "quad", 3: "pair", 5: "quad-acnet8"}.get(k.value), "tile": (tw.value, th.value),
-                "ctas_per_sm": ps.value}
+                "ctas_per_sm": ps.value, "fusion_depth": fd.value}
 
     def profile(self, enable=True):
         native().ac_gb300_profile_enable(ctypes.byref(self._p), 1 if enable else 0)

@@ -356,19 +356,22 @@ uint64_t ac_gb300_graph_replays(void) { return acgb::graph_replays(); }
 
 void ac_gb300_debug_fail_alloc(int nth) { acgb::arm_alloc_failure(nth); }
 
-int ac_gb300_last_plan(ACProcessor* processor, int* kernel, int* tile_w, int* tile_h, int* ctas_per_sm)
+int ac_gb300_last_plan(ACProcessor* processor, int* kernel, int* tile_w, int* tile_h, int* ctas_per_sm,
+                       int* fusion_depth)
 {
     acgb::GB300Processor* g = gpu_of(processor);
     if (!g || !kernel || !tile_w || !tile_h || !ctas_per_sm) return AC_ERROR(AC_EINVAL);
     const acgb::GB300Processor::LastPlan p = g->lastPlan();
     int tw = 0, th = 0;
-    if (p.kernel == 4) acgb::acnet_tc4_shape(p.shape, &tw, &th);
+    if (p.kernel == 4 && p.depth == 5) acgb::acnet_tc4_split_tail_shape(&tw, &th);
+    else if (p.kernel == 4) acgb::acnet_tc4_shape(p.shape, &tw, &th);
     else if (p.kernel == 3) acgb::acnet_tc3_shape(p.shape, &tw, &th);
     else if (p.kernel == 5) acgb::acnet8_tc4_shape(g->spec().blocks, &tw, &th);
     *kernel = p.kernel;
     *tile_w = tw;
     *tile_h = th;
     *ctas_per_sm = p.perSm;
+    if (fusion_depth) *fusion_depth = p.kernel ? p.depth : 0;
     return AC_SUCCESS;
 }
 

@@ -142,6 +142,92 @@ cudaError_t launch_acnet_legacy_tc4_core(const AcnetLegacyWeights& wts, const vo
     return err;
 }
 
+void acnet_tc4_split_tail_shape(int* tw, int* th)
+{
+    *tw = tcv4::GeoTail::TW;
+    *th = tcv4::GeoTail::TH;
+}
+
+size_t acnet_tc4_split_map_bytes(int w, int h)
+{
+    return static_cast<size_t>((w * 16 + 255) & ~255) * h;
+}
+
+// The network in two launches (fusion depth 5 + 4): the head runs layers
+// 0 .. 4 over 54x54 tiles and writes layer 4's 16-bit activations (16 bytes
+// per pixel) to one map per image in `maps` (acnet_tc4_split_map_bytes each,
+// 256-byte aligned, in image order); the tail reads them over 46x57 tiles
+// and runs layers 5 .. 8, the transposed conv and the colour merge.  The
+// tail reads exactly the values the whole-network kernel keeps in shared
+// memory, and both parts' windows put every image column at the whole-
+// network windows' column parity (the grouping of the taps in the MMAs), so
+// the bytes are the same.  counters[0] / [1]: the two launches' tile
+// counters (zeroed here on `stream`).
+cudaError_t launch_acnet_legacy_tc4_split(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n,
+                                          const Plane* in, const Plane* out, const Phase2* phase2, void* maps,
+                                          int* counters, int ctas, cudaStream_t stream, int per_sm_cap)
+{
+    using namespace tcv4;
+    if (n <= 0) return cudaSuccess;
+    if (n > kMaxImages || !packed4 || !counters || !maps || ctas <= 0) return cudaErrorInvalidValue;
+    int* status = tc_status_buffer();
+    if (!status) return cudaErrorMemoryAllocation;
+    const int c = in[0].channels, type = in[0].type;
+    if (c > 1 && !phase2) return cudaErrorInvalidValue;
+    Params H, T;
+    std::memset(&H, 0, sizeof(Params));
+    std::memset(&T, 0, sizeof(Params));
+    H.bw = static_cast<const uint4*>(packed4);
+    T.bw = static_cast<const uint4*>(packed4) + static_cast<size_t>(kSplitK) * (BL_BYTES / 16);
+    for (int l = 0; l < kSplitK; l++)
+        for (int k = 0; k < 8; k++) H.bias[l][k] = wts.b[8 * l + k];
+    for (int l = 0; l < 9 - kSplitK; l++)
+        for (int k = 0; k < 8; k++) T.bias[l][k] = wts.b[8 * (kSplitK + l) + k];
+    for (int i = 0; i < 32; i++) T.k2[i] = wts.k[72 + 576 * 8 + i];
+    if (phase2) T.ph = *phase2;
+    size_t off = 0;
+    int th = 0, tt = 0;
+    for (int i = 0; i < n; i++)
+    {
+        if (in[i].channels != c || in[i].type != type || in[i].w <= 0 || in[i].h <= 0) return cudaErrorInvalidValue;
+        Plane m;
+        m.ptr = static_cast<char*>(maps) + off;
+        m.w = in[i].w;
+        m.h = in[i].h;
+        m.pitch = (in[i].w * 16 + 255) & ~255;
+        m.channels = 8;
+        m.type = type;
+        off += acnet_tc4_split_map_bytes(in[i].w, in[i].h);
+        H.img[i].in = in[i];
+        H.img[i].out = m;
+        H.img[i].map = m;
+        H.img[i].tiles_x = (in[i].w + GeoHead::TW - 1) / GeoHead::TW;
+        H.img[i].tile0 = th;
+        th += H.img[i].tiles_x * ((in[i].h + GeoHead::TH - 1) / GeoHead::TH);
+        T.img[i].in = in[i];
+        T.img[i].out = out[i];
+        T.img[i].map = m;
+        T.img[i].tiles_x = (in[i].w + GeoTail::TW - 1) / GeoTail::TW;
+        T.img[i].tile0 = tt;
+        tt += T.img[i].tiles_x * ((in[i].h + GeoTail::TH - 1) / GeoTail::TH);
+    }
+    H.nimg = T.nimg = n;
+    H.ntiles = th;
+    T.ntiles = tt;
+    H.tile_counter = counters;
+    T.tile_counter = counters + 1;
+    H.status = T.status = status;
+    stage_maps<GeoHead>(H, n, in);
+    cudaError_t err = cudaMemsetAsync(counters, 0, 2 * sizeof(int), stream);
+    if (err != cudaSuccess) return err;
+    err = launch_shape<GeoHead, NetLegacyHead<kSplitK>>(type, c, bf16, H, th < ctas ? th : ctas, per_sm_cap, stream);
+    if (err != cudaSuccess) return err;
+    count_launch();
+    err = launch_shape<GeoTail, NetLegacyTail<kSplitK>>(type, c, bf16, T, tt < ctas ? tt : ctas, per_sm_cap, stream);
+    if (err == cudaSuccess) count_launch();
+    return err;
+}
+
 cudaError_t launch_acnet_legacy_tc4(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n, const Plane* in,
                                     const Plane* out, const Phase2* phase2, int* counter, int ctas, cudaStream_t stream,
                                     int per_sm_cap, int shape)

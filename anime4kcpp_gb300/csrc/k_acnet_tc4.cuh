@@ -70,10 +70,31 @@ constexpr int kMaxImages = 64;
 static_assert(NBLK * 32 <= static_cast<int>(TMEM_COLS), "one 32-column accumulator per block");
 
 // ACNetLegacy: layer 0, eight 3x3 8->8 layers (ReLU), 2x2 transposed conv.
+// PART 0: the whole network in one launch.
 struct NetLegacy
 {
     static constexpr int NL = 9;  // MMA layers (3x3 convolutions)
     static constexpr bool ACN8 = false;
+    static constexpr int PART = 0;
+};
+// The network split in two launches at layer K (fusion depth K + (9 - K)):
+// the head runs layers 0 .. K-1 from the image and writes layer K-1's
+// 16-bit activations of its tile to an 8-channel map in global memory (the
+// values the whole-network kernel keeps in shared memory); the tail reads
+// the map, runs layers K .. 8, the transposed conv and the colour merge.
+template <int K>
+struct NetLegacyHead
+{
+    static constexpr int NL = K;
+    static constexpr bool ACN8 = false;
+    static constexpr int PART = 1;
+};
+template <int K>
+struct NetLegacyTail
+{
+    static constexpr int NL = 9 - K;
+    static constexpr bool ACN8 = false;
+    static constexpr int PART = 2;
 };
 // ACNet<8> with B blocks: layer 0, B 3x3 8->8 layers (PReLU), conv3x3 8->4.
 template <int B>
@@ -81,22 +102,33 @@ struct NetAcn8
 {
     static constexpr int NL = B + 2;
     static constexpr bool ACN8 = true;
+    static constexpr int PART = 0;
 };
 
-template <int TW_, int TH_, int HALO_>
+// COL: the tile ends in the colour merge (its chroma sums must fit the
+// dead activation buffer); a head part's tiles do not.
+// XE: extra window columns on each side beyond the halo.  A layer sums an
+// output's three horizontal taps in two MMAs, grouped (2 + 1) or (1 + 2) by
+// the pixel's column parity in the window, and the FP32 accumulator rounds
+// between them; with TW even every tile of a shape puts an image column at
+// the same parity, and shapes of one network with the same parity of
+// HALO + XE give identical bytes.
+template <int TW_, int TH_, int HALO_, bool COL_ = true, int XE_ = 0>
 struct Geo
 {
-    static constexpr int TW = TW_, TH = TH_, HALO = HALO_;
-    static constexpr int WW = TW + 2 * HALO, WH = TH + 2 * HALO;
+    static constexpr int TW = TW_, TH = TH_, HALO = HALO_, XE = XE_;
+    static constexpr int HX = HALO + XE;  // window columns left of the tile
+    static constexpr int WW = TW + 2 * HX, WH = TH + 2 * HALO;
     static constexpr int QPR = WW / 4;  // quads per window row
     static constexpr int PADQ = QPR + 2;
     static constexpr int PLANE_BYTES = (PADQ + NBLK * 128 + PADQ) * 16;
     static constexpr int ACT_BYTES = 4 * PLANE_BYTES;
     static constexpr int UVW = TW + 4, UVH = TH + 4;
-    static constexpr int UVX0 = HALO - 2;
+    static constexpr int UVX0 = HX - 2, UVY0 = HALO - 2;  // chroma region origin in the window
     static_assert(WW % 4 == 0, "window rows hold whole quads");
+    static_assert(TW % 2 == 0, "each image column at one window column parity");
     static_assert(WW * WH <= NBLK * 512, "window must fit the quad blocks");
-    static_assert(UVH * 2 * TW * 3 * 4 <= ACT_BYTES, "chroma sums must fit the activation buffer");
+    static_assert(!COL_ || UVH * 2 * TW * 3 * 4 <= ACT_BYTES, "chroma sums must fit the activation buffer");
     static_assert(PADQ >= QPR + 1, "taps of the first and last rows stay inside the planes");
     // Bytes per row of the TMA-staged input window of a C-channel u8 image:
     // the window's WW * C bytes plus up to 15 bytes in front of them (the
@@ -105,20 +137,21 @@ struct Geo
     static constexpr int stage_bx() { return (WW * C + 15 + 15) / 16 * 16; }
 };
 
-template <class G, typename T, int C>
+template <class G, typename T, int C, int PART = 0>
 struct Layout
 {
     static constexpr int ACT_OFF = 0;
     static constexpr int B_OFF = G::ACT_BYTES;
     static constexpr int UVW = G::UVW, UVH = G::UVH;
     static constexpr int uv_off = B_OFF + B_BYTES;
-    static constexpr int uv_bytes = C == 1 ? 0 : (UVW * UVH * (C - 1) * static_cast<int>(sizeof(T)) + 15) / 16 * 16;
+    static constexpr int uv_bytes =
+        (C == 1 || PART == 1) ? 0 : (UVW * UVH * (C - 1) * static_cast<int>(sizeof(T)) + 15) / 16 * 16;
     static constexpr int lut_off = uv_off + uv_bytes;
     static constexpr int lut_bytes = sizeof(T) == 1 ? 1024 : 0;
     // TMA-staged input window (u8 images of 1 or 3 channels: the box of a
     // window row fits one 256-byte TMA box row, and two CTAs still share an
     // SM); 4-channel and 16/32-bit images load the window directly.
-    static constexpr bool STAGE = sizeof(T) == 1 && C != 4;
+    static constexpr bool STAGE = sizeof(T) == 1 && C != 4 && PART != 2;
     static constexpr int BX = STAGE ? G::template stage_bx<C>() : 0;
     static_assert(BX <= 256, "a staged window row must fit one TMA box row");
     static constexpr int stage_off = (lut_off + lut_bytes + 127) / 128 * 128;
@@ -130,6 +163,7 @@ struct Layout
 struct Image4
 {
     Plane in, out;
+    Plane map;   // split network: the 8-channel 16-bit activation map (16 bytes per pixel)
     int tiles_x;
     int tile0;
     int staged;  // the input window is TMA-staged through tmap[image] (u8, 1 or 3 channels)
@@ -289,8 +323,8 @@ struct LayerRange
     {
         ry0 = max(l + 1, iy0);
         ry1 = min(WH - 2 - l, iy1);
-        rx0 = max(l + 1, ix0);
-        rx1 = min(WW - 2 - l, ix1);
+        rx0 = max(l + 1 + G::XE, ix0);
+        rx1 = min(WW - 2 - l - G::XE, ix1);
         b0 = ((ry0 * WW + rx0) >> 2) >> 7;
         b1 = ((ry1 * WW + rx1) >> 2) >> 7;
     }
@@ -300,12 +334,12 @@ template <class G, class NET, typename T, int C, bool BF16>
 __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_constant__ Params P)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
-    using L = Layout<G, T, C>;
-    constexpr int NL = NET::NL, LAST = NL - 1, HALO = G::HALO;
+    using L = Layout<G, T, C, NET::PART>;
+    constexpr int NL = NET::NL, LAST = NL - 1, HALO = G::HALO, HX = G::HX;
     static_assert(HALO == NL && NL <= NLMAX, "one halo pixel per 3x3 layer");
     constexpr int TW = G::TW, TH = G::TH, WW = G::WW, WH = G::WH, QPR = G::QPR, PADQ = G::PADQ;
     constexpr int PLANE_BYTES = G::PLANE_BYTES, ACT_BYTES = G::ACT_BYTES;
-    constexpr int UVW = G::UVW, UVH = G::UVH, UVX0 = G::UVX0;
+    constexpr int UVW = G::UVW, UVH = G::UVH, UVX0 = G::UVX0, UVY0 = G::UVY0;
     T* uvs = reinterpret_cast<T*>(smem + L::uv_off);
     float* lut = reinterpret_cast<float*>(smem + L::lut_off);
     uint64_t* mma_bar = reinterpret_cast<uint64_t*>(smem + L::misc_off);         // [NBLK]
@@ -389,7 +423,7 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
                 if (J.staged)
                 {
                     const int loc = t - J.tile0;
-                    const int sx = ((loc % J.tiles_x) * TW - HALO) * C, sy = (loc / J.tiles_x) * TH - HALO;
+                    const int sx = ((loc % J.tiles_x) * TW - HX) * C, sy = (loc / J.tiles_x) * TH - HALO;
                     tc::mbar_arrive_expect_tx(tbar, static_cast<uint32_t>(WH * L::BX));
                     tc::tma_load_2d(stage, &P.tmap[j], sx & ~15, sy, tbar);
                     stage_issued++;
@@ -407,7 +441,7 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
         while (im + 1 < P.nimg && P.img[im + 1].tile0 <= tile) im++;
         const Image4& I = P.img[im];
         const int local = tile - I.tile0;
-        const int gx0 = (local % I.tiles_x) * TW - HALO, gy0 = (local / I.tiles_x) * TH - HALO;
+        const int gx0 = (local % I.tiles_x) * TW - HX, gy0 = (local / I.tiles_x) * TH - HALO;
         const int W = I.in.w, H = I.in.h;
         const int ix0 = max(0, -gx0), ix1 = min(WW - 1, W - 1 - gx0);
         const int iy0 = max(0, -gy0), iy1 = min(WH - 1, H - 1 - gy0);
@@ -415,6 +449,34 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
         const bool wide = ((reinterpret_cast<uintptr_t>(I.out.ptr) | static_cast<uintptr_t>(I.out.pitch)) &
                            (store_px2_align<T, C>() - 1)) == 0;
 
+        if constexpr (NET::PART == 2)
+        {
+            // ---- prologue of a tail part: the window's layer-K input from the
+            // 16-bit activation map (clamped: taps that leave the image read
+            // the edge pixel, the clamp-to-edge of the intermediate map), and
+            // the chroma region from the source image ----
+            for (int i = tid; i < WW * WH; i += THREADS)
+            {
+                const int wy = i / WW, wx = i - wy * WW;
+                const int gx = clampi(gx0 + wx, 0, W - 1), gy = clampi(gy0 + wy, 0, H - 1);
+                *slot<G>(act, i) = *reinterpret_cast<const uint4*>(row_ptr<unsigned char>(I.map.ptr, I.map.pitch, gy) + gx * 16);
+            }
+            if constexpr (C > 1)
+                for (int e = tid; e < UVW * UVH; e += THREADS)
+                {
+                    const int uy = e / UVW, ux = e - uy * UVW;
+                    const int gx = clampi(gx0 + UVX0 + ux, 0, W - 1), gy = clampi(gy0 + UVY0 + uy, 0, H - 1);
+                    const T* sp = row_ptr<T>(I.in.ptr, I.in.pitch, gy) + gx * C;
+                    T px[C], yq, uvq[C - 1];
+#pragma unroll
+                    for (int c = 0; c < C; c++) px[c] = sp[c];
+                    rgb_to_yuv_q_lut<T, C>(px, yq, uvq, lut);
+#pragma unroll
+                    for (int c = 0; c < C - 1; c++) uvs[e * (C - 1) + c] = uvq[c];
+                }
+        }
+        else
+        {
         // ---- prologue (all warps): window luma as layer-0 input slots (+ chroma region) ----
         // A staged window is read from shared memory once its TMA load
         // completed (bounded wait); otherwise straight from the image.
@@ -463,16 +525,18 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
                     const int wy = i / WW, wx = i - wy * WW;
                     T uvq[C - 1];
                     rgb_to_yuv_q_lut<T, C>(px[k], yq, uvq, lut);
-                    const int ux = wx - UVX0, uy = wy - UVX0;
-                    if (ux >= 0 && ux < UVW && uy >= 0 && uy < UVH)
-                    {
+                    const int ux = wx - UVX0, uy = wy - UVY0;
+                    if constexpr (NET::PART == 0)
+                        if (ux >= 0 && ux < UVW && uy >= 0 && uy < UVH)
+                        {
 #pragma unroll
-                        for (int c = 0; c < C - 1; c++) uvs[(uy * UVW + ux) * (C - 1) + c] = uvq[c];
-                    }
+                            for (int c = 0; c < C - 1; c++) uvs[(uy * UVW + ux) * (C - 1) + c] = uvq[c];
+                        }
                 }
                 // clamped loads: taps that leave the image read the edge pixel
                 *slot<G>(act, i) = luma_slot<BF16>(to_float_lut<T>(yq, lut));
             }
+        }
         }
         // Layer 0's bias into the accumulators of the blocks this warp drains.
         if (!mma_warp)
@@ -581,7 +645,7 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
                 if constexpr (NET::ACN8)
                     if (l < LAST) pack_slopes<BF16>(P.alpha[l], slopes);
                 float* Hs = reinterpret_cast<float*>(act);  // last layer: the activations are dead once its MMAs completed
-                if constexpr (C > 1)
+                if constexpr (C > 1 && NET::PART != 1)
                 {
                     if (l == LAST)
                     {
@@ -666,6 +730,13 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
                                         if (xr) *slot<G>(act, p + WW + 1) = val;
                                     }
                                 }
+                                else if constexpr (NET::PART == 1)
+                                {
+                                    // head part: layer K-1's activations of the tile
+                                    // (this range is the tile inside the image) to the map
+                                    *reinterpret_cast<uint4*>(row_ptr_w<unsigned char>(I.map.ptr, I.map.pitch, gy0 + y) +
+                                                              (gx0 + x) * 16) = pack8<BF16>(v + 8 * kk);
+                                }
                                 else
                                 {
                                     T o[2][2];
@@ -717,7 +788,7 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
                                         row1[0] = o[1][0];
                                         row1[1] = o[1][1];
                                     }
-                                    else merge_block2_hv<T, C>(Hs, 2 * TW, x - HALO, y - HALO, P.ph, o, row0, row1, wide, lut);
+                                    else merge_block2_hv<T, C>(Hs, 2 * TW, x - HX, y - HALO, P.ph, o, row0, row1, wide, lut);
                                 }
                             }
                         }
@@ -772,7 +843,7 @@ cudaError_t launch_typed(const Params& p, int grid, int per_sm_cap, cudaStream_t
     // one-time set-up per device, thread-safe
     const LaunchSetup setup = device_once([] {
         cudaError_t err = cudaFuncSetAttribute(acnet_tc4_kernel<G, NET, T, C, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               Layout<G, T, C>::smem);
+                                               Layout<G, T, C, NET::PART>::smem);
         if (err != cudaSuccess) return LaunchSetup{err, 0, 0};
         err = cudaFuncSetAttribute(acnet_tc4_kernel<G, NET, T, C, BF16>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                    cudaSharedmemCarveoutMaxShared);
@@ -788,17 +859,17 @@ cudaError_t launch_typed(const Params& p, int grid, int per_sm_cap, cudaStream_t
         cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
         cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
         const int regs_cta = (fa.numRegs + 7) / 8 * 8 * THREADS;
-        const int need_smem = Layout<G, T, C>::smem + static_cast<int>(fa.sharedSizeBytes) + reserved;
+        const int need_smem = Layout<G, T, C, NET::PART>::smem + static_cast<int>(fa.sharedSizeBytes) + reserved;
         const int per_sm = (2 * need_smem <= smem_sm && 2 * regs_cta <= regs_sm && 2 * TMEM_COLS <= 512) ? 2 : 1;
         if (std::getenv("AC_GB300_DEBUG"))
             std::fprintf(stderr, "tc4 <%d,%d,%d>: %d CTAs per SM, %d bytes shared, %d registers\n", static_cast<int>(sizeof(T)),
-                         C, BF16 ? 1 : 0, per_sm, Layout<G, T, C>::smem, fa.numRegs);
+                         C, BF16 ? 1 : 0, per_sm, Layout<G, T, C, NET::PART>::smem, fa.numRegs);
         return LaunchSetup{cudaSuccess, per_sm, 0};
     });
     if (setup.err != cudaSuccess) return setup.err;
     const int per_sm = setup.per_sm;
     const int k = per_sm < per_sm_cap ? per_sm : (per_sm_cap < 1 ? 1 : per_sm_cap);
-    acnet_tc4_kernel<G, NET, T, C, BF16><<<grid * k, THREADS, Layout<G, T, C>::smem, stream>>>(p);
+    acnet_tc4_kernel<G, NET, T, C, BF16><<<grid * k, THREADS, Layout<G, T, C, NET::PART>::smem, stream>>>(p);
     return cudaGetLastError();
 }
 
@@ -832,9 +903,19 @@ cudaError_t launch_shape(int type, int c, bool bf16, const Params& p, int grid, 
     }
 }
 
+using GeoHead = Geo<54, 54, 5, false>;  // ACNetLegacy split at layer 5: head part, 64 x 64 window
+// tail part: 56 x 65 window, one extra column each side (the head's and the
+// whole network's column parity); its chroma sums fit the buffer
+using GeoTail = Geo<46, 57, 4, true, 1>;
+constexpr int kSplitK = 5;
+extern template cudaError_t launch_shape<GeoHead, NetLegacyHead<kSplitK>>(int, int, bool, const Params&, int, int, cudaStream_t);
+extern template cudaError_t launch_shape<GeoTail, NetLegacyTail<kSplitK>>(int, int, bool, const Params&, int, int, cudaStream_t);
 using Geo0 = Geo<46, 46, 9>;     // ACNetLegacy: 64 x 64 window (shape 0, the default)
 using GeoQ1 = Geo<62, 33, 9>;    // ACNetLegacy shape 1: 80 x 51 window (wide tiles)
 using GeoQ2 = Geo<30, 67, 9>;    // ACNetLegacy shape 2: 48 x 85 window (tall tiles)
+static_assert(GeoQ1::HX % 2 == Geo0::HX % 2 && GeoQ2::HX % 2 == Geo0::HX % 2 && GeoHead::HX % 2 == Geo0::HX % 2 &&
+                  GeoTail::HX % 2 == Geo0::HX % 2,
+              "every ACNetLegacy tiling sums the taps of an image column alike");
 // Shapes 1 and 2 are instantiated in k_acnet_tc4_shapes.cu (built in parallel).
 extern template cudaError_t launch_shape<GeoQ1, NetLegacy>(int, int, bool, const Params&, int, int, cudaStream_t);
 extern template cudaError_t launch_shape<GeoQ2, NetLegacy>(int, int, bool, const Params&, int, int, cudaStream_t);

@@ -144,6 +144,16 @@ void pack_acnet_tc4_weights(const AcnetLegacyWeights& wts, bool bf16, std::vecto
 cudaError_t launch_acnet_legacy_tc4(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n, const Plane* in,
                                     const Plane* out, const Phase2* phase2, int* counter, int ctas, cudaStream_t stream,
                                     int per_sm_cap = 2, int shape = 0);
+// The network in two launches, split at layer 5 (fusion depth 5 + 4): the
+// head writes layer 4's 16-bit activations to one map per image in `maps`
+// (acnet_tc4_split_map_bytes(w, h) each, in image order, 256-byte aligned),
+// the tail reads them and runs layers 5 .. 8 and the colour merge; the same
+// bytes as the whole-network launch.  counters: two device ints.
+size_t acnet_tc4_split_map_bytes(int w, int h);
+void acnet_tc4_split_tail_shape(int* tw, int* th);
+cudaError_t launch_acnet_legacy_tc4_split(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n,
+                                          const Plane* in, const Plane* out, const Phase2* phase2, void* maps,
+                                          int* counters, int ctas, cudaStream_t stream, int per_sm_cap);
 // The same with the caller's status word (`status`, 0 or 1 after a timed-out wait).
 cudaError_t launch_acnet_legacy_tc4_core(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n, const Plane* in,
                                          const Plane* out, const Phase2* phase2, int* counter, int* status, int ctas,

@@ -382,6 +382,7 @@ GB300Processor::GB300Processor(int device, const ModelSpec& spec) : spec_(spec)
     if (tc3Shape_ >= kTc3Shapes) tc3Shape_ = -1;
     if (const char* v = std::getenv("AC_GB300_TC3_PER_SM")) tc3PerSm_ = std::atoi(v);
     if (const char* v = std::getenv("AC_GB300_AUTOTUNE")) autotune_ = std::atoi(v) != 0;
+    if (const char* v = std::getenv("AC_GB300_FUSION_DEPTH")) fusionDepth_ = std::atoi(v) == 5 ? 5 : (std::atoi(v) == 9 ? 9 : 0);
     if (const char* v = std::getenv("AC_GB300_ARNET_TC")) arnetTc_ = std::atoi(v) != 0;
     phase2Ok_ = phase_weights(2, &phase2_.w[0][0]);
     int n = 0;
@@ -450,6 +451,7 @@ GB300Processor::~GB300Processor()
         ts.counter.release();
         ts.batchTmp.release();
         ts.yuvTmp.release();
+        ts.splitMap.release();
         for (auto& t : ts.tables) t.second.dev.release();
         for (auto& e : ts.events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
         for (auto& e : ts.pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -736,18 +738,18 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
             const bool bf16 = precision_ == Precision::BF16;
             if (tcKernel_ == 4)
             {
-                // persistent quad form (one tile shape, no autotune)
+                // persistent quad form: tile shape, CTAs per SM and fusion depth autotuned
                 const void* w = tcWeights(precision_, 3);
                 if (!w) err = cudaErrorMemoryAllocation;
                 else if ((err = ts.counter.ensure(256)) == cudaSuccess)
                 {
-                    int* counter = static_cast<int*>(ts.counter.ptr) + (ts.counterSlot++ & 63);
+                    // two counters (the split network's two launches)
+                    int* counter = static_cast<int*>(ts.counter.ptr) + (ts.counterSlot & 62);
+                    ts.counterSlot += 2;
                     bool ran = false;
-                    const Tc3Plan plan = tc3Plan(1, &in, &out, ph, w, bf16, counter, stream, ran, err, true);
-                    ts.lastPlan = LastPlan{4, plan.shape, plan.perSm};
-                    if (err == cudaSuccess && !ran)
-                        err = launch_acnet_legacy_tc4(*acnet_, w, bf16, 1, &in, &out, ph, counter,
-                                                      tc3Ctas_ > 0 ? tc3Ctas_ : smCount_, stream, plan.perSm, plan.shape);
+                    const Tc3Plan plan = tc3Plan(1, &in, &out, ph, w, bf16, counter, stream, ran, err, true, &ts.splitMap);
+                    ts.lastPlan = LastPlan{4, plan.shape, plan.perSm, plan.depth};
+                    if (err == cudaSuccess && !ran) err = launchQuad(ts, plan, 1, &in, &out, ph, w, bf16, counter, stream);
                 }
             }
             else
@@ -762,7 +764,7 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
                     int* counter = static_cast<int*>(ts.counter.ptr) + (ts.counterSlot++ & 63);
                     bool ran = false;
                     const Tc3Plan plan = tc3Plan(1, &in, &out, ph, w, bf16, counter, stream, ran, err);
-                    ts.lastPlan = LastPlan{3, plan.shape, plan.perSm};
+                    ts.lastPlan = LastPlan{3, plan.shape, plan.perSm, 9};
                     if (err == cudaSuccess && !ran)
                         err = launch_acnet_legacy_tc3(*acnet_, w, bf16, 1, &in, &out, ph, counter,
                                                       tc3Ctas_ > 0 ? tc3Ctas_ : smCount_, stream, plan.shape, plan.perSm);
@@ -882,16 +884,39 @@ static int ilog2(double v)
     return k;
 }
 
+size_t GB300Processor::splitMapBytes(int n, const Plane* in)
+{
+    size_t b = 0;
+    for (int i = 0; i < n; i++) b += acnet_tc4_split_map_bytes(in[i].w, in[i].h);
+    return b;
+}
+
+cudaError_t GB300Processor::launchQuad(ThreadState& ts, const Tc3Plan& plan, int n, const Plane* in, const Plane* out,
+                                       const Phase2* ph, const void* w, bool bf16, int* counter, cudaStream_t stream)
+{
+    const int ctas = tc3Ctas_ > 0 ? tc3Ctas_ : smCount_;
+    if (plan.depth == 5)
+    {
+        cudaError_t err = ts.splitMap.ensure(splitMapBytes(n, in));
+        if (err != cudaSuccess) return err;
+        return launch_acnet_legacy_tc4_split(*acnet_, w, bf16, n, in, out, ph, ts.splitMap.ptr, counter, ctas, stream,
+                                             plan.perSm);
+    }
+    return launch_acnet_legacy_tc4(*acnet_, w, bf16, n, in, out, ph, counter, ctas, stream, plan.perSm, plan.shape);
+}
+
 GB300Processor::Tc3Plan GB300Processor::tc3Plan(int n, const Plane* in, const Plane* out, const Phase2* ph, const void* w,
                                                 bool bf16, int* counter, cudaStream_t stream, bool& ran, cudaError_t& err,
-                                                bool quad)
+                                                bool quad, DeviceBuffer* mapBuffer)
 {
     ran = false;
     err = cudaSuccess;
     Tc3Plan plan;
     if (tc3Shape_ >= 0) plan.shape = tc3Shape_;
     if (tc3PerSm_ > 0) plan.perSm = tc3PerSm_;
-    if (!autotune_ || tc3Shape_ >= 0 || tc3PerSm_ > 0) return plan;
+    if (quad && fusionDepth_ != 0) plan.depth = fusionDepth_;
+    if (quad && plan.depth == 5) plan.shape = 0;  // the split network has its own tile shapes
+    if (!autotune_ || tc3Shape_ >= 0 || tc3PerSm_ > 0 || (quad && fusionDepth_ != 0)) return plan;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) return plan;
     double total = 0.0, sw = 0.0, sh = 0.0;
@@ -908,9 +933,10 @@ GB300Processor::Tc3Plan GB300Processor::tc3Plan(int n, const Plane* in, const Pl
         auto it = plans_.find(key);
         if (it != plans_.end()) return it->second;
     }
-    // Measure every shape x {2, 1} CTAs per SM: one warm launch, then two
-    // timed ones with events on the launching stream.  Each candidate writes
-    // the same bytes, so the output is valid afterwards.
+    // Measure every shape x {2, 1} CTAs per SM (quad kernel: and the split
+    // network x {2, 1}): one warm launch, then two timed ones with events on
+    // the launching stream.  Each candidate writes the same bytes, so the
+    // output is valid afterwards.
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if ((err = cudaEventCreate(&e0)) != cudaSuccess) return plan;
     if ((err = cudaEventCreate(&e1)) != cudaSuccess)
@@ -918,14 +944,21 @@ GB300Processor::Tc3Plan GB300Processor::tc3Plan(int n, const Plane* in, const Pl
         cudaEventDestroy(e0);
         return plan;
     }
+    // the split network's activation maps, only while it is a candidate
+    // (an allocation failure drops the candidate)
+    void* maps = nullptr;
+    if (quad && mapBuffer && mapBuffer->ensure(splitMapBytes(n, in)) == cudaSuccess) maps = mapBuffer->ptr;
     const int ctas = tc3Ctas_ > 0 ? tc3Ctas_ : smCount_;
     float best = 1e30f;
     Tc3Plan bestPlan = plan;
     auto launch = [&](int shape, int perSm) {
+        if (quad && shape == kTc4Shapes)
+            return launch_acnet_legacy_tc4_split(*acnet_, w, bf16, n, in, out, ph, maps, counter, ctas, stream, perSm);
         return quad ? launch_acnet_legacy_tc4(*acnet_, w, bf16, n, in, out, ph, counter, ctas, stream, perSm, shape)
                     : launch_acnet_legacy_tc3(*acnet_, w, bf16, n, in, out, ph, counter, ctas, stream, shape, perSm);
     };
-    const int shapes = quad ? kTc4Shapes : kTc3Shapes;
+    // quad kernel: "shape" kTc4Shapes stands for the split network
+    const int shapes = quad ? kTc4Shapes + (maps ? 1 : 0) : kTc3Shapes;
     for (int shape = 0; shape < shapes && err == cudaSuccess; shape++)
         for (int perSm = 2; perSm >= 1 && err == cudaSuccess; perSm--)
         {
@@ -939,7 +972,9 @@ GB300Processor::Tc3Plan GB300Processor::tc3Plan(int n, const Plane* in, const Pl
             if (err == cudaSuccess && ms < best)
             {
                 best = ms;
-                bestPlan.shape = shape;
+                const bool split = quad && shape == kTc4Shapes;
+                bestPlan.shape = split ? 0 : shape;
+                bestPlan.depth = split ? 5 : 9;
                 bestPlan.perSm = perSm;
             }
         }
@@ -1238,7 +1273,9 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
         if (!w) return fail(ts, "tensor-core weights", cudaErrorMemoryAllocation), false;
         cudaError_t err = ts.counter.ensure(256);
         if (err != cudaSuccess) return fail(ts, "device allocation", err), false;
-        int* counter = static_cast<int*>(ts.counter.ptr) + (ts.counterSlot++ & 63);
+        // two counters per launch (the split network's two launches)
+        int* counter = static_cast<int*>(ts.counter.ptr) + (ts.counterSlot & 62);
+        ts.counterSlot += 2;
         if (!phase2Ok_) return fail(ts, "chroma resample weights"), false;
         const Phase2& ph = phase2_;
         const int maxImages = std::min(quad ? acnet_tc4_max_images() : acnet_tc3_max_images(), 64);
@@ -1279,10 +1316,15 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
             bool ran = false;
             Tc3Plan plan;
             if (acn8) plan.perSm = tc3PerSm_ > 0 ? tc3PerSm_ : 2;  // one tile shape per ACNet<8> depth
-            else plan = tc3Plan(m, in, out, php, w, bf16, counter, s, ran, err, quad);
+            else plan = tc3Plan(m, in, out, php, w, bf16, counter, s, ran, err, quad, &ts.splitMap);
             if (err != cudaSuccess) return fail(ts, "batched upscale", err), false;
-            ts.lastPlan = LastPlan{acn8 ? 5 : (quad ? 4 : 3), plan.shape, plan.perSm};
+            // the split network's maps exist before a capture begins
+            if (quad && plan.depth == 5 && (err = ts.splitMap.ensure(splitMapBytes(m, in))) != cudaSuccess)
+                return fail(ts, "device allocation", err), false;
+            ts.lastPlan = LastPlan{acn8 ? 5 : (quad ? 4 : 3), plan.shape, plan.perSm, plan.depth};
             mix(static_cast<uint64_t>(plan.shape * 4 + plan.perSm));
+            mix(static_cast<uint64_t>(plan.depth));
+            mix(reinterpret_cast<uint64_t>(plan.depth == 5 ? ts.splitMap.ptr : nullptr));
             mix(static_cast<uint64_t>(quad));
             const int ctas = tc3Ctas_ > 0 ? tc3Ctas_ : smCount_;
             auto launchGroup = [&]() {
@@ -1292,8 +1334,7 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
                     return launch_acnet8_tc4(mp.biases.data(), mp.alphas.data(), spec_.blocks, w, bf16, m, in, out, php,
                                              counter, ctas, s, plan.perSm);
                 }
-                return quad ? launch_acnet_legacy_tc4(*acnet_, w, bf16, m, in, out, php, counter, ctas, s, plan.perSm,
-                                                      plan.shape)
+                return quad ? launchQuad(ts, plan, m, in, out, php, w, bf16, counter, s)
                             : launch_acnet_legacy_tc3(*acnet_, w, bf16, m, in, out, php, counter, ctas, s, plan.shape,
                                                       plan.perSm);
             };

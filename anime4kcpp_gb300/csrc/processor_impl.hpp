@@ -111,6 +111,7 @@ private:
     {
         int shape = 0;  // tile geometry of the persistent kernel
         int perSm = 2;  // CTAs per SM (cap)
+        int depth = 9;  // quad kernel: layers fused per launch, 9 (one launch) or 5 (split 5 + 4)
     };
     struct GraphEntry
     {
@@ -123,7 +124,7 @@ public:
     // (ACNet<8>), 0 none; tile shape index; CTAs per SM.
     struct LastPlan
     {
-        int kernel = 0, shape = 0, perSm = 0;
+        int kernel = 0, shape = 0, perSm = 0, depth = 9;
     };
     LastPlan lastPlan();
 
@@ -138,6 +139,7 @@ private:
         unsigned counterSlot = 0;
         DeviceBuffer batchTmp; // x2 intermediates of batched x4 passes
         DeviceBuffer yuvTmp;   // shifted Y planes of the YUV path
+        DeviceBuffer splitMap; // 16-bit activation maps of the split quad network
         std::map<std::tuple<int, int, int>, AxisTable> tables;
         bool ok = true;
         std::string err = "NO ERROR";
@@ -193,7 +195,13 @@ private:
     // image sizes) over every tile shape x {2, 1} CTAs per SM.  When it
     // measured, the launches already produced the output (`ran`).
     Tc3Plan tc3Plan(int n, const Plane* in, const Plane* out, const Phase2* ph, const void* w, bool bf16, int* counter,
-                    cudaStream_t stream, bool& ran, cudaError_t& err, bool quad = false);
+                    cudaStream_t stream, bool& ran, cudaError_t& err, bool quad = false, DeviceBuffer* maps = nullptr);
+    // The quad kernel's launch under `plan` (whole network, or split in two
+    // launches over ts.splitMap, which the caller sized with splitMapBytes);
+    // `counter` points at two device ints.
+    cudaError_t launchQuad(ThreadState& ts, const Tc3Plan& plan, int n, const Plane* in, const Plane* out,
+                           const Phase2* ph, const void* w, bool bf16, int* counter, cudaStream_t stream);
+    static size_t splitMapBytes(int n, const Plane* in);
 
     int device_ = -1;
     int smCount_ = 0;
@@ -211,6 +219,7 @@ private:
     int tcKernel_ = 4;               // tensor-core kernel: 4 persistent quad (default), 3 persistent pair, 2 pair-interleaved per tile, 1 one-pixel-per-row (AC_GB300_TC_KERNEL)
     int tc3Shape_ = -1;              // forced tile shape (AC_GB300_TC3_SHAPE), -1: autotuned
     int tc3PerSm_ = 0;               // forced CTAs per SM (AC_GB300_TC3_PER_SM), 0: autotuned
+    int fusionDepth_ = 0;            // forced quad-kernel fusion depth (AC_GB300_FUSION_DEPTH: 9 or 5), 0: autotuned
     bool autotune_ = true;           // AC_GB300_AUTOTUNE=0: default shape, two CTAs per SM
     std::map<std::tuple<int, int, int, int, int, int>, Tc3Plan> plans_;
     // x2 Catmull-Rom phase weights of the fused chroma resample, computed

@@ -463,8 +463,9 @@ def time_batch(ac, torch, args):
                      "steps": steps, "launches_per_batch": (ac.launch_count() - l0) / steps,
                      "graph_replays_per_batch": (ac.graph_replays() - r0) / steps}
         if form != "fp32":
-            res[form]["plan"] = dict(proc.last_plan(), chosen_by="autotuner: every tile shape x {2, 1} CTAs per SM "
-                                                                  "timed once for this batch class")
+            res[form]["plan"] = dict(proc.last_plan(), chosen_by="autotuner: every tile shape, and the network split "
+                                                                  "in two launches, x {2, 1} CTAs per SM, timed once "
+                                                                  "for this batch class")
         if not args.no_error_stats:
             res[form]["error"] = dict(error_vs_fp64(dsts[0].cpu().numpy(), imgs[0], BATCH_MODEL),
                                       sample="image 0 (%dx%d)" % (imgs[0].shape[1], imgs[0].shape[0]))

@@ -66,12 +66,17 @@ AC_C_API int ac_gb300_process_batch_device(ACProcessor* processor, int count, co
 /* The persistent tensor-core launch plan of the calling thread's most recent
  * call on this processor: *kernel 4 (the quad kernel, ACNetLegacy), 3 (the
  * pair kernel), 5 (the quad kernel, ACNet<8>) or 0 (no such launch yet);
- * *tile_w x *tile_h its tile shape; *ctas_per_sm the CTAs-per-SM cap.  The
- * plan is the autotuner's choice for the call's batch class, measured the
- * first time the class was seen, or the one the environment forced
- * (AC_GB300_TC3_SHAPE, AC_GB300_TC3_PER_SM).  Returns AC_SUCCESS or
+ * *tile_w x *tile_h its tile shape; *ctas_per_sm the CTAs-per-SM cap;
+ * *fusion_depth (may be NULL) the layers one launch runs: 9 for the whole
+ * network in one launch, 5 for the network split in two launches (layers
+ * 0-4 in 54x54 tiles writing a 16-bit activation map, then layers 5-8 and
+ * the colour epilogue in the reported 46x57 tiles).  The plan is the
+ * autotuner's choice for the call's batch class, measured the first time
+ * the class was seen, or the one the environment forced (AC_GB300_TC3_SHAPE,
+ * AC_GB300_TC3_PER_SM, AC_GB300_FUSION_DEPTH).  Returns AC_SUCCESS or
  * AC_ERROR(AC_EINVAL). */
-AC_C_API int ac_gb300_last_plan(ACProcessor* processor, int* kernel, int* tile_w, int* tile_h, int* ctas_per_sm);
+AC_C_API int ac_gb300_last_plan(ACProcessor* processor, int* kernel, int* tile_w, int* tile_h, int* ctas_per_sm,
+                                int* fusion_depth);
 
 /* Host-side fault injection for tests of the failure paths: arms the
  * nth next device allocation of the library's work buffers or serving pool

@@ -101,6 +101,45 @@ def test_tile_shapes_and_cta_caps_give_identical_bytes(c, kernel, monkeypatch):
         assert np.array_equal(o, outs[0])
 
 
+def _source(h, w, c, dtype, seed):
+    x = synthetic.rgb_u8(h, w, seed=seed, alpha=(c == 4)) if c > 1 else synthetic.luma(h, w, np.uint8, seed=seed)
+    if dtype == "uint16":
+        return (x.astype(np.uint16) * 257).astype(np.uint16)
+    if dtype == "float32":
+        return (x.astype(np.float32) / 255.0).astype(np.float32)
+    return x
+
+
+@pytest.mark.parametrize("form", ["fp16", "bf16"])
+@pytest.mark.parametrize("dtype", ["uint8", "uint16", "float32"])
+@pytest.mark.parametrize("c", [1, 3, 4])
+def test_split_network_gives_identical_bytes(c, dtype, form, monkeypatch):
+    """The quad kernel's network split in two launches (layers 0-4 writing
+    a 16-bit activation map, layers 5-8 and the colour merge reading it)
+    against the whole network in one launch: the same bytes, for one image
+    and for a batch of images of several sizes (tiles at every edge, images
+    smaller than a tile)."""
+    monkeypatch.setenv("AC_GB300_TC_KERNEL", "4")
+    imgs = [_source(h, w, c, dtype, seed=h * 3 + w) for h, w in [(131, 150), (1, 1), (7, 93), (54, 54), (200, 49)]]
+    srcs = [torch.from_numpy(x).cuda() for x in imgs]
+    outs = {}
+    for depth in ("9", "5"):
+        monkeypatch.setenv("AC_GB300_FUSION_DEPTH", depth)
+        p = ac.Processor("cuda", 0, "acnet-legacy-hdn2", precision=form)
+        single = _out_like(srcs[0])
+        p.process_device(srcs[0], single, 2.0)
+        assert p.ok(), p.error()
+        assert p.last_plan()["fusion_depth"] == int(depth)
+        dsts = [_out_like(s) for s in srcs]
+        p.process_batch_device(srcs, dsts, 2.0)
+        assert p.ok(), p.error()
+        assert p.last_plan()["fusion_depth"] == int(depth)
+        outs[depth] = [single.cpu().numpy()] + [d.cpu().numpy() for d in dsts]
+    for a, b in zip(outs["9"], outs["5"]):
+        assert np.array_equal(a, b)
+    assert np.array_equal(outs["5"][0], outs["5"][1])
+
+
 @pytest.mark.parametrize("kernel", ["3", "4"])
 @pytest.mark.parametrize("batch", [False, True])
 def test_autotuned_equals_untuned(kernel, batch, monkeypatch):
@@ -128,6 +167,9 @@ def test_autotuned_equals_untuned(kernel, batch, monkeypatch):
     assert plans[0]["kernel"] == plans[1]["kernel"] == ("quad" if kernel == "4" else "pair")
     assert plans[0]["tile"][0] > 0 and plans[0]["ctas_per_sm"] in (1, 2)
     assert plans[1]["ctas_per_sm"] == 2  # untuned: the default plan
+    # the quad kernel's candidates include the network split in two launches
+    assert plans[0]["fusion_depth"] in ((9, 5) if kernel == "4" else (9,))
+    assert plans[1]["fusion_depth"] == 9
 
 
 @pytest.mark.parametrize("form,factor", [("fp32", 2.0), ("fp16", 4.0)])

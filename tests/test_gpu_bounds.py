@@ -86,6 +86,34 @@ def test_dst_guard_bands_x2(form, c, dtype, shape):
     assert np.array_equal(got.reshape(want.shape), want)
 
 
+@pytest.mark.parametrize("c", [1, 3, 4])
+@pytest.mark.parametrize("dtype", ["uint8", "uint16", "float32"])
+def test_dst_guard_bands_split_network(c, dtype, monkeypatch):
+    """The network split in two launches (AC_GB300_FUSION_DEPTH=5), one
+    image and a batch, against the whole-network launch's bytes."""
+    monkeypatch.setenv("AC_GB300_TC_KERNEL", "4")
+    sizes = [(1, 1), (3, 5), (17, 33), (47, 93), (55, 109)]
+    imgs = [source(h, w, c, dtype, seed=h + 2 * w) for h, w in sizes]
+    monkeypatch.setenv("AC_GB300_FUSION_DEPTH", "9")
+    p9 = ac.Processor("cuda", 0, "acnet-legacy-hdn1", precision="fp16")
+    want = [p9.process(x, 2.0) for x in imgs]
+    assert p9.ok(), p9.error()
+    monkeypatch.setenv("AC_GB300_FUSION_DEPTH", "5")
+    p = ac.Processor("cuda", 0, "acnet-legacy-hdn1", precision="fp16")
+    srcs = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in imgs]
+    for s, (h, w), wv in zip(srcs, sizes, want):
+        g = Guarded(2 * h, 2 * w, c, dtype)
+        p.process_device(s, g.image(), 2.0)
+        assert p.ok(), p.error()
+        assert np.array_equal(g.check().reshape(wv.shape), wv)
+    gs = [Guarded(2 * h, 2 * w, c, dtype) for h, w in sizes]
+    p.process_batch_device(srcs, [g.image() for g in gs], 2.0)
+    assert p.ok(), p.error()
+    assert p.last_plan()["fusion_depth"] == 5
+    for g, wv in zip(gs, want):
+        assert np.array_equal(g.check().reshape(wv.shape), wv)
+
+
 @pytest.mark.parametrize("form", ["fp32", "fp16"])
 @pytest.mark.parametrize("model,factor", [("acnet-legacy-hdn0", 4.0), ("acnet-legacy-hdn0", 3.0), ("arnet-b8", 2.0),
                                           ("acnet-f8b8-hdn", 2.0), ("artcnn-c4f16", 2.0), ("fsrcnnx-f8", 2.0)])
