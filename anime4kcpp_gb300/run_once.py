@@ -8,8 +8,12 @@ persistent launch per call in the tensor-core forms); with --yuv, one planar
     python -m anime4kcpp_gb300.run_once --form fp16 --size 1920x1080 --channels 3 --repeat 2
     python -m anime4kcpp_gb300.run_once --form fp16 --size 1920x1080 --channels 3 --batch 8 --repeat 2
     python -m anime4kcpp_gb300.run_once --form fp16 --model arnet-b8 --size 1920x1080 --yuv --factor 4 --repeat 2
+
+--fusion-depth 9 or 5 forces the quad kernel's plan (the whole network in
+one launch, or split in two launches) instead of the autotuner's choice.
 """
 import argparse
+import os
 
 import numpy as np
 
@@ -24,7 +28,11 @@ def main():
     ap.add_argument("--repeat", type=int, default=2)
     ap.add_argument("--batch", type=int, default=0, help="frames per call through the batch entry point (0: single)")
     ap.add_argument("--yuv", action="store_true", help="one planar 10-bit YUV 4:2:0 u16 frame (shift 6)")
+    ap.add_argument("--fusion-depth", type=int, default=0, choices=[0, 5, 9],
+                    help="quad kernel: 9 = one launch, 5 = split in two launches (0: autotuned)")
     a = ap.parse_args()
+    if a.fusion_depth:
+        os.environ["AC_GB300_FUSION_DEPTH"] = str(a.fusion_depth)
     import torch
 
     import anime4kcpp_gb300 as ac
