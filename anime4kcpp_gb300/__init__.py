@@ -60,7 +60,8 @@ class ACGB300ServeJob(ctypes.Structure):
 
 class ACGB300ServeResult(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("queue_ms", ctypes.c_double), ("device_ms", ctypes.c_double),
-                ("latency_ms", ctypes.c_double), ("batch", ctypes.c_int), ("error", ctypes.c_char * 160)]
+                ("latency_ms", ctypes.c_double), ("h2d_ms", ctypes.c_double), ("compute_ms", ctypes.c_double),
+                ("d2h_ms", ctypes.c_double), ("batch", ctypes.c_int), ("error", ctypes.c_char * 160)]
 
 
 class ACGB300ServeStats(ctypes.Structure):
@@ -403,7 +404,8 @@ class Server:
             raise RuntimeError("wait failed")
         self._keep.pop(ticket, None)
         return {"status": r.status, "queue_ms": r.queue_ms, "device_ms": r.device_ms, "latency_ms": r.latency_ms,
-                "batch": r.batch, "error": r.error.decode()}
+                "h2d_ms": r.h2d_ms, "compute_ms": r.compute_ms, "d2h_ms": r.d2h_ms, "batch": r.batch,
+                "error": r.error.decode()}
 
     def stats(self):
         st = ACGB300ServeStats()

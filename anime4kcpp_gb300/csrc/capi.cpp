@@ -513,6 +513,9 @@ int ac_gb300_server_wait(ACGB300Server* server, uint64_t ticket, double timeout_
     result->queue_ms = r.queueMs;
     result->device_ms = r.deviceMs;
     result->latency_ms = r.latencyMs;
+    result->h2d_ms = r.h2dMs;
+    result->compute_ms = r.computeMs;
+    result->d2h_ms = r.d2hMs;
     result->batch = r.batch;
     std::snprintf(result->error, sizeof(result->error), "%s", r.error.c_str());
     return AC_SUCCESS;

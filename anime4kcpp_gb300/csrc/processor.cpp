@@ -1354,7 +1354,7 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
             {
                 // the same batch again: replay its graph (memset + persistent kernel)
                 if ((err = cudaGraphLaunch(git->second.exec, s)) != cudaSuccess) return fail(ts, "graph launch", err), false;
-                count_launch();
+                count_launch(git->second.kernels);
                 g_graph_replays++;
             }
             else if (cap == cudaStreamCaptureStatusNone && ts.seen.count(sig) && ts.graphs.size() < 64)
@@ -1364,6 +1364,7 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
                 if ((err = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
                     return fail(ts, "stream capture", err), false;
                 const cudaError_t lerr = launchGroup();
+                ge.kernels = quad && !acn8 && plan.depth == 5 ? 2 : 1;  // the split network: two kernels
                 err = cudaStreamEndCapture(s, &ge.graph);
                 if (lerr != cudaSuccess || err != cudaSuccess)
                 {

@@ -117,6 +117,7 @@ private:
     {
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
+        int kernels = 1;  // kernel launches a replay runs
     };
 public:
     // The persistent launch plan of the calling thread's most recent

@@ -87,6 +87,17 @@ Server::Server(int device, Precision precision, size_t budget, int workers, int 
             break;
         }
         streams_.push_back(s);
+        for (int k = 0; k < 4; k++)
+        {
+            cudaEvent_t e = nullptr;
+            if ((err = cudaEventCreate(&e)) != cudaSuccess)
+            {
+                initError_ = std::string("cudaEventCreate: ") + cudaGetErrorString(err);
+                break;
+            }
+            events_.push_back(e);
+        }
+        if (!initError_.empty()) break;
     }
     if (!initError_.empty()) return;
     counters_.budgetBytes = static_cast<double>(budget_);
@@ -113,6 +124,7 @@ Server::~Server()
     free_.clear();
     procs_.clear();
     for (cudaStream_t s : streams_) cudaStreamDestroy(s);
+    for (cudaEvent_t e : events_) cudaEventDestroy(e);
 }
 
 GB300Processor* Server::processorFor(const std::string& model, bool express, std::string& err)
@@ -464,6 +476,8 @@ void Server::workerLoop(int w)
         std::string err;
         cudaError_t e = cudaSuccess;
         GB300Processor* proc = processorFor(batch[0]->job.model, batch[0]->express, err);
+        cudaEvent_t* ev = events_.data() + 4 * w;
+        bool timed = cudaEventRecord(ev[0], st) == cudaSuccess;
         for (auto& j : batch)
             for (int p = 0; p < j->job.planes && e == cudaSuccess; p++)
             {
@@ -472,6 +486,7 @@ void Server::workerLoop(int w)
                               static_cast<size_t>(h.w) * h.c * (h.type & 0xff), h.h, cudaMemcpyHostToDevice, st);
             }
         int rc = proc ? 0 : -1;
+        timed = timed && cudaEventRecord(ev[1], st) == cudaSuccess;
         if (proc && e == cudaSuccess)
         {
             const ServeJob& s0 = batch[0]->job;
@@ -491,6 +506,7 @@ void Server::workerLoop(int w)
                 rc = proc->processYuvDevice(1, s0.planes, batch[0]->dsrc, batch[0]->ddst, s0.factor, s0.shift, st, false);
             if (rc != 0) err = proc->error();
         }
+        timed = timed && cudaEventRecord(ev[2], st) == cudaSuccess;
         if (rc == 0)
             for (auto& j : batch)
                 for (int p = 0; p < j->job.planes && e == cudaSuccess; p++)
@@ -499,6 +515,7 @@ void Server::workerLoop(int w)
                     e = copy_rows(h.ptr, h.stride, j->ddst[p].ptr, j->ddst[p].stride,
                                   static_cast<size_t>(h.w) * h.c * (h.type & 0xff), h.h, cudaMemcpyDeviceToHost, st);
                 }
+        timed = timed && cudaEventRecord(ev[3], st) == cudaSuccess;
         const bool tc = precision_ != Precision::FP32;
         if (tc && e == cudaSuccess) e = tc_status_enqueue(st);
         const cudaError_t se = cudaStreamSynchronize(st);
@@ -510,8 +527,15 @@ void Server::workerLoop(int w)
             err = "tensor-core wait timed out";
         }
         const double t1 = now_s();
+        float part[3] = {0.0f, 0.0f, 0.0f};
+        if (timed && e == cudaSuccess && rc == 0)
+            for (int k = 0; k < 3; k++)
+                if (cudaEventElapsedTime(&part[k], ev[k], ev[k + 1]) != cudaSuccess) part[k] = 0.0f;
         for (auto& j : batch)
         {
+            j->result.h2dMs = part[0];
+            j->result.computeMs = part[1];
+            j->result.d2hMs = part[2];
             release(*j);
             complete(std::move(j), (e == cudaSuccess && rc == 0) ? 0 : -1, err, t1);
         }

@@ -47,6 +47,9 @@ struct ServeResult
     double queueMs = 0.0;    // submit -> admitted
     double deviceMs = 0.0;   // first copy issued -> result in the dst planes
     double latencyMs = 0.0;  // submit -> result in the dst planes
+    // GPU time on the worker's stream (CUDA events): the input copies, the
+    // processing, the output copies; 0 when the job failed before them
+    double h2dMs = 0.0, computeMs = 0.0, d2hMs = 0.0;
     int batch = 0;           // jobs that shared this job's launch
 };
 
@@ -129,6 +132,7 @@ private:
     size_t poolBytes_ = 0;               // cached + handed out
 
     std::vector<cudaStream_t> streams_;  // one per worker
+    std::vector<cudaEvent_t> events_;    // four per worker: the job's copy / processing boundaries
     int express_ = 0;                    // workers 0 .. express_-1 serve small jobs on high-priority streams
     std::thread admitter_;
     std::vector<std::thread> workers_;

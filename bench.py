@@ -740,6 +740,12 @@ def time_serve(ac, torch, args, forms=("fp16", "fp32")):
             "p99_ms_1080p_parts": {"admission": pct([r["queue_ms"] for r in r1080], 99),
                                    "worker_wait": pct([r["latency_ms"] - r["queue_ms"] - r["device_ms"] for r in r1080], 99),
                                    "device": pct([r["device_ms"] for r in r1080], 99)},
+            # the device part on the worker's stream (CUDA events): input copies, processing, output
+            # copies, and what the events do not cover (host work of the worker between them)
+            "p99_ms_1080p_device_parts": {
+                "h2d": pct([r["h2d_ms"] for r in r1080], 99), "compute": pct([r["compute_ms"] for r in r1080], 99),
+                "d2h": pct([r["d2h_ms"] for r in r1080], 99),
+                "outside_events": pct([r["device_ms"] - r["h2d_ms"] - r["compute_ms"] - r["d2h_ms"] for r in r1080], 99)},
             # 1080p classes (factor, family, format): jobs and p99 device ms
             "p99_device_ms_1080p_by_class": {
                 "x%d/%s/%s" % (f, fam, fmt): {"jobs": len(v), "p99": pct(v, 99)}
@@ -930,6 +936,10 @@ def run_gb300(args, rank, world, local_rank):
                "kernel_ms_per_launch": prof[0] / max(prof[1], 1), "kernel_launches": prof[1],
                "kernel_out_px": prof[2], "steps": steps, "launch": "one per step (8 frames)" if batched else "one per frame"}
         if batched:
+            # the autotuner's plan for the 8-frame class: one kernel (fusion
+            # depth 9) or the network split in two kernels (depth 5)
+            rec["plan"] = proc.last_plan()
+            rec["kernels_per_launch"] = 2 if rec["plan"].get("fusion_depth") == 5 else 1
             # the same frames, each in its own launch
             pms, plaunches, pprof = time_device(ac, torch, proc, srcs, dsts, frames, max(3, steps // 2), args.warmup,
                                                 profile=True)
@@ -971,8 +981,9 @@ def run_gb300(args, rank, world, local_rank):
     fp32_peak = 2.0 * 128 * props.multi_processor_count * sm_max * 1e6 / 1e12
     traffic = None
     tr_path = os.path.join(ROOT, "profiles", "traffic.json")
+    split = rec.get("kernels_per_launch", 1) == 2
     if os.path.exists(tr_path):
-        rec_t = json.load(open(tr_path)).get(form)
+        rec_t = json.load(open(tr_path)).get(form + ("_split" if split else ""))
         traffic = rec_t.get("bytes") if isinstance(rec_t, dict) else rec_t
     if form == "fp32":
         roofline = {"bound": "fp32-core", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
@@ -984,7 +995,9 @@ def run_gb300(args, rank, world, local_rank):
         peak = float(peaks.get("bf16_tflops", 1900.0))
         roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                     "traffic": traffic, "peak_source": "of measured (MEASURED_PEAKS.json bf16_tflops, burst)"
-                    if "bf16_tflops" in peaks else "of fallback (1.9 PFLOP/s burst)"}
+                    if "bf16_tflops" in peaks else "of fallback (1.9 PFLOP/s burst)",
+                    "kernel": "the step's launch: head + tail kernels of the split network (fusion depth 5 + 4)"
+                    if split else "the step's launch: the quad kernel, whole network (fusion depth 9)"}
 
     out = {
         "metric": METRIC, "value": rec["value"], "unit": "Mpx/s", "n_gpus": world, "steps": rec["steps"],

@@ -203,6 +203,9 @@ typedef struct ACGB300ServeResult
     double queue_ms;   /* submit -> admitted */
     double device_ms;  /* first copy issued -> result in dst */
     double latency_ms; /* submit -> result in dst */
+    double h2d_ms;     /* GPU time of the input copies (CUDA events on the worker's stream) */
+    double compute_ms; /* GPU time from the input copies' end to the processing's end */
+    double d2h_ms;     /* GPU time of the output copies */
     int batch;         /* jobs that shared this job's launch */
     char error[160];
 } ACGB300ServeResult;

@@ -73,6 +73,10 @@ def test_results_are_the_same_alone_and_in_the_mix(form):
     for r in results:
         assert r["status"] == 0, r["error"]
         assert r["latency_ms"] >= r["device_ms"] >= 0.0
+        # the GPU-timed parts (CUDA events on the worker's stream) lie inside the device span
+        parts = (r["h2d_ms"], r["compute_ms"], r["d2h_ms"])
+        assert min(parts) >= 0.0 and r["compute_ms"] > 0.0
+        assert sum(parts) <= r["device_ms"] + 0.05
     st = srv.stats()
     assert st["completed"] == len(jobs) and st["failed"] == 0
     if form == "fp16":
