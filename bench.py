@@ -618,7 +618,7 @@ SERVE_MODELS = ["acnet-legacy-hdn0", "acnet-legacy-hdn1", "acnet-legacy-hdn2", "
 def time_serve(ac, torch, args, forms=("fp16", "fp32")):
     """The serving workload: an open-loop Poisson stream of upscale jobs at
     `args.serve_rate` jobs/s for `args.serve_seconds` s through the serving
-    loop (ac.Server, 80 GB HBM budget, 6 worker streams).  Sizes 854x480,
+    loop (ac.Server, 80 GB HBM budget, `args.serve_workers` worker streams).  Sizes 854x480,
     1280x720, 1920x1080, 3840x2160 in ratio 1:2:2:1; factor 2 or 4 in ratio
     3:1; models ACNetLegacy HDN0-3 and ARNet B8 chosen uniformly; formats RGB
     u8 or 10-bit YUV 4:2:0 u16 (planar, shift 6) in ratio 4:1.  Latency =
