@@ -451,7 +451,7 @@ GB300Processor::~GB300Processor()
         ts.counter.release();
         ts.batchTmp.release();
         ts.yuvTmp.release();
-        ts.splitMap.release();
+        for (auto& m : ts.splitMaps) m.second.release();
         for (auto& t : ts.tables) t.second.dev.release();
         for (auto& e : ts.events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
         for (auto& e : ts.pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -459,6 +459,7 @@ GB300Processor::~GB300Processor()
         {
             if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
             if (g.second.graph) cudaGraphDestroy(g.second.graph);
+            if (g.second.counters) cudaFree(g.second.counters);
         }
         if (ts.stream) cudaStreamDestroy(ts.stream);
     }
@@ -747,7 +748,8 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
                     int* counter = static_cast<int*>(ts.counter.ptr) + (ts.counterSlot & 62);
                     ts.counterSlot += 2;
                     bool ran = false;
-                    const Tc3Plan plan = tc3Plan(1, &in, &out, ph, w, bf16, counter, stream, ran, err, true, &ts.splitMap);
+                    const Tc3Plan plan =
+                        tc3Plan(1, &in, &out, ph, w, bf16, counter, stream, ran, err, true, splitMapFor(ts, stream));
                     ts.lastPlan = LastPlan{4, plan.shape, plan.perSm, plan.depth};
                     if (err == cudaSuccess && !ran) err = launchQuad(ts, plan, 1, &in, &out, ph, w, bf16, counter, stream);
                 }
@@ -891,18 +893,28 @@ size_t GB300Processor::splitMapBytes(int n, const Plane* in)
     return b;
 }
 
+DeviceBuffer* GB300Processor::splitMapFor(ThreadState& ts, cudaStream_t stream)
+{
+    auto it = ts.splitMaps.find(stream);
+    if (it != ts.splitMaps.end()) return &it->second;
+    if (ts.splitMaps.size() >= 16) return nullptr;
+    return &ts.splitMaps[stream];
+}
+
 cudaError_t GB300Processor::launchQuad(ThreadState& ts, const Tc3Plan& plan, int n, const Plane* in, const Plane* out,
                                        const Phase2* ph, const void* w, bool bf16, int* counter, cudaStream_t stream)
 {
     const int ctas = tc3Ctas_ > 0 ? tc3Ctas_ : smCount_;
-    if (plan.depth == 5)
+    DeviceBuffer* maps = plan.depth == 5 ? splitMapFor(ts, stream) : nullptr;
+    if (maps)
     {
-        cudaError_t err = ts.splitMap.ensure(splitMapBytes(n, in));
+        cudaError_t err = maps->ensure(splitMapBytes(n, in));
         if (err != cudaSuccess) return err;
-        return launch_acnet_legacy_tc4_split(*acnet_, w, bf16, n, in, out, ph, ts.splitMap.ptr, counter, ctas, stream,
-                                             plan.perSm);
+        return launch_acnet_legacy_tc4_split(*acnet_, w, bf16, n, in, out, ph, maps->ptr, counter, ctas, stream, plan.perSm);
     }
-    return launch_acnet_legacy_tc4(*acnet_, w, bf16, n, in, out, ph, counter, ctas, stream, plan.perSm, plan.shape);
+    // the whole network (also when this thread has no map buffer left for the stream)
+    return launch_acnet_legacy_tc4(*acnet_, w, bf16, n, in, out, ph, counter, ctas, stream, plan.perSm,
+                                   plan.depth == 5 ? 0 : plan.shape);
 }
 
 GB300Processor::Tc3Plan GB300Processor::tc3Plan(int n, const Plane* in, const Plane* out, const Phase2* ph, const void* w,
@@ -934,9 +946,8 @@ GB300Processor::Tc3Plan GB300Processor::tc3Plan(int n, const Plane* in, const Pl
         if (it != plans_.end()) return it->second;
     }
     // Measure every shape x {2, 1} CTAs per SM (quad kernel: and the split
-    // network x {2, 1}): one warm launch, then two timed ones with events on
-    // the launching stream.  Each candidate writes the same bytes, so the
-    // output is valid afterwards.
+    // network x {2, 1}) with events on the launching stream.  Each candidate
+    // writes the same bytes, so the output is valid afterwards.
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if ((err = cudaEventCreate(&e0)) != cudaSuccess) return plan;
     if ((err = cudaEventCreate(&e1)) != cudaSuccess)
@@ -962,13 +973,20 @@ GB300Processor::Tc3Plan GB300Processor::tc3Plan(int n, const Plane* in, const Pl
     for (int shape = 0; shape < shapes && err == cudaSuccess; shape++)
         for (int perSm = 2; perSm >= 1 && err == cudaSuccess; perSm--)
         {
+            // a warm launch, then the faster of two timings of two launches
+            // (candidates a few percent apart are told apart more reliably)
             err = launch(shape, perSm);
-            if (err == cudaSuccess) err = cudaEventRecord(e0, stream);
-            for (int r = 0; r < 2 && err == cudaSuccess; r++) err = launch(shape, perSm);
-            if (err == cudaSuccess) err = cudaEventRecord(e1, stream);
-            if (err == cudaSuccess) err = cudaEventSynchronize(e1);
-            float ms = 0.0f;
-            if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+            float ms = 1e30f;
+            for (int rep = 0; rep < 2 && err == cudaSuccess; rep++)
+            {
+                err = cudaEventRecord(e0, stream);
+                for (int r = 0; r < 2 && err == cudaSuccess; r++) err = launch(shape, perSm);
+                if (err == cudaSuccess) err = cudaEventRecord(e1, stream);
+                if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+                float t = 0.0f;
+                if (err == cudaSuccess) err = cudaEventElapsedTime(&t, e0, e1);
+                if (err == cudaSuccess && t < ms) ms = t;
+            }
             if (err == cudaSuccess && ms < best)
             {
                 best = ms;
@@ -1316,15 +1334,21 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
             bool ran = false;
             Tc3Plan plan;
             if (acn8) plan.perSm = tc3PerSm_ > 0 ? tc3PerSm_ : 2;  // one tile shape per ACNet<8> depth
-            else plan = tc3Plan(m, in, out, php, w, bf16, counter, s, ran, err, quad, &ts.splitMap);
+            else plan = tc3Plan(m, in, out, php, w, bf16, counter, s, ran, err, quad, splitMapFor(ts, s));
             if (err != cudaSuccess) return fail(ts, "batched upscale", err), false;
             // the split network's maps exist before a capture begins
-            if (quad && plan.depth == 5 && (err = ts.splitMap.ensure(splitMapBytes(m, in))) != cudaSuccess)
+            DeviceBuffer* maps = quad && plan.depth == 5 ? splitMapFor(ts, s) : nullptr;
+            if (maps && (err = maps->ensure(splitMapBytes(m, in))) != cudaSuccess)
                 return fail(ts, "device allocation", err), false;
+            if (quad && plan.depth == 5 && !maps)
+            {
+                plan.depth = 9;  // no map buffer for this stream: the whole network
+                plan.shape = 0;
+            }
             ts.lastPlan = LastPlan{acn8 ? 5 : (quad ? 4 : 3), plan.shape, plan.perSm, plan.depth};
             mix(static_cast<uint64_t>(plan.shape * 4 + plan.perSm));
             mix(static_cast<uint64_t>(plan.depth));
-            mix(reinterpret_cast<uint64_t>(plan.depth == 5 ? ts.splitMap.ptr : nullptr));
+            mix(reinterpret_cast<uint64_t>(maps && plan.depth == 5 ? maps->ptr : nullptr));
             mix(static_cast<uint64_t>(quad));
             const int ctas = tc3Ctas_ > 0 ? tc3Ctas_ : smCount_;
             auto launchGroup = [&]() {
@@ -1361,19 +1385,29 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
             {
                 // second sighting: capture the launch into a graph, then replay it
                 GraphEntry ge;
+                if ((err = cudaMalloc(&ge.counters, 2 * sizeof(int))) != cudaSuccess)
+                    return fail(ts, "device allocation", err), false;
                 if ((err = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+                {
+                    cudaFree(ge.counters);
                     return fail(ts, "stream capture", err), false;
+                }
+                int* const ringCounter = counter;
+                counter = ge.counters;  // launchGroup reads `counter`
                 const cudaError_t lerr = launchGroup();
+                counter = ringCounter;
                 ge.kernels = quad && !acn8 && plan.depth == 5 ? 2 : 1;  // the split network: two kernels
                 err = cudaStreamEndCapture(s, &ge.graph);
                 if (lerr != cudaSuccess || err != cudaSuccess)
                 {
                     if (ge.graph) cudaGraphDestroy(ge.graph);
+                    cudaFree(ge.counters);
                     return fail(ts, "stream capture", lerr != cudaSuccess ? lerr : err), false;
                 }
                 if ((err = cudaGraphInstantiate(&ge.exec, ge.graph, 0)) != cudaSuccess)
                 {
                     cudaGraphDestroy(ge.graph);
+                    cudaFree(ge.counters);
                     return fail(ts, "graph instantiation", err), false;
                 }
                 ts.graphs[sig] = ge;

@@ -118,6 +118,10 @@ private:
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
         int kernels = 1;  // kernel launches a replay runs
+        // the graph's own two tile counters: a replay may run beside the
+        // thread's direct launches on other streams, which take counters
+        // from the ring
+        int* counters = nullptr;
     };
 public:
     // The persistent launch plan of the calling thread's most recent
@@ -140,7 +144,10 @@ private:
         unsigned counterSlot = 0;
         DeviceBuffer batchTmp; // x2 intermediates of batched x4 passes
         DeviceBuffer yuvTmp;   // shifted Y planes of the YUV path
-        DeviceBuffer splitMap; // 16-bit activation maps of the split quad network
+        // 16-bit activation maps of the split quad network, one buffer per
+        // stream: calls on different streams may run at once, as the whole
+        // network's launches may
+        std::map<cudaStream_t, DeviceBuffer> splitMaps;
         std::map<std::tuple<int, int, int>, AxisTable> tables;
         bool ok = true;
         std::string err = "NO ERROR";
@@ -198,11 +205,14 @@ private:
     Tc3Plan tc3Plan(int n, const Plane* in, const Plane* out, const Phase2* ph, const void* w, bool bf16, int* counter,
                     cudaStream_t stream, bool& ran, cudaError_t& err, bool quad = false, DeviceBuffer* maps = nullptr);
     // The quad kernel's launch under `plan` (whole network, or split in two
-    // launches over ts.splitMap, which the caller sized with splitMapBytes);
-    // `counter` points at two device ints.
+    // launches over the stream's map buffer); `counter` points at two device
+    // ints.
     cudaError_t launchQuad(ThreadState& ts, const Tc3Plan& plan, int n, const Plane* in, const Plane* out,
                            const Phase2* ph, const void* w, bool bf16, int* counter, cudaStream_t stream);
     static size_t splitMapBytes(int n, const Plane* in);
+    // The split network's map buffer of `stream` (null when the thread
+    // already holds buffers for 16 other streams: the split is then not used).
+    static DeviceBuffer* splitMapFor(ThreadState& ts, cudaStream_t stream);
 
     int device_ = -1;
     int smCount_ = 0;

@@ -140,6 +140,42 @@ def test_split_network_gives_identical_bytes(c, dtype, form, monkeypatch):
     assert np.array_equal(outs["5"][0], outs["5"][1])
 
 
+@pytest.mark.parametrize("depth", ["9", "5"])
+def test_async_calls_on_several_streams_from_one_thread(depth, monkeypatch):
+    """x2 calls queued with sync=0 on four streams from one host thread run
+    at the same time; each stream has its own tile counters and (split
+    network) its own activation maps, so every result equals the result of
+    a synchronous call."""
+    monkeypatch.setenv("AC_GB300_TC_KERNEL", "4")
+    monkeypatch.setenv("AC_GB300_FUSION_DEPTH", depth)
+    imgs = [synthetic.rgb_u8(360 + 40 * k, 640 - 32 * k, seed=50 + k) for k in range(4)]
+    srcs = [torch.from_numpy(x).cuda() for x in imgs]
+    p = ac.Processor("cuda", 0, "acnet-legacy-hdn3", precision="fp16")
+    want = []
+    for s in srcs:
+        d = _out_like(s)
+        p.process_device(s, d, 2.0)
+        want.append(d.cpu().numpy())
+    streams = [torch.cuda.Stream() for _ in srcs]
+    for rep in range(3):
+        dsts = [_out_like(s) for s in srcs]
+        torch.cuda.synchronize()
+        for k in range(4):  # each stream: one frame, then a batch of the other three
+            p.process_device(srcs[k], dsts[k], 2.0, stream=streams[k].cuda_stream, sync=False)
+        bd = [[_out_like(srcs[j]) for j in range(4) if j != k] for k in range(4)]
+        for k in range(4):
+            p.process_batch_device([srcs[j] for j in range(4) if j != k], bd[k], 2.0, stream=streams[k].cuda_stream,
+                                   sync=False)
+        torch.cuda.synchronize()
+        assert p.ok(), p.error()
+        for k in range(4):
+            assert np.array_equal(dsts[k].cpu().numpy(), want[k])
+            others = [j for j in range(4) if j != k]
+            for d, j in zip(bd[k], others):
+                assert np.array_equal(d.cpu().numpy(), want[j])
+    assert p.last_plan()["fusion_depth"] == int(depth)
+
+
 @pytest.mark.parametrize("kernel", ["3", "4"])
 @pytest.mark.parametrize("batch", [False, True])
 def test_autotuned_equals_untuned(kernel, batch, monkeypatch):
