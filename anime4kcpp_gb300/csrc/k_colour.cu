@@ -244,12 +244,41 @@ __global__ void resize_kernel(Plane src, Plane dst, ResizeAxis ax, ResizeAxis ay
 // result is stored back in the element type (a left shift drops high bits).
 // In place when src and dst are the same plane.
 template <typename T>
+__device__ __forceinline__ T shift_one(unsigned v, int n)
+{
+    return static_cast<T>(n >= 0 ? (v << n) : (v >> (-n)));
+}
+template <typename T>
 __global__ void shift_kernel(Plane src, Plane dst, int n)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
     if (x >= src.w * src.channels) return;
     const unsigned v = row_ptr<T>(src.ptr, src.pitch, y)[x];
-    row_ptr_w<T>(dst.ptr, dst.pitch, y)[x] = static_cast<T>(n >= 0 ? (v << n) : (v >> (-n)));
+    row_ptr_w<T>(dst.ptr, dst.pitch, y)[x] = shift_one<T>(v, n);
+}
+// The same with 16 bytes per thread, for planes whose base addresses and
+// pitches are 16-byte aligned: thread x of a row takes elements
+// [x * E, x * E + E) (E = 16 / sizeof(T)); the row's last partial chunk
+// goes element by element.
+template <typename T>
+__global__ void shift16_kernel(Plane src, Plane dst, int n)
+{
+    constexpr int E = 16 / static_cast<int>(sizeof(T));
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    const int elems = src.w * src.channels, x0 = x * E;
+    if (x0 >= elems) return;
+    const T* in = row_ptr<T>(src.ptr, src.pitch, y) + x0;
+    T* out = row_ptr_w<T>(dst.ptr, dst.pitch, y) + x0;
+    if (x0 + E <= elems)
+    {
+        uint4 v = *reinterpret_cast<const uint4*>(in);
+        T* e = reinterpret_cast<T*>(&v);
+#pragma unroll
+        for (int k = 0; k < E; k++) e[k] = shift_one<T>(e[k], n);
+        *reinterpret_cast<uint4*>(out) = v;
+    }
+    else
+        for (int k = 0; x0 + k < elems; k++) out[k] = shift_one<T>(in[k], n);
 }
 
 namespace {
@@ -341,6 +370,18 @@ cudaError_t launch_shift(const Plane& src, const Plane& dst, int n, cudaStream_t
 {
     if (src.w <= 0 || src.h <= 0 || n == 0) return cudaSuccess;
     if (n <= -16 || n >= 16) return cudaErrorInvalidValue;
+    const bool vec = ((reinterpret_cast<uintptr_t>(src.ptr) | reinterpret_cast<uintptr_t>(dst.ptr) |
+                       static_cast<uintptr_t>(src.pitch) | static_cast<uintptr_t>(dst.pitch)) & 15) == 0;
+    if (vec && (src.type == kU8 || src.type == kU16))
+    {
+        const int es = src.type & 0xff;
+        const int chunks = (src.w * src.channels * es + 15) / 16;
+        const dim3 g = row_grid(chunks, src.h, 256);
+        if (src.type == kU8) shift16_kernel<uint8_t><<<g, 256, 0, stream>>>(src, dst, n);
+        else shift16_kernel<uint16_t><<<g, 256, 0, stream>>>(src, dst, n);
+        count_launch();
+        return cudaGetLastError();
+    }
     dim3 grid = row_grid(src.w * src.channels, src.h, 256);
     switch (src.type)
     {

@@ -139,3 +139,40 @@ def test_video_config_full_size():
             d = np.abs(gy[4 * wy:4 * (wy + n), 4 * wx:4 * (wx + n)].astype(int) -
                        want[oy:oy + 4 * n, ox:ox + 4 * n].astype(int))
             assert d.max() <= 1 and (d == 0).mean() >= 0.95, (d.max(), (d == 0).mean())
+
+
+@pytest.mark.parametrize("bits,shift", [(10, 6), (12, 4)])
+def test_yuv_shift_any_row_layout(bits, shift):
+    """The shl / shr of Y with padded, 16-byte-aligned row strides (the
+    16-byte-per-thread path, rows whose last chunk is partial) and with tight
+    odd strides (element by element): the same bytes, nothing written past
+    a row."""
+    h, w = 37, 51
+    y = synthetic.luma(h, w, np.uint16, seed=bits, noise=4.0, bits=bits)
+    u = synthetic.luma(h // 2, w // 2, np.uint16, seed=bits + 1, noise=4.0, bits=bits)
+    p = ac.Processor("cuda", 0, "acnet-legacy-hdn0", precision="fp16")
+    outs = []
+    for pad in (False, True):
+        stride_in = 256 if pad else 2 * w
+        stride_out = 512 if pad else 2 * 2 * w
+        ybuf = torch.full((h * stride_in // 2,), 0xFFFF, dtype=torch.uint16, device="cuda")
+        ybuf.view(h, stride_in // 2)[:, :w] = torch.from_numpy(y).cuda()
+        obuf = torch.full((2 * h * stride_out // 2,), 0xA5A5, dtype=torch.uint16, device="cuda")
+        src_y = (ybuf.data_ptr(), w, h, 1, stride_in, ac.UINT16)
+        dst_y = (obuf.data_ptr(), 2 * w, 2 * h, 1, stride_out, ac.UINT16)
+        su = _dev(u)
+        du = torch.empty((2 * (h // 2), 2 * (w // 2)), dtype=torch.uint16, device="cuda")
+        p.process_yuv_device([(src_y, su)], [(dst_y, du)], 2.0, shift)
+        assert p.ok(), p.error()
+        o = obuf.view(2 * h, stride_out // 2).cpu().numpy()
+        assert np.all(o[:, 2 * w:] == 0xA5A5)  # padding untouched
+        outs.append(o[:, :2 * w].copy())
+        # the source plane is left as it was
+        assert np.array_equal(ybuf.view(h, stride_in // 2)[:, :w].cpu().numpy(), y)
+    assert np.array_equal(outs[0], outs[1])
+    want = _oracle_frame((y, u), 2.0, "acnet-legacy-hdn0", shift)[0]
+    d = np.abs(outs[0].astype(int) - want.astype(int))
+    # FP16 keeps 11 significant bits: within 1 LSB of a 10-bit output, a few
+    # LSB of a 12-bit one
+    lsb = 1 << (bits - 10)
+    assert (d <= lsb).mean() >= 0.99 and d.max() <= 8 * lsb
