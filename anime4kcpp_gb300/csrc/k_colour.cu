@@ -162,6 +162,68 @@ __host__ __device__ constexpr int phase_off(int k)
     return F == 2 ? (k == 0 ? -2 : -1) : (k < F / 2 ? -2 : -1);
 }
 
+// The integer-factor resample alone (a planar chroma plane of the video
+// recipe): the same phase-table sums as merge_int_kernel, each output
+// encoded to the plane's element type.  One thread per source pixel writes
+// its F x F block of NC-channel outputs.
+template <typename T, int NC, int F>
+__global__ void resize_int_kernel(Plane src, PhaseTable<F> tab, Plane dst)
+{
+    const int sx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int sy = blockIdx.y;
+    if (sx >= src.w) return;
+    constexpr int RLO = -2, NR = 5;  // source rows sy-2 .. sy+2 cover every phase
+    float h[NR][F][NC];
+#pragma unroll
+    for (int rr = 0; rr < NR; rr++)
+    {
+        const T* row = row_ptr<T>(src.ptr, src.pitch, clampi(sy + RLO + rr, 0, src.h - 1));
+        T v[5][NC];
+#pragma unroll
+        for (int dx = 0; dx < 5; dx++)
+        {
+            const int xs = clampi(sx - 2 + dx, 0, src.w - 1);
+#pragma unroll
+            for (int c = 0; c < NC; c++) v[dx][c] = row[xs * NC + c];
+        }
+#pragma unroll
+        for (int k = 0; k < F; k++)
+#pragma unroll
+            for (int c = 0; c < NC; c++)
+            {
+                float s = 0.0f;
+#pragma unroll
+                for (int t = 0; t < 4; t++)
+                {
+                    const float wt = tab.w[k][t];
+                    if (wt == 0.0f) continue;
+                    s = __fadd_rn(s, __fmul_rn(wt, decode_float<T>(v[phase_off<F>(k) + t + 2][c])));
+                }
+                h[rr][k][c] = s;
+            }
+    }
+#pragma unroll
+    for (int j = 0; j < F; j++)
+    {
+        T* orow = row_ptr_w<T>(dst.ptr, dst.pitch, F * sy + j) + F * sx * NC;
+#pragma unroll
+        for (int k = 0; k < F; k++)
+#pragma unroll
+            for (int c = 0; c < NC; c++)
+            {
+                float s = 0.0f;
+#pragma unroll
+                for (int t = 0; t < 4; t++)
+                {
+                    const float wt = tab.w[j][t];
+                    if (wt == 0.0f) continue;
+                    s = __fadd_rn(s, __fmul_rn(wt, h[phase_off<F>(j) + t - RLO][k][c]));
+                }
+                orow[k * NC + c] = encode_resampled<T>(s);
+            }
+    }
+}
+
 template <typename T, int C, int F>
 __global__ void merge_int_kernel(Plane yp, Plane uvp, PhaseTable<F> tab, Plane rgb)
 {
@@ -356,6 +418,37 @@ static cudaError_t launch_merge_int_f(const Plane& y, const Plane& uv, const flo
 }
 
 int merge_int_phase_offset(int factor, int k) { return factor == 2 ? phase_off<2>(k) : phase_off<4>(k); }
+
+template <int F>
+static cudaError_t launch_resize_int_f(const Plane& src, const Plane& dst, const float* wx, cudaStream_t stream)
+{
+    PhaseTable<F> tab;
+    for (int k = 0; k < F; k++)
+        for (int t = 0; t < 4; t++) tab.w[k][t] = wx[k * 4 + t];
+    dim3 grid = row_grid(src.w, src.h, 128);
+    ACGB_TYPE_SWITCH(src.type,
+        switch (src.channels)
+        {
+        case 1: resize_int_kernel<T, 1, F><<<grid, 128, 0, stream>>>(src, tab, dst); break;
+        case 2: resize_int_kernel<T, 2, F><<<grid, 128, 0, stream>>>(src, tab, dst); break;
+        case 3: resize_int_kernel<T, 3, F><<<grid, 128, 0, stream>>>(src, tab, dst); break;
+        case 4: resize_int_kernel<T, 4, F><<<grid, 128, 0, stream>>>(src, tab, dst); break;
+        default: return cudaErrorInvalidValue;
+        })
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_resize_int(const Plane& src, const Plane& dst, int factor, const float* phase_weights,
+                              cudaStream_t stream)
+{
+    if (src.w <= 0 || src.h <= 0) return cudaSuccess;
+    if (dst.w != factor * src.w || dst.h != factor * src.h || dst.channels != src.channels || dst.type != src.type)
+        return cudaErrorInvalidValue;
+    if (factor == 2) return launch_resize_int_f<2>(src, dst, phase_weights, stream);
+    if (factor == 4) return launch_resize_int_f<4>(src, dst, phase_weights, stream);
+    return cudaErrorInvalidValue;
+}
 
 cudaError_t launch_merge_int(const Plane& y, const Plane& uv, int factor, const float* phase_weights, const Plane& rgb,
                              cudaStream_t stream)

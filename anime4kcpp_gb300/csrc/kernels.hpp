@@ -266,6 +266,10 @@ cudaError_t launch_shift(const Plane& src, const Plane& dst, int n, cudaStream_t
 
 // General separable resize of an interleaved plane (any channel count).
 cudaError_t launch_resize(const Plane& src, const Plane& dst, ResizeAxis ax, ResizeAxis ay, cudaStream_t stream);
+// Catmull-Rom resize by exactly 2 or 4 on both axes (phase weights of
+// phase_weights(factor)), the same values as launch_resize with the axis tables.
+cudaError_t launch_resize_int(const Plane& src, const Plane& dst, int factor, const float* phase_weights,
+                              cudaStream_t stream);
 
 // Number of kernel launches issued by this library in the process so far.
 uint64_t launch_count();

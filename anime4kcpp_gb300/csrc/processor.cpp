@@ -1608,6 +1608,15 @@ int GB300Processor::processYuvDevice(int frames, int planes, const DeviceImage* 
         {
             const DeviceImage& a = src[f * planes + p];
             const DeviceImage& b = dst[f * planes + p];
+            // exactly x2 / x4 (4:2:0 chroma of a x2 / x4 frame): the phase-table kernel
+            const int F = (b.w == 2 * a.w && b.h == 2 * a.h) ? 2 : ((b.w == 4 * a.w && b.h == 4 * a.h) ? 4 : 0);
+            float pw[16];
+            if (F && phase_weights(F, pw))
+            {
+                if ((err = launch_resize_int(plane_of(a), plane_of(b), F, pw, s)) != cudaSuccess)
+                    return fail(ts, "chroma resize", err), -1;
+                continue;
+            }
             const ResizeAxis* ax = axis(ts, a.w, b.w, 1, s, err);
             if (!ax) return fail(ts, "resize table", err), -1;
             const ResizeAxis* ay = axis(ts, a.h, b.h, 1, s, err);
