@@ -499,6 +499,7 @@ __global__ void __launch_bounds__(THREADS, 4) conv2_kernel(const __grid_constant
 struct HeadParams
 {
     float k[72];
+    unsigned long long kd[72];  // each weight twice, (k, k), for the paired FMAs (filled by launch_head)
     float b[8];
     float a[8];   // PReLU slopes when `prelu` is set (the ACNet<8> head)
     int prelu;
@@ -507,71 +508,124 @@ struct HeadParams
 };
 
 // Head: conv3x3 1->8 in FP32 from the input plane, identity (ARNet) or PReLU
-// (ACNet<8>), stored as a 16-bit 8-channel map.  One thread per pixel, taps
-// clamped to the plane.
-template <typename T, bool BF16>
-__global__ void __launch_bounds__(256) head_kernel(const __grid_constant__ HeadParams P)
-{
-    const Plane& in = P.in[blockIdx.z];
-    uint4* __restrict__ feat = P.feat[blockIdx.z];
-    const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
-    if (x >= in.w || y >= in.h) return;
-    float t[9];
-#pragma unroll
-    for (int p = 0; p < 9; p++)
-    {
-        const int gy = clampi(y + p / 3 - 1, 0, in.h - 1), gx = clampi(x + p % 3 - 1, 0, in.w - 1);
-        t[p] = to_float<T>(row_ptr<T>(in.ptr, in.pitch, gy)[gx]);
-    }
-    float r[8];
-#pragma unroll
-    for (int n = 0; n < 8; n++)
-    {
-        float v = P.b[n];
-#pragma unroll
-        for (int p = 0; p < 9; p++) v = fmaf(t[p], P.k[n * 9 + p], v);
-        r[n] = P.prelu ? prelu(v, P.a[n]) : v;
-    }
-    feat[static_cast<size_t>(y) * in.w + x] = pack8<BF16>(r);
-}
+// (ACNet<8>), stored as a 16-bit 8-channel map, taps clamped to the plane:
+// head2_kernel below.
 
 struct UpParams
 {
     float k[288];
+    unsigned long long kd[288];  // each weight twice, (k, k): an operand of the paired FMAs (filled by launch_up)
     float b[4];
     int no_nearest;  // FSRCNNX<8>: no nearest-input add
     const uint4* map[kMaxImg];  // image blockIdx.z
     Plane src[kMaxImg], dst[kMaxImg];
 };
 
+// Two FP32 lanes in a 64-bit register pair and the paired fused
+// multiply-add (fma.rn.f32x2): each lane is exactly fmaf.
+__device__ __forceinline__ unsigned long long pk2(float lo, float hi)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void upk2(unsigned long long v, float& lo, float& hi)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c)
+{
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
 // Upscale: conv3x3 8->4 (identity) in FP32 from the 16-bit map, pixel
 // shuffle 2x2, plus the nearest input pixel, fromFloat (Common.hpp:290-342).
+// Two horizontally adjacent pixels per thread, in the lanes of paired FMAs:
+// each output is the fmaf chain over the taps (rows, columns, channels in
+// that order) from the bias; the pair shares its taps' middle columns (four
+// map columns per row instead of six).
 template <typename T, bool BF16>
-__global__ void __launch_bounds__(256) up_kernel(const __grid_constant__ UpParams U)
+__global__ void __launch_bounds__(256) up2_kernel(const __grid_constant__ UpParams U)
 {
     const uint4* __restrict__ map = U.map[blockIdx.z];
     const Plane& src = U.src[blockIdx.z];
     const Plane& dst = U.dst[blockIdx.z];
     const int w = src.w, h = src.h;
-    const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    const int x = 2 * (blockIdx.x * 32 + (threadIdx.x & 31)), y = blockIdx.y * 8 + (threadIdx.x >> 5);
     if (x >= w || y >= h) return;
-    float acc[4];
+    const bool has_b = x + 1 < w;
+    unsigned long long acc[4];
 #pragma unroll
-    for (int n = 0; n < 4; n++) acc[n] = U.b[n];
+    for (int n = 0; n < 4; n++) acc[n] = pk2(U.b[n], U.b[n]);
 #pragma unroll
-    for (int p = 0; p < 9; p++)
+    for (int dy = 0; dy < 3; dy++)
     {
-        const int gy = clampi(y + p / 3 - 1, 0, h - 1), gx = clampi(x + p % 3 - 1, 0, w - 1);
-        float xv[8];
-        unpack8<BF16>(map[static_cast<size_t>(gy) * w + gx], xv);
+        const int gy = clampi(y + dy - 1, 0, h - 1);
+        float xv[4][8];  // map columns x - 1 .. x + 2 (clamped)
 #pragma unroll
-        for (int n = 0; n < 4; n++)
+        for (int j = 0; j < 4; j++) unpack8<BF16>(map[static_cast<size_t>(gy) * w + clampi(x - 1 + j, 0, w - 1)], xv[j]);
 #pragma unroll
-            for (int c = 0; c < 8; c++) acc[n] = fmaf(xv[c], U.k[n * 72 + p * 8 + c], acc[n]);
+        for (int dx = 0; dx < 3; dx++)
+#pragma unroll
+            for (int c = 0; c < 8; c++)
+            {
+                const unsigned long long xp = pk2(xv[dx][c], xv[dx + 1][c]);  // (pixel x, pixel x + 1)
+#pragma unroll
+                for (int n = 0; n < 4; n++) acc[n] = fma2(xp, U.kd[n * 72 + (dy * 3 + dx) * 8 + c], acc[n]);
+            }
     }
-    const float near = U.no_nearest ? 0.0f : to_float<T>(row_ptr<T>(src.ptr, src.pitch, y)[x]);
+    const T* srow = row_ptr<T>(src.ptr, src.pitch, y);
+    const float near_a = U.no_nearest ? 0.0f : to_float<T>(srow[x]);
+    const float near_b = U.no_nearest || !has_b ? 0.0f : to_float<T>(srow[x + 1]);
 #pragma unroll
-    for (int n = 0; n < 4; n++) row_ptr_w<T>(dst.ptr, dst.pitch, 2 * y + (n >> 1))[2 * x + (n & 1)] = from_float<T>(acc[n] + near);
+    for (int n = 0; n < 4; n++)
+    {
+        float a, b;
+        upk2(acc[n], a, b);
+        T* orow = row_ptr_w<T>(dst.ptr, dst.pitch, 2 * y + (n >> 1));
+        orow[2 * x + (n & 1)] = from_float<T>(a + near_a);
+        if (has_b) orow[2 * x + 2 + (n & 1)] = from_float<T>(b + near_b);
+    }
+}
+
+// The head, two horizontally adjacent pixels per thread in the lanes of
+// paired FMAs: each output is the fmaf chain over the nine taps from the
+// bias; the pair shares its taps' middle columns.
+template <typename T, bool BF16>
+__global__ void __launch_bounds__(256) head2_kernel(const __grid_constant__ HeadParams P)
+{
+    const Plane& in = P.in[blockIdx.z];
+    uint4* __restrict__ feat = P.feat[blockIdx.z];
+    const int x = 2 * (blockIdx.x * 32 + (threadIdx.x & 31)), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= in.w || y >= in.h) return;
+    const bool has_b = x + 1 < in.w;
+    unsigned long long t[9];  // tap p of (pixel x, pixel x + 1)
+#pragma unroll
+    for (int dy = 0; dy < 3; dy++)
+    {
+        const T* row = row_ptr<T>(in.ptr, in.pitch, clampi(y + dy - 1, 0, in.h - 1));
+        float c4[4];  // columns x - 1 .. x + 2 (clamped)
+#pragma unroll
+        for (int j = 0; j < 4; j++) c4[j] = to_float<T>(row[clampi(x - 1 + j, 0, in.w - 1)]);
+#pragma unroll
+        for (int dx = 0; dx < 3; dx++) t[dy * 3 + dx] = pk2(c4[dx], c4[dx + 1]);
+    }
+    float ra[8], rb[8];
+#pragma unroll
+    for (int n = 0; n < 8; n++)
+    {
+        unsigned long long v = pk2(P.b[n], P.b[n]);
+#pragma unroll
+        for (int p = 0; p < 9; p++) v = fma2(t[p], P.kd[n * 9 + p], v);
+        float a, b;
+        upk2(v, a, b);
+        ra[n] = P.prelu ? prelu(a, P.a[n]) : a;
+        rb[n] = P.prelu ? prelu(b, P.a[n]) : b;
+    }
+    feat[static_cast<size_t>(y) * in.w + x] = pack8<BF16>(ra);
+    if (has_b) feat[static_cast<size_t>(y) * in.w + x + 1] = pack8<BF16>(rb);
 }
 
 template <int MODE, bool BF16>
@@ -642,20 +696,28 @@ void pack_pair_conv8(const float* k, bool bf16, uint16_t* out)
 namespace arnettc {
 
 // The head over n images (grid z = image); hp.in / hp.feat filled in.
-cudaError_t launch_head(const HeadParams& hp, bool bf16, int n, cudaStream_t stream)
+cudaError_t launch_head(const HeadParams& hp0, bool bf16, int n, cudaStream_t stream)
 {
+    HeadParams hp = hp0;
+    for (int i = 0; i < 72; i++)
+    {
+        unsigned int b;
+        std::memcpy(&b, &hp.k[i], 4);
+        hp.kd[i] = (static_cast<unsigned long long>(b) << 32) | b;
+    }
     int mw = 0, mh = 0;
     for (int i = 0; i < n; i++)
     {
         mw = hp.in[i].w > mw ? hp.in[i].w : mw;
         mh = hp.in[i].h > mh ? hp.in[i].h : mh;
     }
-    const dim3 pgrid((mw + 31) / 32, (mh + 7) / 8, n);
+    // two pixels per thread
+    const dim3 pgrid((mw + 63) / 64, (mh + 7) / 8, n);
     switch (hp.in[0].type)
     {
-    case kU8: bf16 ? head_kernel<uint8_t, true><<<pgrid, 256, 0, stream>>>(hp) : head_kernel<uint8_t, false><<<pgrid, 256, 0, stream>>>(hp); break;
-    case kU16: bf16 ? head_kernel<uint16_t, true><<<pgrid, 256, 0, stream>>>(hp) : head_kernel<uint16_t, false><<<pgrid, 256, 0, stream>>>(hp); break;
-    case kF32: bf16 ? head_kernel<float, true><<<pgrid, 256, 0, stream>>>(hp) : head_kernel<float, false><<<pgrid, 256, 0, stream>>>(hp); break;
+    case kU8: bf16 ? head2_kernel<uint8_t, true><<<pgrid, 256, 0, stream>>>(hp) : head2_kernel<uint8_t, false><<<pgrid, 256, 0, stream>>>(hp); break;
+    case kU16: bf16 ? head2_kernel<uint16_t, true><<<pgrid, 256, 0, stream>>>(hp) : head2_kernel<uint16_t, false><<<pgrid, 256, 0, stream>>>(hp); break;
+    case kF32: bf16 ? head2_kernel<float, true><<<pgrid, 256, 0, stream>>>(hp) : head2_kernel<float, false><<<pgrid, 256, 0, stream>>>(hp); break;
     default: return cudaErrorInvalidValue;
     }
     const cudaError_t err = cudaGetLastError();
@@ -664,20 +726,28 @@ cudaError_t launch_head(const HeadParams& hp, bool bf16, int n, cudaStream_t str
 }
 
 // The upscale layer over n images (grid z = image); u.map / src / dst filled in.
-cudaError_t launch_up(const UpParams& u, bool bf16, int n, cudaStream_t stream)
+cudaError_t launch_up(const UpParams& u0, bool bf16, int n, cudaStream_t stream)
 {
+    UpParams u = u0;
+    for (int i = 0; i < 288; i++)
+    {
+        unsigned int b;
+        std::memcpy(&b, &u.k[i], 4);
+        u.kd[i] = (static_cast<unsigned long long>(b) << 32) | b;
+    }
     int mw = 0, mh = 0;
     for (int i = 0; i < n; i++)
     {
         mw = u.src[i].w > mw ? u.src[i].w : mw;
         mh = u.src[i].h > mh ? u.src[i].h : mh;
     }
-    const dim3 pgrid((mw + 31) / 32, (mh + 7) / 8, n);
+    // two pixels per thread
+    const dim3 pgrid((mw + 63) / 64, (mh + 7) / 8, n);
     switch (u.src[0].type)
     {
-    case kU8: bf16 ? up_kernel<uint8_t, true><<<pgrid, 256, 0, stream>>>(u) : up_kernel<uint8_t, false><<<pgrid, 256, 0, stream>>>(u); break;
-    case kU16: bf16 ? up_kernel<uint16_t, true><<<pgrid, 256, 0, stream>>>(u) : up_kernel<uint16_t, false><<<pgrid, 256, 0, stream>>>(u); break;
-    case kF32: bf16 ? up_kernel<float, true><<<pgrid, 256, 0, stream>>>(u) : up_kernel<float, false><<<pgrid, 256, 0, stream>>>(u); break;
+    case kU8: bf16 ? up2_kernel<uint8_t, true><<<pgrid, 256, 0, stream>>>(u) : up2_kernel<uint8_t, false><<<pgrid, 256, 0, stream>>>(u); break;
+    case kU16: bf16 ? up2_kernel<uint16_t, true><<<pgrid, 256, 0, stream>>>(u) : up2_kernel<uint16_t, false><<<pgrid, 256, 0, stream>>>(u); break;
+    case kF32: bf16 ? up2_kernel<float, true><<<pgrid, 256, 0, stream>>>(u) : up2_kernel<float, false><<<pgrid, 256, 0, stream>>>(u); break;
     default: return cudaErrorInvalidValue;
     }
     const cudaError_t err = cudaGetLastError();
