@@ -366,6 +366,7 @@ int ac_gb300_last_plan(ACProcessor* processor, int* kernel, int* tile_w, int* ti
     if (p.kernel == 4 && p.depth == 5) acgb::acnet_tc4_split_tail_shape(&tw, &th);
     else if (p.kernel == 4) acgb::acnet_tc4_shape(p.shape, &tw, &th);
     else if (p.kernel == 3) acgb::acnet_tc3_shape(p.shape, &tw, &th);
+    else if (p.kernel == 5 && p.depth == 5) acgb::acnet8_tc4_split_tail_shape(&tw, &th);
     else if (p.kernel == 5) acgb::acnet8_tc4_shape(g->spec().blocks, &tw, &th);
     *kernel = p.kernel;
     *tile_w = tw;

@@ -104,6 +104,24 @@ struct NetAcn8
     static constexpr bool ACN8 = true;
     static constexpr int PART = 0;
 };
+// ACNet<8> split at layer K (K <= B, so the head ends on a PReLU layer): the
+// head writes layer K-1's activations after PReLU; the tail runs layers
+// K .. B and the conv 8->4.
+template <int B, int K>
+struct NetAcn8Head
+{
+    static constexpr int NL = K;
+    static constexpr bool ACN8 = true;
+    static constexpr int PART = 1;
+    static_assert(K >= 1 && K <= B, "the head ends on a PReLU layer");
+};
+template <int B, int K>
+struct NetAcn8Tail
+{
+    static constexpr int NL = B + 2 - K;
+    static constexpr bool ACN8 = true;
+    static constexpr int PART = 2;
+};
 
 // COL: the tile ends in the colour merge (its chroma sums must fit the
 // dead activation buffer); a head part's tiles do not.
@@ -643,7 +661,7 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
                 const LayerRange<G> R(l, ix0, ix1, iy0, iy1);
                 uint32_t slopes[4] = {0u, 0u, 0u, 0u};
                 if constexpr (NET::ACN8)
-                    if (l < LAST) pack_slopes<BF16>(P.alpha[l], slopes);
+                    if (l < LAST || NET::PART == 1) pack_slopes<BF16>(P.alpha[l], slopes);
                 float* Hs = reinterpret_cast<float*>(act);  // last layer: the activations are dead once its MMAs completed
                 if constexpr (C > 1 && NET::PART != 1)
                 {
@@ -734,8 +752,13 @@ __global__ void __launch_bounds__(THREADS, 2) acnet_tc4_kernel(const __grid_cons
                                 {
                                     // head part: layer K-1's activations of the tile
                                     // (this range is the tile inside the image) to the map
+                                    uint4 val;
+                                    if constexpr (NET::ACN8)
+                                        val = pack8_prelu<BF16>(v + 8 * kk, slopes);
+                                    else
+                                        val = pack8<BF16>(v + 8 * kk);
                                     *reinterpret_cast<uint4*>(row_ptr_w<unsigned char>(I.map.ptr, I.map.pitch, gy0 + y) +
-                                                              (gx0 + x) * 16) = pack8<BF16>(v + 8 * kk);
+                                                              (gx0 + x) * 16) = val;
                                 }
                                 else
                                 {
@@ -921,6 +944,14 @@ extern template cudaError_t launch_shape<GeoQ1, NetLegacy>(int, int, bool, const
 extern template cudaError_t launch_shape<GeoQ2, NetLegacy>(int, int, bool, const Params&, int, int, cudaStream_t);
 using GeoA8B4 = Geo<52, 48, 6>;  // ACNet<8> B4: 64 x 60 window (chroma sums of a 52 x 52 tile would not fit)
 using GeoA8B8 = Geo<44, 44, 10>; // ACNet<8> B8
+// ACNet<8> B8 split at layer 5: head 52 x 54 tiles in a 64 x 64 window, tail
+// 44 x 60 tiles in a 56 x 70 window, one extra column each side in both (the
+// whole-network B8 windows' column parity)
+constexpr int kSplitKA8 = 5;
+using GeoA8B8Head = Geo<52, 54, 5, false, 1>;
+using GeoA8B8Tail = Geo<44, 60, 5, true, 1>;
+static_assert(GeoA8B8Head::HX % 2 == GeoA8B8::HX % 2 && GeoA8B8Tail::HX % 2 == GeoA8B8::HX % 2,
+              "every ACNet<8> B8 tiling sums the taps of an image column alike");
 
 // One layer of 3x3 8->8 weights k[n * 72 + tap * 8 + c] (reference NHWC
 // order) as the nine N32 x K16 B chunks of the quad GEMM.  Chunk 3 dy + j

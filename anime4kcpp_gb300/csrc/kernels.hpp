@@ -164,10 +164,17 @@ cudaError_t launch_acnet_legacy_tc4_core(const AcnetLegacyWeights& wts, const vo
 // biases / alphas in the reference layout (8 + 8 blocks + 4 / 8 (blocks + 1)).
 bool acnet8_tc4_supported(int blocks);
 void acnet8_tc4_shape(int blocks, int* tw, int* th);
+void acnet8_tc4_split_tail_shape(int* tw, int* th);
 void pack_acnet8_tc4_weights(const float* kernels, int blocks, bool bf16, std::vector<uint16_t>& packed);
 cudaError_t launch_acnet8_tc4(const float* biases, const float* alphas, int blocks, const void* packed4, bool bf16, int n,
                               const Plane* in, const Plane* out, const Phase2* phase2, int* counter, int ctas,
                               cudaStream_t stream, int per_sm_cap = 2);
+// ACNet<8> B8 split in two launches at layer 5 (the head writes block 4's
+// activations to one 16-bit map per image in `maps`, acnet_tc4_split_map_bytes
+// each); the same bytes as launch_acnet8_tc4.  counters: two device ints.
+cudaError_t launch_acnet8_tc4_split(const float* biases, const float* alphas, int blocks, const void* packed4, bool bf16, int n,
+                                    const Plane* in, const Plane* out, const Phase2* phase2, void* maps, int* counters, int ctas,
+                                    cudaStream_t stream, int per_sm_cap);
 // The quad launch with its tile counter and status word in the static
 // scratch of the allocation-free entry (see launch_acnet_legacy_tc3_noalloc).
 cudaError_t launch_acnet_legacy_tc4_noalloc(const AcnetLegacyWeights& wts, const void* packed4, bool bf16, int n,

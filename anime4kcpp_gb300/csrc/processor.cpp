@@ -694,9 +694,11 @@ cudaError_t GB300Processor::luma_pass(ThreadState& ts, const Plane& in, const Pl
             if (!w) err = cudaErrorMemoryAllocation;
             else if ((err = ts.counter.ensure(256)) == cudaSuccess)
             {
-                int* counter = static_cast<int*>(ts.counter.ptr) + (ts.counterSlot++ & 63);
-                err = launch_acnet8_tc4(mp.biases.data(), mp.alphas.data(), spec_.blocks, w, bf16, 1, &in, &out, ph, counter,
-                                        tc3Ctas_ > 0 ? tc3Ctas_ : smCount_, stream, tc3PerSm_ > 0 ? tc3PerSm_ : 2);
+                int* counter = static_cast<int*>(ts.counter.ptr) + (ts.counterSlot & 62);
+                ts.counterSlot += 2;
+                const int perSm = tc3PerSm_ > 0 ? tc3PerSm_ : 2;
+                ts.lastPlan = LastPlan{5, 0, perSm, acn8Depth()};
+                err = launchAcn8(ts, acn8Depth(), 1, &in, &out, ph, w, bf16, counter, stream, perSm);
             }
         }
         else if (precision_ != Precision::FP32 && arnetTc_)
@@ -891,6 +893,28 @@ size_t GB300Processor::splitMapBytes(int n, const Plane* in)
     size_t b = 0;
     for (int i = 0; i < n; i++) b += acnet_tc4_split_map_bytes(in[i].w, in[i].h);
     return b;
+}
+
+// ACNet<8> B8 runs split at layer 5 unless AC_GB300_FUSION_DEPTH=9: the
+// split was faster for one 1080p RGB frame (0.199 against 0.220 ms) and for
+// eight (1.338 against 1.586 ms), with the same bytes.
+int GB300Processor::acn8Depth() const { return spec_.blocks == 8 && fusionDepth_ != 9 ? 5 : 9; }
+
+cudaError_t GB300Processor::launchAcn8(ThreadState& ts, int depth, int n, const Plane* in, const Plane* out, const Phase2* ph,
+                                       const void* w, bool bf16, int* counter, cudaStream_t stream, int perSm)
+{
+    const ModelParams& mp = model_params(spec_);
+    const int ctas = tc3Ctas_ > 0 ? tc3Ctas_ : smCount_;
+    DeviceBuffer* maps = depth != 9 ? splitMapFor(ts, stream) : nullptr;
+    if (maps)
+    {
+        cudaError_t err = maps->ensure(splitMapBytes(n, in));
+        if (err != cudaSuccess) return err;
+        return launch_acnet8_tc4_split(mp.biases.data(), mp.alphas.data(), spec_.blocks, w, bf16, n, in, out, ph, maps->ptr,
+                                       counter, ctas, stream, perSm);
+    }
+    return launch_acnet8_tc4(mp.biases.data(), mp.alphas.data(), spec_.blocks, w, bf16, n, in, out, ph, counter, ctas, stream,
+                             perSm);
 }
 
 DeviceBuffer* GB300Processor::splitMapFor(ThreadState& ts, cudaStream_t stream)
@@ -1333,7 +1357,14 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
             const Phase2* php = in[0].channels > 1 ? &ph : nullptr;
             bool ran = false;
             Tc3Plan plan;
-            if (acn8) plan.perSm = tc3PerSm_ > 0 ? tc3PerSm_ : 2;  // one tile shape per ACNet<8> depth
+            if (acn8)
+            {
+                plan.perSm = tc3PerSm_ > 0 ? tc3PerSm_ : 2;  // one tile shape per ACNet<8> depth
+                plan.depth = acn8Depth();
+                if (plan.depth != 9 && (err = splitMapFor(ts, s) ? splitMapFor(ts, s)->ensure(splitMapBytes(m, in))
+                                                                 : cudaErrorMemoryAllocation) != cudaSuccess)
+                    return fail(ts, "device allocation", err), false;
+            }
             else plan = tc3Plan(m, in, out, php, w, bf16, counter, s, ran, err, quad, splitMapFor(ts, s));
             if (err != cudaSuccess) return fail(ts, "batched upscale", err), false;
             // the split network's maps exist before a capture begins
@@ -1352,12 +1383,7 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
             mix(static_cast<uint64_t>(quad));
             const int ctas = tc3Ctas_ > 0 ? tc3Ctas_ : smCount_;
             auto launchGroup = [&]() {
-                if (acn8)
-                {
-                    const ModelParams& mp = model_params(spec_);
-                    return launch_acnet8_tc4(mp.biases.data(), mp.alphas.data(), spec_.blocks, w, bf16, m, in, out, php,
-                                             counter, ctas, s, plan.perSm);
-                }
+                if (acn8) return launchAcn8(ts, plan.depth, m, in, out, php, w, bf16, counter, s, plan.perSm);
                 return quad ? launchQuad(ts, plan, m, in, out, php, w, bf16, counter, s)
                             : launch_acnet_legacy_tc3(*acnet_, w, bf16, m, in, out, php, counter, ctas, s, plan.shape,
                                                       plan.perSm);
@@ -1396,7 +1422,7 @@ bool GB300Processor::batchRun(ThreadState& ts, int n, const DeviceImage* src, co
                 counter = ge.counters;  // launchGroup reads `counter`
                 const cudaError_t lerr = launchGroup();
                 counter = ringCounter;
-                ge.kernels = quad && !acn8 && plan.depth == 5 ? 2 : 1;  // the split network: two kernels
+                ge.kernels = plan.depth != 9 && (quad || acn8) ? 2 : 1;  // the split network: two kernels
                 err = cudaStreamEndCapture(s, &ge.graph);
                 if (lerr != cudaSuccess || err != cudaSuccess)
                 {

@@ -210,6 +210,11 @@ private:
     cudaError_t launchQuad(ThreadState& ts, const Tc3Plan& plan, int n, const Plane* in, const Plane* out,
                            const Phase2* ph, const void* w, bool bf16, int* counter, cudaStream_t stream);
     static size_t splitMapBytes(int n, const Plane* in);
+    // ACNet<8> in the quad kernel: the whole network (depth 9) or, for B8,
+    // split in two launches at layer 5 (depth 5, AC_GB300_FUSION_DEPTH=5)
+    int acn8Depth() const;
+    cudaError_t launchAcn8(ThreadState& ts, int depth, int n, const Plane* in, const Plane* out, const Phase2* ph,
+                           const void* w, bool bf16, int* counter, cudaStream_t stream, int perSm);
     // The split network's map buffer of `stream` (null when the thread
     // already holds buffers for 16 other streams: the split is then not used).
     static DeviceBuffer* splitMapFor(ThreadState& ts, cudaStream_t stream);

@@ -68,9 +68,10 @@ AC_C_API int ac_gb300_process_batch_device(ACProcessor* processor, int count, co
  * pair kernel), 5 (the quad kernel, ACNet<8>) or 0 (no such launch yet);
  * *tile_w x *tile_h its tile shape; *ctas_per_sm the CTAs-per-SM cap;
  * *fusion_depth (may be NULL) the layers one launch runs: 9 for the whole
- * network in one launch, 5 for the network split in two launches (layers
- * 0-4 in 54x54 tiles writing a 16-bit activation map, then layers 5-8 and
- * the colour epilogue in the reported 46x57 tiles).  The plan is the
+ * network in one launch, 5 for the network split in two launches at layer 5
+ * (the first launch writes a 16-bit activation map, the second runs the
+ * rest and the colour epilogue in the reported tiles: 46x57 for
+ * ACNetLegacy, 44x60 for ACNet<8> B8, which runs split by default).  The plan is the
  * autotuner's choice for the call's batch class, measured the first time
  * the class was seen, or the one the environment forced (AC_GB300_TC3_SHAPE,
  * AC_GB300_TC3_PER_SM, AC_GB300_FUSION_DEPTH).  Returns AC_SUCCESS or

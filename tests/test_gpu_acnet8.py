@@ -186,3 +186,36 @@ def test_acnet8_quad_close_to_layer_pair_form(monkeypatch):
     monkeypatch.setenv("AC_GB300_TC_KERNEL", "3")
     pair = run("acnet-f8b8-hdn", x, 2.0, "fp16")
     assert np.abs(quad.astype(int) - pair.astype(int)).max() <= 2
+
+
+@pytest.mark.parametrize("form", ["fp16", "bf16"])
+@pytest.mark.parametrize("c", [1, 3, 4])
+@pytest.mark.parametrize("dtype", ["uint8", "uint16", "float32"])
+def test_acnet8_b8_split_gives_identical_bytes(form, c, dtype, monkeypatch):
+    """ACNet<8> B8 split in two quad-kernel launches at layer 5 (the head
+    stores block 4's activations after PReLU in a 16-bit map) against the
+    whole network in one launch: the same bytes, one image and a batch of
+    sizes with tiles at every edge and images smaller than a tile."""
+    torch = pytest.importorskip("torch")
+    sizes = [(131, 150), (1, 1), (7, 93), (54, 52), (200, 45)]
+    imgs = []
+    for h, w in sizes:
+        x = synthetic.rgb_u8(h, w, seed=h + w, alpha=(c == 4)) if c > 1 else synthetic.luma(h, w, np.uint8, seed=h + w)
+        if dtype == "uint16":
+            x = (x.astype(np.uint16) * 257).astype(np.uint16)
+        elif dtype == "float32":
+            x = (x.astype(np.float32) / 255.0).astype(np.float32)
+        imgs.append(np.ascontiguousarray(x))
+    srcs = [torch.from_numpy(x).cuda() for x in imgs]
+    outs = {}
+    for depth in ("9", "5"):
+        monkeypatch.setenv("AC_GB300_FUSION_DEPTH", depth)
+        p = ac.Processor("cuda", 0, "acnet-f8b8-hdn", precision=form)
+        single = torch.empty((2 * sizes[0][0], 2 * sizes[0][1]) + imgs[0].shape[2:], dtype=srcs[0].dtype, device="cuda")
+        p.process_device(srcs[0], single, 2.0)
+        dsts = [torch.empty((2 * s.shape[0], 2 * s.shape[1]) + tuple(s.shape[2:]), dtype=s.dtype, device="cuda") for s in srcs]
+        p.process_batch_device(srcs, dsts, 2.0)
+        assert p.ok(), p.error()
+        outs[depth] = [single.cpu().numpy()] + [d.cpu().numpy() for d in dsts]
+    for a, b in zip(outs["9"], outs["5"]):
+        assert np.array_equal(a, b)
