@@ -13,30 +13,6 @@
 
 namespace acgb {
 
-// RGB(A) pixel -> quantised Y and UV(A) of the same element type.
-template <typename T, int C>
-__device__ __forceinline__ void rgb_to_yuv_q(const T* in, T& yq, T* uvq)
-{
-    float r = to_float<T>(in[0]);
-    float g = to_float<T>(in[1]);
-    float b = to_float<T>(in[2]);
-    float a = 1.0f;
-    if constexpr (C == 4)
-    {
-        a = to_float<T>(in[3]);
-        r = __fmul_rn(r, a);
-        g = __fmul_rn(g, a);
-        b = __fmul_rn(b, a);
-    }
-    const float yy = __fadd_rn(__fadd_rn(__fmul_rn(0.299f, r), __fmul_rn(0.587f, g)), __fmul_rn(0.114f, b));
-    const float u = __fadd_rn(__fmul_rn(0.564f, __fsub_rn(b, yy)), 0.5f);
-    const float v = __fadd_rn(__fmul_rn(0.713f, __fsub_rn(r, yy)), 0.5f);
-    yq = from_float<T>(yy);
-    uvq[0] = from_float<T>(u);
-    uvq[1] = from_float<T>(v);
-    if constexpr (C == 4) uvq[2] = from_float<T>(a);
-}
-
 // yuv2rgb on normalised inputs; writes C channels.
 template <typename T, int C>
 __device__ __forceinline__ void yuv_to_rgb_store(float yy, float u, float v, float a, T* out)
@@ -324,59 +300,6 @@ __device__ __forceinline__ void merge_block2_hv(const float* H, int hpitch, int 
             yuv_to_rgb_store<T, C>(to_float_lut<T>(yq[dy][k], lut), q[0], q[1], C == 4 ? q[2] : 1.0f, px + k * C);
         }
         store_px2<T, C>(dy ? out1 : out0, px, wide);
-    }
-}
-
-// The 2x2 output block of source pixel (cx, cy): luma yq[dy][dx] (already
-// quantised) merged with the chroma of a UV(A) region `uv` (UC channels of
-// type T per pixel, `pitch` pixels per row; (cx, cy) in region coordinates
-// with two pixels of neighbourhood available on every side).  Horizontal
-// sums per source row first (ascending taps), then vertical sums: the same
-// operations, in the same order, as the separable resampler.
-template <typename T, int C>
-__device__ __forceinline__ void merge_block2(const T* uv, int pitch, int cx, int cy, const Phase2& ph, const T (&yq)[2][2],
-                                             T* out0, T* out1)
-{
-    constexpr int UC = C - 1;
-    float h[5][2][UC];
-#pragma unroll
-    for (int rr = 0; rr < 5; rr++)
-    {
-        const T* row = uv + ((cy - 2 + rr) * pitch + (cx - 2)) * UC;
-#pragma unroll
-        for (int c = 0; c < UC; c++)
-        {
-            float d[5];
-#pragma unroll
-            for (int i = 0; i < 5; i++) d[i] = decode_float<T>(row[i * UC + c]);
-#pragma unroll
-            for (int k = 0; k < 2; k++)
-            {
-                float s = 0.0f;
-#pragma unroll
-                for (int t = 0; t < 4; t++) s = __fadd_rn(s, __fmul_rn(ph.w[k][t], d[k + t]));
-                h[rr][k][c] = s;
-            }
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < 2; j++)
-    {
-        T* out = j ? out1 : out0;
-#pragma unroll
-        for (int k = 0; k < 2; k++)
-        {
-            float q[UC];
-#pragma unroll
-            for (int c = 0; c < UC; c++)
-            {
-                float s = 0.0f;
-#pragma unroll
-                for (int t = 0; t < 4; t++) s = __fadd_rn(s, __fmul_rn(ph.w[j][t], h[j + t][k][c]));
-                q[c] = to_float<T>(encode_resampled<T>(s));
-            }
-            yuv_to_rgb_store<T, C>(to_float<T>(yq[j][k]), q[0], q[1], C == 4 ? q[2] : 1.0f, out + k * C);
-        }
     }
 }
 

@@ -205,17 +205,6 @@ struct Params
 };
 static_assert(sizeof(Params) <= 32764, "kernel parameters must fit the 32 KB parameter space");
 
-template <bool BF16>
-__device__ __forceinline__ uint4 pack8_plain(const float* v)
-{
-    if constexpr (BF16)
-        return make_uint4(tc::pack_bf16x2(v[0], v[1]), tc::pack_bf16x2(v[2], v[3]), tc::pack_bf16x2(v[4], v[5]),
-                          tc::pack_bf16x2(v[6], v[7]));
-    else
-        return make_uint4(tc::pack_f16x2(v[0], v[1]), tc::pack_f16x2(v[2], v[3]), tc::pack_f16x2(v[4], v[5]),
-                          tc::pack_f16x2(v[6], v[7]));
-}
-
 // A layer's PReLU slopes as four packed 16-bit pairs (rounded to nearest),
 // converted once per layer.
 template <bool BF16>

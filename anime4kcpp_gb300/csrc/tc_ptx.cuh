@@ -79,15 +79,6 @@ __device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence
 __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // ---- tensor memory loads ----
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
-{
-    uint32_t r[8];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-                 : "r"(taddr));
-#pragma unroll
-    for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
-}
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
 {
     uint32_t r[16];
@@ -101,19 +92,8 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 // Store 16 consecutive 32-bit columns of this thread's tensor-memory lane
-// (warp w reaches lanes 32 (w % 4) .. 32 (w % 4) + 31).
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16])
-{
-    asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};"
-        ::"r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
-          "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])),
-          "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])),
-          "r"(__float_as_uint(v[11])), "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
-          "r"(__float_as_uint(v[15]))
-        : "memory");
-}
-// The same with columns 8..15 a copy of columns 0..7 (8 source registers).
+// (warp w reaches lanes 32 (w % 4) .. 32 (w % 4) + 31), columns 8..15 a
+// copy of columns 0..7 (8 source registers).
 __device__ __forceinline__ void tmem_st16_dup8(uint32_t taddr, const float (&v)[8])
 {
     asm volatile(
@@ -170,14 +150,6 @@ __device__ __forceinline__ uint32_t mbar_try_wait_hint(uint64_t* mbar, uint32_t 
         : "memory");
     return ok;
 }
-// Bounded wait: gives up after `limit` polls and returns false.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mbar, uint32_t phase, uint32_t limit)
-{
-    for (uint32_t i = 0; i < limit; i++)
-        if (mbar_try_wait(mbar, phase)) return true;
-    return false;
-}
-
 __device__ __forceinline__ uint64_t global_timer_ns()
 {
     uint64_t t;
@@ -226,17 +198,6 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const void* tmap, int c, 
         "l"(reinterpret_cast<uint64_t>(tmap)), "r"(c), "r"(x), "r"(y), "r"(smem_u32(mbar))
         : "memory");
 }
-// 2-D tiled tensor store from shared memory (bulk group); x, y >= 0.
-__device__ __forceinline__ void tma_store_2d(const void* tmap, int x, int y, const void* src)
-{
-    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
-                     reinterpret_cast<uint64_t>(tmap)),
-                 "r"(x), "r"(y), "r"(smem_u32(src))
-                 : "memory");
-}
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 // Plain bulk copy global -> shared (16-byte aligned addresses, size multiple of 16).
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* mbar)
 {
