@@ -27,7 +27,7 @@ extern const int kAcnet8Words;
 extern const uint32_t kArtFsrBlob[];
 extern const int kArtFsrWords;
 
-bool parse_model(const char* model, ModelSpec& spec, std::string& error)
+bool parse_model(const char* model, ModelSpec& spec, std::string& /*error*/)
 {
     std::string s = model ? model : "";
     for (char& ch : s) ch = static_cast<char>(std::tolower(static_cast<unsigned char>(ch)));

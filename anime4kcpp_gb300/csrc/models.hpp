@@ -30,7 +30,10 @@ struct ModelSpec
 
 // Parses a model string like core/src/processor/Processor.cpp:26-187 does
 // for every family of the reference (ACNetLegacy, ACNet<8>, ARNet<8>,
-// ArtCNN<16/32>, FSRCNNX<8/16>).
+// ArtCNN<16/32>, FSRCNNX<8/16>).  Like the reference it accepts every
+// string (anything unrecognised is ACNetLegacy GAN), so it returns true and
+// leaves `error` alone; the flag and message stay for the callers' uniform
+// failure path.
 bool parse_model(const char* model, ModelSpec& spec, std::string& error);
 
 struct ModelParams
