@@ -206,6 +206,16 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
                  : "memory");
 }
 
+// 16 bytes global -> shared without registers (both addresses 16-byte
+// aligned), cached in L2 only; cp_async_wait_all() waits for this thread's
+// copies, after which they are visible to it (a barrier then shares them).
+__device__ __forceinline__ void cp_async16(void* dst, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(src))
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // ---- shared-memory counters with release / acquire semantics ----
 __device__ __forceinline__ void smem_add_release(uint32_t* p, uint32_t v)
 {
